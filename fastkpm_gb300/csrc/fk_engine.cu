@@ -1,0 +1,1075 @@
+// fk_engine.cu -- the C ABI of include/fastkpm_gb300.h: engine state, device
+// buffers, launch configuration and the call sequences of moments,
+// stoch_matrix, autodiff_matrix and energy_scale.
+//
+// Device layout and buffer plan (one engine = one Hamiltonian on one device):
+//   R (n x ld, row-major, precision of the engine) and four work vectors V0..V3
+//   of the same shape. moments: a_{m+1} overwrites a_{m-1} in place (the step
+//   kernel reads z and writes y at the same position only), so only two work
+//   vectors rotate. stoch_matrix: two rotating vectors plus xi. autodiff: the
+//   two moment vectors (alpha) plus two beta vectors, all updated in place by
+//   the fused adjoint kernel. No allocation happens inside any recursion.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fastkpm_gb300.h"
+#include "fk_dispatch.h"
+#include "fk_prep.h"
+
+using fk::SysDesc;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes && p) return cudaSuccess;
+        if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+        if (need == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, need);
+        if (e == cudaSuccess) bytes = need;
+        else { p = nullptr; cudaGetLastError(); }
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct KCfg {
+    int Gp = 1, NP = 1, slices = 1, W = 1;   // lanes per row, packets per lane, column slices, packets per slice
+    int stage_cap = 0;
+    size_t smem = 0;
+    int ctas = 1;
+    DevBuf sys, cta_sys;
+    bool valid = false;
+};
+
+struct ProfEvent { int kind; cudaEvent_t a, b; };
+
+int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
+
+}  // namespace
+
+struct fk_engine {
+    int device = 0;
+    int cplx = 0;
+    int prec = fk::kF64;
+    int num_sms = 1;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+
+    // options
+    int opt_fuse_d = 1, opt_np = 0, opt_ctas_per_sm = 0, opt_stage = 1, opt_graphs = 0;
+
+    // H (scaled, augmented with diagonal blocks)
+    int n_b = 0, b = 0, nnzb = 0;
+    double es_lo = 0, es_hi = 0;
+    std::vector<int> h_row_ptr, h_col;
+    DevBuf d_row_ptr, d_colc, d_hval;
+
+    // probes and work vectors
+    int n = 0, s = 0;
+    long long ld = 0;
+    int P = 0;
+    DevBuf d_R, d_V[4];
+
+    // moment state: which buffers hold alpha_{M/2-1}, alpha_{M/2} (-1 = R)
+    int mom_M = 0, mom_a0 = -2, mom_a1 = -2;
+    int pending_M = 0;       // moments enqueued, not yet fetched
+
+    // D pattern cache
+    int d_nb = -1, d_nnzb = -1;
+    std::vector<int> dh_row_ptr, dh_col;
+    bool d_same_as_H = false;
+    bool d_symmetric = false;
+    DevBuf dd_row_ptr, dd_colc, dd_rows, dd_pair, dd_acc;
+
+    // scratch
+    DevBuf d_partials, d_raw, d_coef, d_stage;
+    std::vector<double> h_raw;
+
+    KCfg cfg[fk::kNumKinds];
+
+    // timer
+    cudaEvent_t t_start = nullptr, t_stop = nullptr;
+
+    // profiling
+    bool profiling = false;
+    std::vector<ProfEvent> prof_pending;
+    std::vector<cudaEvent_t> prof_pool;
+    long long prof_launches[fk::kNumKinds] = {0, 0, 0, 0};
+    double prof_ms[fk::kNumKinds] = {0, 0, 0, 0};
+
+    int fail(int code, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t ce, const char* what) {
+        cudaGetLastError();
+        return fail(ce == cudaErrorMemoryAllocation ? FK_ERR_OOM : FK_ERR_CUDA, "%s: %s", what,
+                    cudaGetErrorString(ce));
+    }
+    size_t esize() const { return (size_t)fk::elem_bytes(prec, cplx); }
+    int epp() const { return fk::elems_per_packet(prec, cplx); }
+    size_t hsize() const { return esize(); }   // H entries use the element type
+    size_t vec_bytes() const { return (size_t)n * ld * esize(); }
+    void* V(int id) const { return id < 0 ? d_R.p : d_V[id].p; }
+};
+
+namespace {
+
+#define FK_TRY(expr, what)                                   \
+    do {                                                     \
+        cudaError_t _ce = (expr);                            \
+        if (_ce != cudaSuccess) return e->cuda_fail(_ce, what); \
+    } while (0)
+
+cudaError_t prec_launch_step(fk_engine* e, int NP, const fk::StepArgs& a, const fk::Launch& l) {
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_step_f64(e->cplx, e->b, NP, a, l);
+        case fk::kF32: return fk::launch_step_f32(e->cplx, e->b, NP, a, l);
+        default: return fk::launch_step_ds(e->cplx, e->b, NP, a, l);
+    }
+}
+cudaError_t prec_launch_adjoint(fk_engine* e, int NP, const fk::AdjArgs& a, const fk::Launch& l) {
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_adjoint_f64(e->cplx, e->b, NP, a, l);
+        case fk::kF32: return fk::launch_adjoint_f32(e->cplx, e->b, NP, a, l);
+        default: return fk::launch_adjoint_ds(e->cplx, e->b, NP, a, l);
+    }
+}
+cudaError_t prec_launch_outer(fk_engine* e, int NP, const fk::OuterArgs& a, const fk::Launch& l) {
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_outer_f64(e->cplx, e->b, NP, a, l);
+        case fk::kF32: return fk::launch_outer_f32(e->cplx, e->b, NP, a, l);
+        default: return fk::launch_outer_ds(e->cplx, e->b, NP, a, l);
+    }
+}
+cudaError_t prec_occupancy(fk_engine* e, int kind, int NP, size_t smem, int* n) {
+    switch (e->prec) {
+        case fk::kF64: return fk::occupancy_f64(kind, e->cplx, e->b, NP, smem, n);
+        case fk::kF32: return fk::occupancy_f32(kind, e->cplx, e->b, NP, smem, n);
+        default: return fk::occupancy_ds(kind, e->cplx, e->b, NP, smem, n);
+    }
+}
+cudaError_t prec_load_colmajor(fk_engine* e, const double* src, long long n, int ncols, int c0, void* dst) {
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_load_colmajor_f64(e->cplx, src, n, ncols, c0, e->ld, dst, e->stream);
+        case fk::kF32: return fk::launch_load_colmajor_f32(e->cplx, src, n, ncols, c0, e->ld, dst, e->stream);
+        default: return fk::launch_load_colmajor_ds(e->cplx, src, n, ncols, c0, e->ld, dst, e->stream);
+    }
+}
+cudaError_t prec_store_colmajor(fk_engine* e, const void* src, long long n, int ncols, double* dst) {
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_store_colmajor_f64(e->cplx, src, n, ncols, e->ld, dst, e->stream);
+        case fk::kF32: return fk::launch_store_colmajor_f32(e->cplx, src, n, ncols, e->ld, dst, e->stream);
+        default: return fk::launch_store_colmajor_ds(e->cplx, src, n, ncols, e->ld, dst, e->stream);
+    }
+}
+// ---- profiling ----
+cudaEvent_t prof_event(fk_engine* e) {
+    if (!e->prof_pool.empty()) { cudaEvent_t ev = e->prof_pool.back(); e->prof_pool.pop_back(); return ev; }
+    cudaEvent_t ev;
+    cudaEventCreate(&ev);
+    return ev;
+}
+struct ProfScope {
+    fk_engine* e; int kind; cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(fk_engine* e_, int k) : e(e_), kind(k) {
+        if (e->profiling) { a = prof_event(e); b = prof_event(e); cudaEventRecord(a, e->stream); }
+    }
+    ~ProfScope() {
+        if (e->profiling) { cudaEventRecord(b, e->stream); e->prof_pending.push_back({kind, a, b}); }
+    }
+};
+cudaError_t prec_scale(fk_engine* e, const void* x, void* y, double c) {
+    const long long ne = (long long)e->n * e->ld;
+    ProfScope ps(e, fk::kHelper);
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_scale_f64(e->cplx, x, y, ne, c, e->stream);
+        case fk::kF32: return fk::launch_scale_f32(e->cplx, x, y, ne, c, e->stream);
+        default: return fk::launch_scale_ds(e->cplx, x, y, ne, c, e->stream);
+    }
+}
+void prof_flush(fk_engine* e) {
+    for (auto& p : e->prof_pending) {
+        float ms = 0.f;
+        cudaEventSynchronize(p.b);
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        e->prof_launches[p.kind] += 1;
+        e->prof_ms[p.kind] += ms;
+        e->prof_pool.push_back(p.a);
+        e->prof_pool.push_back(p.b);
+    }
+    e->prof_pending.clear();
+}
+
+// ---- launch configuration ----
+int configure(fk_engine* e) {
+    for (auto& c : e->cfg) c.valid = false;
+    if (e->n_b == 0 || e->s == 0 || e->n != e->n_b * e->b) return FK_OK;   // configured once both are set
+    const int P = e->P;
+    int NP = 1, Gp = 1, slices = 1, W = P;
+    const int npmax = e->opt_np > 0 ? e->opt_np : 4;
+    if (P <= 32) {
+        Gp = next_pow2(P);
+        NP = 1;
+    } else {
+        Gp = 32;
+        NP = (P + 31) / 32;
+        if (NP > npmax) {
+            W = 32 * npmax;
+            slices = (P + W - 1) / W;
+            NP = npmax;
+        } else {
+            NP = NP <= 1 ? 1 : NP <= 2 ? 2 : 4;
+            if (NP > npmax) NP = npmax;
+            W = 32 * NP;
+            slices = (P + W - 1) / W;
+        }
+    }
+    if (e->opt_np > 0 && P <= 32) NP = 1;
+    if (slices == 1) W = P;
+    // H blocks per tile of kThreads items: the shared-memory stage size
+    const long long items = (long long)e->n_b * Gp;
+    const long long tiles = (items + fk::kThreads - 1) / fk::kThreads;
+    const int nk_max = fk::max_tile_blocks(e->h_row_ptr.data(), e->n_b, Gp);
+    const size_t per_blk = (size_t)e->b * e->b * e->hsize() + sizeof(unsigned);
+    int stage_cap = (e->opt_stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
+    for (int kind = 0; kind < fk::kHelper; kind++) {
+        KCfg& c = e->cfg[kind];
+        c.Gp = Gp; c.NP = NP; c.slices = slices; c.W = W;
+        c.stage_cap = kind == fk::kOuter ? 0 : stage_cap;
+        c.smem = c.stage_cap ? ((size_t)c.stage_cap * per_blk + 15) / 16 * 16 : 0;
+        int occ = 0;
+        FK_TRY(prec_occupancy(e, kind, NP, c.smem, &occ), "occupancy query");
+        if (occ < 1) return e->fail(FK_ERR_UNSUPPORTED, "kernel kind %d does not fit on an SM", kind);
+        if (e->opt_ctas_per_sm > 0) occ = std::min(occ, e->opt_ctas_per_sm);
+        c.ctas = (int)std::max<long long>(1, std::min<long long>(tiles, (long long)occ * e->num_sms));
+        SysDesc sd{0, e->n_b, 0, c.ctas};
+        FK_TRY(c.sys.ensure(sizeof(SysDesc)), "alloc sys table");
+        FK_TRY(cudaMemcpy(c.sys.p, &sd, sizeof sd, cudaMemcpyHostToDevice), "upload sys table");
+        FK_TRY(c.cta_sys.ensure(sizeof(int) * c.ctas), "alloc cta table");
+        FK_TRY(cudaMemset(c.cta_sys.p, 0, sizeof(int) * c.ctas), "clear cta table");
+        c.valid = true;
+    }
+    return FK_OK;
+}
+
+int require_ready(fk_engine* e) {
+    if (e->n_b == 0) return e->fail(FK_ERR_STATE, "set_H has not been called");
+    if (e->s == 0) return e->fail(FK_ERR_STATE, "R has not been set");
+    if (e->n != e->n_b * e->b)
+        return e->fail(FK_ERR_ARG, "R has %d rows but H has %d scalar rows", e->n, e->n_b * e->b);
+    if (!e->cfg[0].valid) {
+        int rc = configure(e);
+        if (rc != FK_OK) return rc;
+    }
+    return FK_OK;
+}
+
+// One Chebyshev step over every column slice: y = (two?2:1) Hs x - z, optional dots / xi.
+int run_step(fk_engine* e, const void* x, const void* z, void* y, bool two, bool want_dots, int xi_mode, void* xi,
+             const double* coef_dev, double* partials_step) {
+    const KCfg& c = e->cfg[fk::kStep];
+    const size_t es = e->esize();
+    for (int sl = 0; sl < c.slices; sl++) {
+        const long long off = (long long)sl * c.W * e->epp();   // element offset of this slice
+        fk::StepArgs a;
+        a.sys = c.sys.as<SysDesc>();
+        a.cta_sys = c.cta_sys.as<int>();
+        a.Gp = c.Gp;
+        a.P = std::min(c.W, e->P - sl * c.W);
+        a.ld = e->ld;
+        a.row_ptr = e->d_row_ptr.as<int>();
+        a.colc = e->d_colc.as<unsigned>();
+        a.hval = e->d_hval.p;
+        a.x = (const char*)x + off * es;
+        a.z = z ? (const char*)z + off * es : nullptr;
+        a.y = (char*)y + off * es;
+        a.xi = xi ? (char*)xi + off * es : nullptr;
+        a.coef = coef_dev;
+        a.cstride = 2;
+        a.two = two; a.has_z = z != nullptr; a.want_dots = want_dots; a.xi_mode = xi_mode;
+        a.partials = want_dots ? partials_step + (size_t)sl * c.ctas * 2 : nullptr;
+        a.stage_cap = c.stage_cap;
+        ProfScope ps(e, fk::kStep);
+        FK_TRY(prec_launch_step(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "step kernel launch");
+    }
+    return FK_OK;
+}
+
+int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp, const double* coef_dev, double* Dacc) {
+    const KCfg& c = e->cfg[fk::kAdjoint];
+    const size_t es = e->esize();
+    for (int sl = 0; sl < c.slices; sl++) {
+        const long long off = (long long)sl * c.W * e->epp();
+        fk::AdjArgs a;
+        a.sys = c.sys.as<SysDesc>();
+        a.cta_sys = c.cta_sys.as<int>();
+        a.Gp = c.Gp;
+        a.P = std::min(c.W, e->P - sl * c.W);
+        a.ld = e->ld;
+        a.row_ptr = e->d_row_ptr.as<int>();
+        a.colc = e->d_colc.as<unsigned>();
+        a.hval = e->d_hval.p;
+        a.A = (const char*)A + off * es;
+        a.Ap = (char*)Ap + off * es;
+        a.Bv = (const char*)Bv + off * es;
+        a.Bp = (char*)Bp + off * es;
+        a.coef = coef_dev;
+        a.cstride = 3;
+        a.Dacc = Dacc;
+        a.dscale = 2.0;
+        a.stage_cap = c.stage_cap;
+        ProfScope ps(e, fk::kAdjoint);
+        FK_TRY(prec_launch_adjoint(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "adjoint kernel launch");
+    }
+    return FK_OK;
+}
+
+int run_outer(fk_engine* e, const void* A, const void* Bv, double alpha1, double alpha2) {
+    const KCfg& c = e->cfg[fk::kOuter];
+    const size_t es = e->esize();
+    for (int sl = 0; sl < c.slices; sl++) {
+        const long long off = (long long)sl * c.W * e->epp();
+        fk::OuterArgs a;
+        a.sys = c.sys.as<SysDesc>();
+        a.cta_sys = c.cta_sys.as<int>();
+        a.Gp = c.Gp;
+        a.P = std::min(c.W, e->P - sl * c.W);
+        a.ld = e->ld;
+        a.row_ptr = e->dd_row_ptr.as<int>();
+        a.colc = e->dd_colc.as<unsigned>();
+        a.A = (const char*)A + off * es;
+        a.Bv = (const char*)Bv + off * es;
+        a.alpha1 = alpha1;
+        a.alpha2 = alpha2;
+        a.Dacc = e->dd_acc.as<double>();
+        ProfScope ps(e, fk::kOuter);
+        FK_TRY(prec_launch_outer(e, c.NP, a, fk::Launch{c.ctas, 0, e->stream}), "outer kernel launch");
+    }
+    return FK_OK;
+}
+
+int ensure_vectors(fk_engine* e) {
+    const size_t vb = e->vec_bytes();
+    FK_TRY(e->d_R.ensure(vb), "allocate R");
+    for (auto& v : e->d_V) FK_TRY(v.ensure(vb), "allocate work vector");
+    return FK_OK;
+}
+
+int check_pattern(fk_engine* e, int n_b, int nnzb, const int* row_ptr, const int* col_idx, const char* what) {
+    std::string why;
+    const int rc = fk::check_bsr_pattern(n_b, nnzb, row_ptr, col_idx, why);
+    return rc == FK_OK ? FK_OK : e->fail(rc, "%s: %s", what, why.c_str());
+}
+
+// Upload (or reuse) D's pattern. need_pairs: autodiff's symmetrize needs the (j,i) partner of every block.
+int set_D_pattern(fk_engine* e, int d_n_b, int d_nnzb, const int* rp, const int* ci, bool need_pairs) {
+    if (d_n_b != e->n_b) return e->fail(FK_ERR_ARG, "D has %d block rows, H has %d", d_n_b, e->n_b);
+    if (d_nnzb < 0) return e->fail(FK_ERR_ARG, "negative D nnzb");
+    const bool same = d_n_b == e->d_nb && d_nnzb == e->d_nnzb &&
+                      std::equal(rp, rp + d_n_b + 1, e->dh_row_ptr.begin()) &&
+                      (d_nnzb == 0 || std::equal(ci, ci + d_nnzb, e->dh_col.begin()));
+    if (!same) {
+        int rc = check_pattern(e, d_n_b, d_nnzb, rp, ci, "D pattern");
+        if (rc != FK_OK) return rc;
+        e->dh_row_ptr.assign(rp, rp + d_n_b + 1);
+        e->dh_col.assign(ci, ci + d_nnzb);
+        std::vector<int> rows(d_nnzb), pair(d_nnzb, -1);
+        bool sym = true;
+        for (int i = 0; i < d_n_b; i++) {
+            for (int k = rp[i]; k < rp[i + 1]; k++) {
+                rows[k] = i;
+                const int j = ci[k];
+                const int* lo = ci + rp[j];
+                const int* hi = ci + rp[j + 1];
+                const int* f = std::lower_bound(lo, hi, i);
+                if (f != hi && *f == i) pair[k] = (int)(f - ci);
+                else sym = false;
+            }
+        }
+        std::vector<unsigned> colc(ci, ci + d_nnzb);
+        FK_TRY(e->dd_row_ptr.ensure(sizeof(int) * (d_n_b + 1)), "alloc D row_ptr");
+        FK_TRY(e->dd_colc.ensure(sizeof(unsigned) * std::max(d_nnzb, 1)), "alloc D cols");
+        FK_TRY(e->dd_rows.ensure(sizeof(int) * std::max(d_nnzb, 1)), "alloc D rows");
+        FK_TRY(e->dd_pair.ensure(sizeof(int) * std::max(d_nnzb, 1)), "alloc D pairs");
+        FK_TRY(cudaMemcpy(e->dd_row_ptr.p, rp, sizeof(int) * (d_n_b + 1), cudaMemcpyHostToDevice), "upload D row_ptr");
+        if (d_nnzb) {
+            FK_TRY(cudaMemcpy(e->dd_colc.p, colc.data(), sizeof(unsigned) * d_nnzb, cudaMemcpyHostToDevice), "upload D cols");
+            FK_TRY(cudaMemcpy(e->dd_rows.p, rows.data(), sizeof(int) * d_nnzb, cudaMemcpyHostToDevice), "upload D rows");
+            FK_TRY(cudaMemcpy(e->dd_pair.p, pair.data(), sizeof(int) * d_nnzb, cudaMemcpyHostToDevice), "upload D pairs");
+        }
+        e->d_nb = d_n_b;
+        e->d_nnzb = d_nnzb;
+        e->d_symmetric = sym;
+        e->d_same_as_H = d_nnzb == e->nnzb && std::equal(rp, rp + d_n_b + 1, e->h_row_ptr.begin()) &&
+                         std::equal(ci, ci + d_nnzb, e->h_col.begin());
+    }
+    if (need_pairs && !e->d_symmetric)
+        return e->fail(FK_ERR_PATTERN, "D pattern is not symmetric: a block (i,j) has no (j,i) partner");
+    const size_t dbytes = sizeof(double) * (size_t)std::max(d_nnzb, 1) * e->b * e->b * (e->cplx ? 2 : 1);
+    FK_TRY(e->dd_acc.ensure(dbytes), "alloc D accumulator");
+    return FK_OK;
+}
+
+int ensure_coef(fk_engine* e, size_t ndoubles) {
+    FK_TRY(e->d_coef.ensure(sizeof(double) * std::max<size_t>(ndoubles, 1)), "alloc coefficients");
+    return FK_OK;
+}
+
+int ensure_partials(fk_engine* e, int nsteps) {
+    const KCfg& c = e->cfg[fk::kStep];
+    FK_TRY(e->d_partials.ensure(sizeof(double) * 2 * (size_t)nsteps * c.slices * c.ctas), "alloc partials");
+    FK_TRY(e->d_raw.ensure(sizeof(double) * 2 * (size_t)nsteps), "alloc moment sums");
+    return FK_OK;
+}
+
+__global__ void k_reduce_steps(const double* partials, int per_step, double* raw, int nsteps) {
+    // one warp per step: fixed-order sum of per_step (= slices * ctas) CTA partials
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nsteps) return;
+    const double* p = partials + (size_t)w * per_step * 2;
+    double a = 0.0, bsum = 0.0;
+    for (int c = lane; c < per_step; c += 32) { a += p[2 * c]; bsum += p[2 * c + 1]; }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        bsum += __shfl_xor_sync(0xffffffffu, bsum, off);
+    }
+    if (lane == 0) { raw[2 * w] = a; raw[2 * w + 1] = bsum; }
+}
+
+int moments_enqueue(fk_engine* e, int M) {
+    if (M < 2 || M % 2 != 0) return e->fail(FK_ERR_ARG, "moments: M must be even and >= 2 (got %d)", M);
+    int rc = require_ready(e);
+    if (rc != FK_OK) return rc;
+    const int nsteps = M / 2;
+    rc = ensure_partials(e, nsteps);
+    if (rc != FK_OK) return rc;
+    const KCfg& c = e->cfg[fk::kStep];
+    const size_t per_step = (size_t)c.slices * c.ctas * 2;
+    double* part = e->d_partials.as<double>();
+    // step 0: alpha_1 = Hs R; dots <R,R>, Re<alpha_1,R>
+    rc = run_step(e, e->d_R.p, nullptr, e->d_V[0].p, false, true, 0, nullptr, nullptr, part);
+    if (rc != FK_OK) return rc;
+    int x = 0, z = -1;   // x = alpha_m, z = alpha_{m-1}  (-1 = R)
+    for (int m = 1; m < nsteps; m++) {
+        const int y = (z == -1) ? 1 : z;   // never overwrite R
+        rc = run_step(e, e->V(x), e->V(z), e->V(y), true, true, 0, nullptr, nullptr, part + per_step * m);
+        if (rc != FK_OK) return rc;
+        z = x;
+        x = y;
+    }
+    // after the loop: alpha_{M/2-1} in z, alpha_{M/2} in x
+    e->mom_M = M;
+    e->mom_a0 = z;
+    e->mom_a1 = x;
+    {
+        ProfScope ps(e, fk::kHelper);
+        k_reduce_steps<<<(nsteps * 32 + 255) / 256, 256, 0, e->stream>>>(part, (int)(per_step / 2), e->d_raw.as<double>(), nsteps);
+        FK_TRY(cudaGetLastError(), "moment reduction launch");
+    }
+    e->pending_M = M;
+    return FK_OK;
+}
+
+int moments_fetch(fk_engine* e, double* mu) {
+    if (e->pending_M == 0) return e->fail(FK_ERR_STATE, "no moments enqueued");
+    const int M = e->pending_M, nsteps = M / 2;
+    e->h_raw.resize(2 * (size_t)nsteps);
+    FK_TRY(cudaMemcpyAsync(e->h_raw.data(), e->d_raw.p, sizeof(double) * 2 * nsteps, cudaMemcpyDeviceToHost, e->stream),
+           "copy moment sums");
+    FK_TRY(cudaStreamSynchronize(e->stream), "moments");
+    // mu_0 = <a0,a0>, mu_1 = Re<a1,a0>, mu_2m = 2<a_m,a_m> - mu_0, mu_2m+1 = 2 Re<a_m+1,a_m> - mu_1
+    mu[0] = e->h_raw[0];
+    mu[1] = e->h_raw[1];
+    for (int m = 1; m < nsteps; m++) {
+        mu[2 * m] = 2 * e->h_raw[2 * m] - mu[0];
+        mu[2 * m + 1] = 2 * e->h_raw[2 * m + 1] - mu[1];
+    }
+    if (e->profiling) prof_flush(e);
+    return FK_OK;
+}
+
+int stoch_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp, const int* ci) {
+    if (M < 2) return e->fail(FK_ERR_ARG, "stoch_matrix: need at least 2 coefficients (got %d)", M);
+    if (!c) return e->fail(FK_ERR_ARG, "stoch_matrix: null coefficients");
+    int rc = require_ready(e);
+    if (rc != FK_OK) return rc;
+    rc = set_D_pattern(e, d_n_b, d_nnzb, rp, ci, false);
+    if (rc != FK_OK) return rc;
+    rc = ensure_coef(e, 2 * (size_t)M);
+    if (rc != FK_OK) return rc;
+    std::vector<double> coef(2 * (size_t)M, 0.0);
+    coef[0] = c[0];
+    coef[1] = c[1];
+    for (int m = 2; m < M; m++) coef[2 * m + 1] = c[m];
+    FK_TRY(cudaMemcpyAsync(e->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, e->stream),
+           "upload coefficients");
+    const double* cd = e->d_coef.as<double>();
+    void* xi = e->d_V[2].p;
+    // m = 1: alpha_1 = Hs R, xi = c0 R + c1 alpha_1
+    rc = run_step(e, e->d_R.p, nullptr, e->d_V[0].p, false, false, 1, xi, cd, nullptr);
+    if (rc != FK_OK) return rc;
+    int x = 0, z = -1;
+    for (int m = 2; m < M; m++) {
+        const int y = (z == -1) ? 1 : z;
+        rc = run_step(e, e->V(x), e->V(z), e->V(y), true, false, 2, xi, cd + 2 * m, nullptr);
+        if (rc != FK_OK) return rc;
+        z = x;
+        x = y;
+    }
+    // D = (R xi^dag + xi R^dag)/2 on D's pattern
+    const size_t dn = (size_t)d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
+    FK_TRY(cudaMemsetAsync(e->dd_acc.p, 0, sizeof(double) * std::max<size_t>(dn, 1), e->stream), "clear D");
+    if (d_nnzb > 0) {
+        rc = run_outer(e, e->d_R.p, xi, 0.5, 0.5);
+        if (rc != FK_OK) return rc;
+    }
+    e->mom_M = 0;   // the recursion state is no longer the one autodiff needs (reference clears a0, a1)
+    e->mom_a0 = e->mom_a1 = -2;
+    return FK_OK;
+}
+
+int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp, const int* ci) {
+    if (!c) return e->fail(FK_ERR_ARG, "autodiff_matrix: null coefficients");
+    int rc = require_ready(e);
+    if (rc != FK_OK) return rc;
+    if (e->mom_M == 0 || e->mom_M != M)
+        return e->fail(FK_ERR_STATE, "autodiff_matrix(M=%d) needs moments(%d) first (have %d)", M, M, e->mom_M);
+    rc = set_D_pattern(e, d_n_b, d_nnzb, rp, ci, true);
+    if (rc != FK_OK) return rc;
+    const size_t dn = (size_t)d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
+    FK_TRY(cudaMemsetAsync(e->dd_acc.p, 0, sizeof(double) * std::max<size_t>(dn, 1), e->stream), "clear D");
+    double diag = c[1];
+    for (int m = 1; m < M / 2; m++) diag -= c[2 * m + 1];
+    const int nsteps = M / 2 - 1;
+    rc = ensure_coef(e, 3 * (size_t)std::max(nsteps, 1));
+    if (rc != FK_OK) return rc;
+    std::vector<double> coef(3 * (size_t)std::max(nsteps, 1), 0.0);
+    for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
+        coef[3 * q + 0] = 4 * c[2 * m];
+        coef[3 * q + 1] = 2 * c[2 * m + 1];
+        coef[3 * q + 2] = (m > 1) ? 2 * c[2 * m - 1] : diag;   // m = 1 folds diag * R R^dag into beta_1
+    }
+    FK_TRY(cudaMemcpyAsync(e->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, e->stream),
+           "upload coefficients");
+    const bool fuse = e->opt_fuse_d && e->d_same_as_H;
+    // buffers: alpha_m in A, alpha_{m+1} in Ap (moments left alpha_{M/2-1}, alpha_{M/2})
+    int A = e->mom_a0, Ap = e->mom_a1;
+    int freeb[4], nf = 0;
+    for (int q = 0; q < 4; q++) if (q != A && q != Ap) freeb[nf++] = q;
+    int Bv = freeb[0], Bp = freeb[1];
+    if (M > 2) {
+        // beta_{M/2} = 2 c_{M-1} alpha_{M/2-1}, beta_{M/2+1} = 0
+        FK_TRY(prec_scale(e, e->V(A), e->V(Bv), 2 * c[M - 1]), "scale kernel");
+        FK_TRY(cudaMemsetAsync(e->V(Bp), 0, e->vec_bytes(), e->stream), "clear beta");
+        for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
+            if (!fuse && d_nnzb > 0) {
+                rc = run_outer(e, e->V(A), e->V(Bv), 2.0, 0.0);   // D += 2 alpha_m beta_{m+1}^dag
+                if (rc != FK_OK) return rc;
+            }
+            rc = run_adjoint(e, e->V(A), e->V(Ap), e->V(Bv), e->V(Bp), e->d_coef.as<double>() + 3 * q,
+                             fuse ? e->dd_acc.as<double>() : nullptr);
+            if (rc != FK_OK) return rc;
+            std::swap(A, Ap);    // A = alpha_{m-1}, Ap = alpha_m
+            std::swap(Bv, Bp);   // Bv = beta_m,   Bp = beta_{m+1}
+        }
+    } else {
+        // M = 2: D = diag R R^dag = R (diag R)^dag
+        FK_TRY(prec_scale(e, e->V(A), e->V(Bv), diag), "scale kernel");
+    }
+    // D += alpha_0 (beta_1 + diag alpha_0)^dag, then symmetrize and divide by mag
+    if (d_nnzb > 0) {
+        rc = run_outer(e, e->V(A), e->V(Bv), 1.0, 0.0);
+        if (rc != FK_OK) return rc;
+        const double mag = (e->es_hi - e->es_lo) / 2.0;
+        const long long work = (long long)d_nnzb * e->b * e->b;
+        int grid = (int)std::min<long long>((work + 255) / 256, 152LL * 16);
+        ProfScope ps(e, fk::kHelper);
+        fk::k_symmetrize_scale<<<std::max(grid, 1), 256, 0, e->stream>>>(
+            e->dd_acc.as<double>(), e->dd_rows.as<int>(), e->dd_colc.as<int>(), e->dd_pair.as<int>(), d_nnzb, e->b,
+            e->cplx, 1.0 / mag);
+        FK_TRY(cudaGetLastError(), "symmetrize launch");
+    }
+    e->mom_M = 0;   // alpha state consumed (reference zeroes a_d[0..1])
+    e->mom_a0 = e->mom_a1 = -2;
+    return FK_OK;
+}
+
+int fetch_D(fk_engine* e, double* D) {
+    if (e->d_nnzb < 0) return e->fail(FK_ERR_STATE, "no D computed");
+    const size_t dn = (size_t)e->d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
+    if (dn) FK_TRY(cudaMemcpyAsync(D, e->dd_acc.p, sizeof(double) * dn, cudaMemcpyDeviceToHost, e->stream), "copy D");
+    FK_TRY(cudaStreamSynchronize(e->stream), "D calculation");
+    if (e->profiling) prof_flush(e);
+    return FK_OK;
+}
+
+}  // namespace
+
+// ===================================================================================
+// Lanczos energy_scale on the device
+// ===================================================================================
+namespace {
+
+// w <- w - alpha v1 - beta v0 (real or complex doubles), partial |w|^2 per CTA
+__global__ void k_lanczos_update(double* w, const double* v1, const double* v0, long long n_dbl, const double* ab,
+                                 double* part) {
+    const double al = ab[0], be = ab[1];
+    double acc = 0.0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_dbl; q += (long long)gridDim.x * blockDim.x) {
+        const double v = w[q] - al * v1[q] - be * v0[q];
+        w[q] = v;
+        acc += v * v;
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    __shared__ double red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += red[q];
+        part[blockIdx.x] = t;
+    }
+}
+
+}  // namespace
+
+namespace {
+int sturm(int n, const double* a, const double* bt, double x) {
+    int cnt = 0;
+    double q = a[0] - x;
+    if (q < 0) cnt++;
+    for (int j = 1; j < n; j++) {
+        q = a[j] - x - bt[j] * bt[j] / (q == 0 ? 1e-300 : q);
+        if (q < 0) cnt++;
+    }
+    return cnt;
+}
+void tridiag_extremes(int n, const double* a, const double* bt, double* emin, double* emax) {
+    double glo = 1e300, ghi = -1e300;
+    for (int j = 0; j < n; j++) {
+        const double r = (j > 0 ? std::fabs(bt[j]) : 0.0) + (j + 1 < n ? std::fabs(bt[j + 1]) : 0.0);
+        glo = std::min(glo, a[j] - r);
+        ghi = std::max(ghi, a[j] + r);
+    }
+    auto kth = [&](int k) {
+        double l = glo, h = ghi;
+        for (int it = 0; it < 200 && h - l > 1e-15 * std::max(1.0, std::fabs(l) + std::fabs(h)); it++) {
+            const double mid = 0.5 * (l + h);
+            if (sturm(n, a, bt, mid) > k) h = mid; else l = mid;
+        }
+        return 0.5 * (l + h);
+    };
+    *emin = kth(0);
+    *emax = kth(n - 1);
+}
+}  // namespace
+
+// ===================================================================================
+// C ABI
+// ===================================================================================
+extern "C" {
+
+const char* fk_version(void) { return "fastkpm_gb300 0.1 (sm_103a)"; }
+
+const char* fk_status_string(int s) {
+    switch (s) {
+        case FK_OK: return "ok";
+        case FK_ERR_ARG: return "invalid argument";
+        case FK_ERR_OOM: return "out of device memory";
+        case FK_ERR_PATTERN: return "malformed sparsity pattern";
+        case FK_ERR_TIMEOUT: return "timeout";
+        case FK_ERR_CUDA: return "CUDA error";
+        case FK_ERR_STATE: return "invalid call order";
+        case FK_ERR_NODEV: return "no CUDA device";
+        case FK_ERR_UNSUPPORTED: return "unsupported";
+        default: return "unknown status";
+    }
+}
+
+int fk_device_count(int* count) {
+    if (!count) return FK_ERR_ARG;
+    int c = 0;
+    cudaError_t ce = cudaGetDeviceCount(&c);
+    if (ce != cudaSuccess) { cudaGetLastError(); *count = 0; return FK_ERR_NODEV; }
+    *count = c;
+    return FK_OK;
+}
+
+int fk_engine_create(int device, int kind, int precision, fk_engine** out) {
+    if (!out) return FK_ERR_ARG;
+    *out = nullptr;
+    if (kind != FK_REAL && kind != FK_COMPLEX) return FK_ERR_ARG;
+    if (precision < FK_PREC_FP64 || precision > FK_PREC_DS) return FK_ERR_ARG;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) { cudaGetLastError(); return FK_ERR_NODEV; }
+    if (device < 0 || device >= count) return FK_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return FK_ERR_CUDA; }
+    fk_engine* e = new fk_engine();
+    e->device = device;
+    e->cplx = kind;
+    e->prec = precision;
+    cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete e;
+        return FK_ERR_CUDA;
+    }
+    e->own_stream = true;
+    *out = e;
+    return FK_OK;
+}
+
+int fk_engine_destroy(fk_engine* e) {
+    if (!e) return FK_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    for (auto& p : e->prof_pending) { e->prof_pool.push_back(p.a); e->prof_pool.push_back(p.b); }
+    for (auto ev : e->prof_pool) cudaEventDestroy(ev);
+    if (e->t_start) cudaEventDestroy(e->t_start);
+    if (e->t_stop) cudaEventDestroy(e->t_stop);
+    DevBuf* bufs[] = {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2], &e->d_V[3],
+                      &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc, &e->d_partials, &e->d_raw,
+                      &e->d_coef, &e->d_stage};
+    for (auto* b : bufs) b->release();
+    for (auto& c : e->cfg) { c.sys.release(); c.cta_sys.release(); }
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return FK_OK;
+}
+
+const char* fk_engine_last_error(const fk_engine* e) { return e ? e->err.c_str() : "null engine"; }
+
+int fk_engine_set_stream(fk_engine* e, void* st) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    if (e->own_stream && e->stream) { cudaStreamSynchronize(e->stream); cudaStreamDestroy(e->stream); }
+    if (st) { e->stream = (cudaStream_t)st; e->own_stream = false; }
+    else {
+        if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) return e->fail(FK_ERR_CUDA, "stream create");
+        e->own_stream = true;
+    }
+    return FK_OK;
+}
+
+int fk_engine_synchronize(fk_engine* e) {
+    if (!e) return FK_ERR_ARG;
+    FK_TRY(cudaStreamSynchronize(e->stream), "synchronize");
+    return FK_OK;
+}
+
+int fk_engine_set_option(fk_engine* e, int option, int value) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    switch (option) {
+        case FK_OPT_FUSE_D: e->opt_fuse_d = value ? 1 : 0; return FK_OK;
+        case FK_OPT_NP:
+            if (value != 0 && value != 1 && value != 2 && value != 4) return e->fail(FK_ERR_ARG, "NP must be 0, 1, 2 or 4");
+            e->opt_np = value; return configure(e);
+        case FK_OPT_CTAS_PER_SM:
+            if (value < 0) return e->fail(FK_ERR_ARG, "negative CTA cap");
+            e->opt_ctas_per_sm = value; return configure(e);
+        case FK_OPT_STAGE_H: e->opt_stage = value ? 1 : 0; return configure(e);
+        case FK_OPT_GRAPHS: e->opt_graphs = value ? 1 : 0; return FK_OK;
+        default: return e->fail(FK_ERR_ARG, "unknown option %d", option);
+    }
+}
+
+int fk_engine_get_option(const fk_engine* e, int option, int* value) {
+    if (!e || !value) return FK_ERR_ARG;
+    switch (option) {
+        case FK_OPT_FUSE_D: *value = e->opt_fuse_d; return FK_OK;
+        case FK_OPT_NP: *value = e->cfg[0].valid ? e->cfg[0].NP : e->opt_np; return FK_OK;
+        case FK_OPT_CTAS_PER_SM: *value = e->opt_ctas_per_sm; return FK_OK;
+        case FK_OPT_STAGE_H: *value = e->opt_stage; return FK_OK;
+        case FK_OPT_GRAPHS: *value = e->opt_graphs; return FK_OK;
+        default: return FK_ERR_ARG;
+    }
+}
+
+int fk_engine_set_H(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx, const double* val,
+                    double es_lo, double es_hi) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    if (n_b > (int)fk::kColMask) return e->fail(FK_ERR_UNSUPPORTED, "set_H: too many block rows");
+    fk::PreparedH ph;
+    std::string why;
+    int rc = fk::prepare_H(e->prec, e->cplx, n_b, b, nnzb, row_ptr, col_idx, val, es_lo, es_hi, 0, ph, why);
+    if (rc != FK_OK) return e->fail(rc, "set_H: %s", why.c_str());
+    const int nk = (int)ph.col.size();
+    FK_TRY(e->d_row_ptr.ensure(sizeof(int) * (n_b + 1)), "alloc H row_ptr");
+    FK_TRY(e->d_colc.ensure(sizeof(unsigned) * std::max(nk, 1)), "alloc H columns");
+    FK_TRY(e->d_hval.ensure(std::max<size_t>(ph.hval.size(), 16)), "alloc H values");
+    FK_TRY(cudaMemcpy(e->d_row_ptr.p, ph.row_ptr.data(), sizeof(int) * (n_b + 1), cudaMemcpyHostToDevice), "upload H row_ptr");
+    FK_TRY(cudaMemcpy(e->d_colc.p, ph.colc.data(), sizeof(unsigned) * nk, cudaMemcpyHostToDevice), "upload H columns");
+    FK_TRY(cudaMemcpy(e->d_hval.p, ph.hval.data(), ph.hval.size(), cudaMemcpyHostToDevice), "upload H values");
+    e->n_b = n_b;
+    e->b = b;
+    e->nnzb = nk;
+    e->es_lo = es_lo;
+    e->es_hi = es_hi;
+    e->h_row_ptr.swap(ph.row_ptr);
+    e->h_col.swap(ph.col);
+    e->mom_M = 0;
+    e->mom_a0 = e->mom_a1 = -2;
+    e->d_nb = -1;   // D pattern comparison against H must be redone
+    e->d_nnzb = -1;
+    return configure(e);
+}
+
+int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    if (n <= 0) return e->fail(FK_ERR_ARG, "set_R: n must be positive");
+    if (s <= 0) return e->fail(FK_ERR_ARG, "set_R: cannot handle an empty R (s = %d)", s);
+    if (!R) return e->fail(FK_ERR_ARG, "set_R: null R");
+    const int epp = e->epp();
+    e->n = n;
+    e->s = s;
+    e->ld = ((long long)s + epp - 1) / epp * epp;
+    e->P = (int)(e->ld / epp);
+    int rc = ensure_vectors(e);
+    if (rc != FK_OK) return rc;
+    FK_TRY(cudaMemsetAsync(e->d_R.p, 0, e->vec_bytes(), e->stream), "clear R");
+    for (auto& v : e->d_V) FK_TRY(cudaMemsetAsync(v.p, 0, e->vec_bytes(), e->stream), "clear work vector");
+    // upload in column chunks of at most ~256 MiB through a staging buffer
+    const size_t col_bytes = sizeof(double) * (size_t)n * (e->cplx ? 2 : 1);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)s, (256u << 20) / col_bytes));
+    FK_TRY(e->d_stage.ensure(col_bytes * chunk), "alloc staging buffer");
+    for (int c0 = 0; c0 < s; c0 += chunk) {
+        const int nc = std::min(chunk, s - c0);
+        FK_TRY(cudaMemcpyAsync(e->d_stage.p, (const char*)R + col_bytes * c0, col_bytes * nc, cudaMemcpyHostToDevice,
+                               e->stream), "upload R");
+        ProfScope ps(e, fk::kHelper);
+        FK_TRY(prec_load_colmajor(e, e->d_stage.as<double>(), n, nc, c0, e->d_R.p), "R layout kernel");
+    }
+    FK_TRY(cudaStreamSynchronize(e->stream), "set_R");
+    e->mom_M = 0;
+    e->mom_a0 = e->mom_a1 = -2;
+    return configure(e);
+}
+
+int fk_engine_get_R(fk_engine* e, double* R) {
+    if (!e || !R) return FK_ERR_ARG;
+    if (e->s == 0) return e->fail(FK_ERR_STATE, "R has not been set");
+    cudaSetDevice(e->device);
+    const size_t bytes = sizeof(double) * (size_t)e->n * e->s * (e->cplx ? 2 : 1);
+    DevBuf tmp;
+    FK_TRY(tmp.ensure(bytes), "alloc readback buffer");
+    cudaError_t ce = prec_store_colmajor(e, e->d_R.p, e->n, e->s, tmp.as<double>());
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(R, tmp.p, bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    tmp.release();
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "read back R");
+    return FK_OK;
+}
+
+int fk_engine_moments(fk_engine* e, int M, double* mu) {
+    if (!e || !mu) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    int rc = moments_enqueue(e, M);
+    if (rc != FK_OK) return rc;
+    return moments_fetch(e, mu);
+}
+int fk_engine_moments_async(fk_engine* e, int M) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    return moments_enqueue(e, M);
+}
+int fk_engine_fetch_moments(fk_engine* e, double* mu) {
+    if (!e || !mu) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    return moments_fetch(e, mu);
+}
+
+int fk_engine_stoch_matrix(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp, const int* ci,
+                           double* D) {
+    if (!e || (!D && d_nnzb > 0)) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    int rc = stoch_enqueue(e, M, c, d_n_b, d_nnzb, rp, ci);
+    if (rc != FK_OK) return rc;
+    return fetch_D(e, D);
+}
+int fk_engine_stoch_matrix_async(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp,
+                                 const int* ci) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    return stoch_enqueue(e, M, c, d_n_b, d_nnzb, rp, ci);
+}
+int fk_engine_autodiff_matrix(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp,
+                              const int* ci, double* D) {
+    if (!e || (!D && d_nnzb > 0)) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    int rc = autodiff_enqueue(e, M, c, d_n_b, d_nnzb, rp, ci);
+    if (rc != FK_OK) return rc;
+    return fetch_D(e, D);
+}
+int fk_engine_autodiff_matrix_async(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp,
+                                    const int* ci) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    return autodiff_enqueue(e, M, c, d_n_b, d_nnzb, rp, ci);
+}
+int fk_engine_fetch_D(fk_engine* e, double* D) {
+    if (!e || !D) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    return fetch_D(e, D);
+}
+
+int fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
+                           const double* val, double extend, int iters, const double* v0, double* lo, double* hi) {
+    if (!e || !lo || !hi) return FK_ERR_ARG;
+    if (iters < 1) return e->fail(FK_ERR_ARG, "energy_scale: iters must be >= 1");
+    cudaSetDevice(e->device);
+    // A scratch FP64 engine holds H unscaled (es = [-1, 1] makes Hs = H) and one probe column.
+    fk_engine* t = nullptr;
+    int rc = fk_engine_create(e->device, e->cplx, FK_PREC_FP64, &t);
+    if (rc != FK_OK) return e->fail(rc, "energy_scale: scratch engine");
+    struct Guard { fk_engine* t; ~Guard() { fk_engine_destroy(t); } } guard{t};
+    rc = fk_engine_set_H(t, n_b, b, nnzb, row_ptr, col_idx, val, -1.0, 1.0);
+    if (rc != FK_OK) return e->fail(rc, "energy_scale: %s", t->err.c_str());
+    const int n = n_b * b, cw = e->cplx ? 2 : 1;
+    std::vector<double> v(static_cast<size_t>(n) * cw);
+    if (v0) std::copy(v0, v0 + v.size(), v.begin());
+    else {
+        // seeded Gaussian start vector (the reference draws arma::randn)
+        unsigned long long st = 0x9e3779b97f4a7c15ull;
+        auto u01 = [&]() { st = st * 6364136223846793005ull + 1442695040888963407ull; return ((st >> 11) + 0.5) / 9007199254740992.0; };
+        for (auto& x : v) x = std::sqrt(-2.0 * std::log(u01())) * std::cos(6.283185307179586 * u01());
+    }
+    double nrm = 0;
+    for (double x : v) nrm += x * x;
+    nrm = std::sqrt(nrm);
+    for (auto& x : v) x /= nrm;
+    rc = fk_engine_set_R(t, n, 1, v.data());
+    if (rc != FK_OK) return e->fail(rc, "energy_scale: %s", t->err.c_str());
+    rc = require_ready(t);
+    if (rc != FK_OK) return e->fail(rc, "energy_scale: %s", t->err.c_str());
+    // vectors: v1 = R buffer copy in V0 (we keep R intact), v0 in V1, w in V2; stride ld (padded) doubles
+    const size_t vb = t->vec_bytes();
+    FK_TRY(cudaMemcpyAsync(t->d_V[0].p, t->d_R.p, vb, cudaMemcpyDeviceToDevice, t->stream), "lanczos init");
+    FK_TRY(cudaMemsetAsync(t->d_V[1].p, 0, vb, t->stream), "lanczos init");
+    const long long n_dbl = (long long)vb / sizeof(double);
+    DevBuf ab, part;
+    const int ugrid = 152 * 4;
+    FK_TRY(ab.ensure(2 * sizeof(double)), "lanczos scalars");
+    FK_TRY(part.ensure(sizeof(double) * std::max(ugrid, 2 * t->cfg[fk::kStep].ctas * t->cfg[fk::kStep].slices)), "lanczos partials");
+    std::vector<double> alpha(iters), beta(iters), hp(std::max(ugrid, 2 * t->cfg[fk::kStep].ctas * t->cfg[fk::kStep].slices));
+    beta[0] = 0;
+    int v1 = 0, vz = 1, w = 2;
+    const int pcount = 2 * t->cfg[fk::kStep].ctas * t->cfg[fk::kStep].slices;
+    for (int j = 1; j <= iters; j++) {
+        // w = H v1 with the step kernel (alpha = <w, v1> from its dots)
+        rc = run_step(t, t->V(v1), nullptr, t->V(w), false, true, 0, nullptr, nullptr, part.as<double>());
+        if (rc != FK_OK) return e->fail(rc, "energy_scale: %s", t->err.c_str());
+        FK_TRY(cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * pcount, cudaMemcpyDeviceToHost, t->stream), "lanczos");
+        FK_TRY(cudaStreamSynchronize(t->stream), "lanczos");
+        double a = 0;
+        for (int q = 1; q < pcount; q += 2) a += hp[q];
+        alpha[j - 1] = a;
+        if (j == iters) break;
+        const double abh[2] = {alpha[j - 1], beta[j - 1]};
+        FK_TRY(cudaMemcpyAsync(ab.p, abh, sizeof abh, cudaMemcpyHostToDevice, t->stream), "lanczos");
+        k_lanczos_update<<<ugrid, 256, 0, t->stream>>>(t->d_V[w].as<double>(), t->d_V[v1].as<double>(),
+                                                       t->d_V[vz].as<double>(), n_dbl, ab.as<double>(), part.as<double>());
+        FK_TRY(cudaGetLastError(), "lanczos update");
+        FK_TRY(cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * ugrid, cudaMemcpyDeviceToHost, t->stream), "lanczos");
+        FK_TRY(cudaStreamSynchronize(t->stream), "lanczos");
+        double ww = 0;
+        for (int q = 0; q < ugrid; q++) ww += hp[q];
+        beta[j] = std::sqrt(ww);
+        if (!(beta[j] > 0)) { iters = j; break; }   // invariant subspace found
+        // v0 <- v1, v1 <- w / beta
+        FK_TRY(fk::launch_scale_f64(e->cplx, t->V(w), t->V(vz), (long long)t->n * t->ld, 1.0 / beta[j], t->stream), "lanczos scale");
+        std::swap(v1, vz);   // new v1 = scaled w (in old vz), new v0 = old v1
+    }
+    double emin, emax;
+    tridiag_extremes(iters, alpha.data(), beta.data(), &emin, &emax);
+    const double slack = extend * (emax - emin);
+    *lo = emin - slack;
+    *hi = emax + slack;
+    ab.release();
+    part.release();
+    return FK_OK;
+}
+
+int fk_engine_set_profiling(fk_engine* e, int on) {
+    if (!e) return FK_ERR_ARG;
+    e->profiling = on != 0;
+    return FK_OK;
+}
+int fk_engine_profile_read(fk_engine* e, int kind, long long* launches, double* total_ms) {
+    if (!e || kind < 0 || kind >= fk::kNumKinds) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    prof_flush(e);
+    if (launches) *launches = e->prof_launches[kind];
+    if (total_ms) *total_ms = e->prof_ms[kind];
+    return FK_OK;
+}
+int fk_engine_profile_reset(fk_engine* e) {
+    if (!e) return FK_ERR_ARG;
+    prof_flush(e);
+    for (int k = 0; k < fk::kNumKinds; k++) { e->prof_launches[k] = 0; e->prof_ms[k] = 0; }
+    return FK_OK;
+}
+int fk_host_register(void* ptr, size_t bytes) {
+    if (!ptr || bytes == 0) return FK_ERR_ARG;
+    cudaError_t ce = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+    if (ce != cudaSuccess) { cudaGetLastError(); return ce == cudaErrorHostMemoryAlreadyRegistered ? FK_OK : FK_ERR_CUDA; }
+    return FK_OK;
+}
+int fk_host_unregister(void* ptr) {
+    if (!ptr) return FK_ERR_ARG;
+    cudaError_t ce = cudaHostUnregister(ptr);
+    if (ce != cudaSuccess) { cudaGetLastError(); return FK_ERR_CUDA; }
+    return FK_OK;
+}
+int fk_engine_timer_start(fk_engine* e) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    if (!e->t_start) FK_TRY(cudaEventCreate(&e->t_start), "timer event");
+    if (!e->t_stop) FK_TRY(cudaEventCreate(&e->t_stop), "timer event");
+    FK_TRY(cudaEventRecord(e->t_start, e->stream), "timer start");
+    return FK_OK;
+}
+int fk_engine_timer_stop(fk_engine* e, double* ms) {
+    if (!e || !ms) return FK_ERR_ARG;
+    if (!e->t_start) return e->fail(FK_ERR_STATE, "timer not started");
+    cudaSetDevice(e->device);
+    FK_TRY(cudaEventRecord(e->t_stop, e->stream), "timer stop");
+    FK_TRY(cudaEventSynchronize(e->t_stop), "timer wait");
+    float f = 0.f;
+    FK_TRY(cudaEventElapsedTime(&f, e->t_start, e->t_stop), "timer elapsed");
+    *ms = f;
+    return FK_OK;
+}
+int fk_engine_memory(const fk_engine* e, size_t* bytes) {
+    if (!e || !bytes) return FK_ERR_ARG;
+    size_t t = e->d_row_ptr.bytes + e->d_colc.bytes + e->d_hval.bytes + e->d_R.bytes + e->dd_row_ptr.bytes +
+               e->dd_colc.bytes + e->dd_rows.bytes + e->dd_pair.bytes + e->dd_acc.bytes + e->d_partials.bytes +
+               e->d_raw.bytes + e->d_coef.bytes + e->d_stage.bytes;
+    for (auto& v : e->d_V) t += v.bytes;
+    *bytes = t;
+    return FK_OK;
+}
+
+}  // extern "C"

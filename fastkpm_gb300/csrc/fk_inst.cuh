@@ -1,0 +1,103 @@
+// fk_inst.cuh -- instantiates every kernel of one precision (included once per
+// fk_inst_<prec>.cu with FK_PREC_NAME, FK_SYS_R and FK_SYS_C defined).
+#pragma once
+#include "fk_dispatch.h"
+
+namespace fk {
+
+namespace {
+template <class S, int B, int NP>
+cudaError_t step_one(const StepArgs& a, const Launch& l) {
+    k_cheb_step<S, B, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    return cudaGetLastError();
+}
+template <class S, int B, int NP>
+cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
+    k_adjoint_step<S, B, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    return cudaGetLastError();
+}
+template <class S, int B, int NP>
+cudaError_t outer_one(const OuterArgs& a, const Launch& l) {
+    k_outer<S, B, NP><<<l.grid, kThreads, 0, l.stream>>>(a);
+    return cudaGetLastError();
+}
+template <class S, int B, int NP>
+cudaError_t occ_one(int kind, size_t smem, int* n) {
+    const void* f = kind == kStep ? (const void*)k_cheb_step<S, B, NP>
+                  : kind == kAdjoint ? (const void*)k_adjoint_step<S, B, NP>
+                  : (const void*)k_outer<S, B, NP>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, f, kThreads, smem);
+}
+}  // namespace
+
+// dispatch on (cplx, B, NP) -> template instance
+#define FK_DISPATCH(FN, ...)                                                            \
+    do {                                                                                \
+        const int key = (cplx ? 100 : 0) + B * 10 + NP;                                 \
+        switch (key) {                                                                  \
+            case 11: return FN<FK_SYS_R, 1, 1>(__VA_ARGS__);                            \
+            case 12: return FN<FK_SYS_R, 1, 2>(__VA_ARGS__);                            \
+            case 14: return FN<FK_SYS_R, 1, 4>(__VA_ARGS__);                            \
+            case 21: return FN<FK_SYS_R, 2, 1>(__VA_ARGS__);                            \
+            case 22: return FN<FK_SYS_R, 2, 2>(__VA_ARGS__);                            \
+            case 24: return FN<FK_SYS_R, 2, 4>(__VA_ARGS__);                            \
+            case 111: return FN<FK_SYS_C, 1, 1>(__VA_ARGS__);                           \
+            case 112: return FN<FK_SYS_C, 1, 2>(__VA_ARGS__);                           \
+            case 114: return FN<FK_SYS_C, 1, 4>(__VA_ARGS__);                           \
+            case 121: return FN<FK_SYS_C, 2, 1>(__VA_ARGS__);                           \
+            case 122: return FN<FK_SYS_C, 2, 2>(__VA_ARGS__);                           \
+            case 124: return FN<FK_SYS_C, 2, 4>(__VA_ARGS__);                           \
+            default: return cudaErrorInvalidValue;                                      \
+        }                                                                               \
+    } while (0)
+
+#define FK_CAT2(a, b) a##_##b
+#define FK_CAT(a, b) FK_CAT2(a, b)
+
+cudaError_t FK_CAT(launch_step, FK_PREC_NAME)(int cplx, int B, int NP, const StepArgs& a, const Launch& l) {
+    FK_DISPATCH(step_one, a, l);
+}
+cudaError_t FK_CAT(launch_adjoint, FK_PREC_NAME)(int cplx, int B, int NP, const AdjArgs& a, const Launch& l) {
+    FK_DISPATCH(adj_one, a, l);
+}
+cudaError_t FK_CAT(launch_outer, FK_PREC_NAME)(int cplx, int B, int NP, const OuterArgs& a, const Launch& l) {
+    FK_DISPATCH(outer_one, a, l);
+}
+cudaError_t FK_CAT(occupancy, FK_PREC_NAME)(int kind, int cplx, int B, int NP, size_t smem, int* n) {
+    FK_DISPATCH(occ_one, kind, smem, n);
+}
+
+static int helper_grid(long long work) {
+    long long g = (work + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+cudaError_t FK_CAT(launch_load_colmajor, FK_PREC_NAME)(int cplx, const double* src, long long n, int ncols, int c0,
+                                                     long long ld, void* dst, cudaStream_t st) {
+    const int g = helper_grid(n * ncols);
+    if (cplx) k_load_colmajor<FK_SYS_C><<<g, 256, 0, st>>>(src, n, ncols, c0, ld, reinterpret_cast<FK_SYS_C::E*>(dst));
+    else k_load_colmajor<FK_SYS_R><<<g, 256, 0, st>>>(src, n, ncols, c0, ld, reinterpret_cast<FK_SYS_R::E*>(dst));
+    return cudaGetLastError();
+}
+cudaError_t FK_CAT(launch_store_colmajor, FK_PREC_NAME)(int cplx, const void* src, long long n, int ncols, long long ld,
+                                                      double* dst, cudaStream_t st) {
+    const int g = helper_grid(n * ncols);
+    if (cplx) k_store_colmajor<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(src), n, ncols, ld, dst);
+    else k_store_colmajor<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(src), n, ncols, ld, dst);
+    return cudaGetLastError();
+}
+cudaError_t FK_CAT(launch_scale, FK_PREC_NAME)(int cplx, const void* x, void* y, long long n_elems, double c,
+                                             cudaStream_t st) {
+    const int g = helper_grid(n_elems);
+    if (cplx) k_scale<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(x), reinterpret_cast<FK_SYS_C::E*>(y), n_elems, c);
+    else k_scale<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(x), reinterpret_cast<FK_SYS_R::E*>(y), n_elems, c);
+    return cudaGetLastError();
+}
+
+}  // namespace fk

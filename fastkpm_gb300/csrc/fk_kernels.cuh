@@ -1,0 +1,681 @@
+// fk_kernels.cuh -- hand-written sm_103a kernels for the stochastic Chebyshev path.
+//
+// Data layout in HBM (all kernels):
+//   * Probe / recursion vectors: row-major N x ld elements (ld = S rounded up to
+//     a whole 16-byte packet); scalar row r = b*i + bi of block row i.
+//     Padding columns hold zeros and stay zero under the recursion.
+//   * H: BSR. row_ptr[n_b+1]; colc[k] = block column | class << 30; hval holds
+//     b*b entries per block, column-major (the reference's BSR block order,
+//     src/fastkpm.h:64-65). Class 0: general entries, 1: real entries, 2: real
+//     multiple of the identity (only the (0,0) entry is read).
+//   * Several Hamiltonians ("systems") can share one launch: their block rows
+//     are concatenated, columns are global, and SysDesc says which CTAs work on
+//     which system. A CTA only ever touches one system, and the number of CTAs a
+//     system gets depends on that system alone, so every per-system reduction is
+//     the same whether the system runs alone or in a batch.
+//
+// Thread mapping: a block row is served by Gp lanes; lane g owns packets
+// g, g+Gp, ..., g+(NP-1)Gp of each scalar row (coalesced 16-byte accesses).
+// Items (row, lane) are cut into tiles of kThreads; each CTA walks the tiles of
+// its system with a CTA-count stride.
+#pragma once
+#include "fk_sys.cuh"
+
+namespace fk {
+
+constexpr int kThreads = 256;
+constexpr unsigned kColMask = 0x3fffffffu;
+
+struct SysDesc {
+    int row_base;    // first global block row
+    int n_b;         // block rows
+    int cta_base;    // first CTA of this system
+    int ctas;        // CTAs assigned to this system
+};
+
+struct StepArgs {
+    const SysDesc* sys;
+    const int* cta_sys;        // CTA -> system index
+    int Gp, P;                 // lanes per block row, packets per row in this launch
+    long long ld;              // elements per scalar row
+    const int* row_ptr;
+    const unsigned* colc;
+    const void* hval;
+    const void* x;             // gathered input
+    const void* z;             // own-row input (may be null)
+    void* y;                   // output (may alias z)
+    void* xi;                  // stochastic-sum accumulator (xi_mode != 0)
+    const double* coef;        // per system: coef[sys * cstride + ...]
+    int cstride;
+    int two, has_z, want_dots, xi_mode;   // xi_mode 1: xi = c0 x + c1 y;  2: xi += c1 y
+    double* partials;          // 2 doubles per CTA: <x,x>, Re<y,x>
+    int stage_cap;             // blocks that fit the shared-memory stage (0: no staging)
+};
+
+struct AdjArgs {
+    const SysDesc* sys;
+    const int* cta_sys;
+    int Gp, P;
+    long long ld;
+    const int* row_ptr;
+    const unsigned* colc;
+    const void* hval;
+    const void* A;        // alpha_m          (gathered)
+    void* Ap;             // alpha_{m+1} in,  alpha_{m-1} out
+    const void* Bv;       // beta_{m+1}       (gathered)
+    void* Bp;             // beta_{m+2} in,   beta_m out
+    const double* coef;   // per system: cA, cAp, cAn
+    int cstride;
+    double* Dacc;         // FP64 D accumulator on H's pattern (null: no fused epilogue)
+    double dscale;        // D += dscale * A_i B_j^dagger
+    int stage_cap;
+};
+
+struct OuterArgs {
+    const SysDesc* sys;
+    const int* cta_sys;
+    int Gp, P;
+    long long ld;
+    const int* row_ptr;        // D pattern
+    const unsigned* colc;      // D pattern columns (class bits ignored)
+    const void* A;
+    const void* Bv;
+    double alpha1, alpha2;     // D += alpha1 A B^dagger + alpha2 B A^dagger
+    double* Dacc;
+};
+
+template <class E, int EPP>
+union Packet {
+    uint4 u;
+    E e[EPP];
+};
+
+// Gathered (read-only for the whole kernel) packets go through the non-coherent path.
+template <class S, int NP>
+__device__ __forceinline__ void ld_nc(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int g, int Gp, int P) {
+    constexpr int EPP = S::EPP;
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+        const int pk = g + Gp * q;
+        Packet<typename S::E, EPP> pkt;
+        pkt.u = make_uint4(0u, 0u, 0u, 0u);
+        if (pk < P) pkt.u = __ldg(reinterpret_cast<const uint4*>(row) + pk);
+#pragma unroll
+        for (int e = 0; e < EPP; e++) v[q * EPP + e] = pkt.e[e];
+    }
+}
+template <class S, int NP>
+__device__ __forceinline__ void ld_rw(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int g, int Gp, int P) {
+    constexpr int EPP = S::EPP;
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+        const int pk = g + Gp * q;
+        Packet<typename S::E, EPP> pkt;
+        pkt.u = make_uint4(0u, 0u, 0u, 0u);
+        if (pk < P) pkt.u = reinterpret_cast<const uint4*>(row)[pk];
+#pragma unroll
+        for (int e = 0; e < EPP; e++) v[q * EPP + e] = pkt.e[e];
+    }
+}
+template <class S, int NP>
+__device__ __forceinline__ void st(typename S::E* row, const typename S::E (&v)[NP * S::EPP], int g, int Gp, int P) {
+    constexpr int EPP = S::EPP;
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+        const int pk = g + Gp * q;
+        Packet<typename S::E, EPP> pkt;
+#pragma unroll
+        for (int e = 0; e < EPP; e++) pkt.e[e] = v[q * EPP + e];
+        if (pk < P) reinterpret_cast<uint4*>(row)[pk] = pkt.u;
+    }
+}
+
+// Block-wide sum of two Dot values; thread 0 gets the result.
+template <class S>
+__device__ __forceinline__ void block_reduce2(typename S::Dot& a, typename S::Dot& b) {
+    typedef typename S::Dot Dot;
+    __shared__ Dot red[2][kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    auto wsum = [&](Dot v) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v = S::dot_shfl_add(v, off);
+        return v;
+    };
+    a = wsum(a);
+    b = wsum(b);
+    __syncthreads();
+    if (lane == 0) { red[0][wid] = a; red[1][wid] = b; }
+    __syncthreads();
+    if (wid == 0) {
+        a = lane < kThreads / 32 ? red[0][lane] : S::dot_zero();
+        b = lane < kThreads / 32 ? red[1][lane] : S::dot_zero();
+        a = wsum(a);
+        b = wsum(b);
+    }
+}
+
+// Stage the H blocks of global block rows [r_lo, r_hi] into shared memory.
+template <class S, int B>
+__device__ __forceinline__ void stage_h(unsigned* s_col, typename S::H* s_h, const unsigned* colc,
+                                        const typename S::H* hval, int k_lo, int nk) {
+    for (int q = threadIdx.x; q < nk; q += blockDim.x) s_col[q] = __ldg(colc + k_lo + q);
+    const int nh = nk * B * B;
+    const typename S::H* src = hval + (size_t)k_lo * B * B;
+    for (int q = threadIdx.x; q < nh; q += blockDim.x) s_h[q] = src[q];
+}
+
+// Accumulate one H block (column block j, entries hk) into acc for B output rows.
+template <class S, int B, int NP>
+__device__ __forceinline__ void block_mac(typename S::Acc (&acc)[B][NP * S::EPP], unsigned cc,
+                                          const typename S::H* hk, const typename S::E* xbase,
+                                          long long ld, int g, int Gp, int P) {
+    constexpr int EPT = NP * S::EPP;
+    const int j = (int)(cc & kColMask);
+    const unsigned cls = cc >> 30;
+#pragma unroll
+    for (int bj = 0; bj < B; bj++) {
+        typename S::E xv[EPT];
+        ld_nc<S, NP>(xv, xbase + (size_t)(B * j + bj) * ld, g, Gp, P);
+        if (cls == 2u) {
+            const typename S::Hr h = S::hreal(hk[bj * B + bj]);
+#pragma unroll
+            for (int e = 0; e < EPT; e++) S::mac_re(acc[bj][e], h, xv[e]);
+        } else if (!S::CPLX || cls == 1u) {
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                const typename S::Hr h = S::hreal(hk[bj * B + bi]);
+#pragma unroll
+                for (int e = 0; e < EPT; e++) S::mac_re(acc[bi][e], h, xv[e]);
+            }
+        } else {
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                const typename S::H h = hk[bj * B + bi];
+#pragma unroll
+                for (int e = 0; e < EPT; e++) S::mac(acc[bi][e], h, xv[e]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Chebyshev step: y = (two ? 2 : 1) * Hs x  (- z), fused with the moment partials
+// <x,x>, Re<y,x> over own rows and with the stochastic sum xi.
+// ---------------------------------------------------------------------------------
+template <class S, int B, int NP>
+__global__ void __launch_bounds__(kThreads) k_cheb_step(StepArgs a) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    constexpr int EPT = NP * S::EPP;
+    extern __shared__ __align__(16) unsigned char smem[];
+    H* s_h = reinterpret_cast<H*>(smem);
+    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int Gp = a.Gp;
+    const long long items = (long long)sd.n_b * Gp;
+    const E* x = reinterpret_cast<const E*>(a.x);
+    const E* z = reinterpret_cast<const E*>(a.z);
+    E* y = reinterpret_cast<E*>(a.y);
+    E* xi = reinterpret_cast<E*>(a.xi);
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef c0 = S::coef(a.xi_mode ? a.coef[sidx * a.cstride + 0] : 0.0);
+    const typename S::Coef c1 = S::coef(a.xi_mode ? a.coef[sidx * a.cstride + 1] : 0.0);
+
+    typename S::Dot dxx = S::dot_zero(), dyx = S::dot_zero();
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const int r_lo = sd.row_base + (int)(t0 / Gp);
+        const long long t_last = min(t0 + kThreads, items) - 1;
+        const int r_hi = sd.row_base + (int)(t_last / Gp);
+        const int k_lo = a.row_ptr[r_lo];
+        const int nk = a.row_ptr[r_hi + 1] - k_lo;
+        const bool staged = nk <= a.stage_cap;
+        if (staged) {
+            __syncthreads();
+            stage_h<S, B>(s_col, s_h, a.colc, hval, k_lo, nk);
+            __syncthreads();
+        }
+        const long long t = t0 + threadIdx.x;
+        if (t < items) {
+            const int il = (int)(t / Gp);
+            const int g = (int)(t - (long long)il * Gp);
+            const int i = sd.row_base + il;
+            typename S::Acc acc[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) acc[bi][e] = S::zero();
+            const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];
+            if (staged) {
+#pragma unroll 2
+                for (int k = kb; k < ke; k++)
+                    block_mac<S, B, NP>(acc, s_col[k - k_lo], s_h + (size_t)(k - k_lo) * B * B, x, a.ld, g, Gp, a.P);
+            } else {
+#pragma unroll 2
+                for (int k = kb; k < ke; k++)
+                    block_mac<S, B, NP>(acc, __ldg(a.colc + k), hval + (size_t)k * B * B, x, a.ld, g, Gp, a.P);
+            }
+            typename S::RowDot rxx = S::rd_zero(), ryx = S::rd_zero();
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                const size_t roff = (size_t)(B * i + bi) * a.ld;
+                E zv[EPT], yv[EPT];
+                if (a.has_z) ld_rw<S, NP>(zv, z + roff, g, Gp, a.P);
+                else {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) zv[e] = S::to(S::zero());
+                }
+#pragma unroll
+                for (int e = 0; e < EPT; e++) yv[e] = S::fin(acc[bi][e], a.two != 0, a.has_z != 0, zv[e]);
+                st<S, NP>(y + roff, yv, g, Gp, a.P);
+                if (a.want_dots || a.xi_mode == 1) {
+                    E xo[EPT];
+                    ld_nc<S, NP>(xo, x + roff, g, Gp, a.P);
+                    if (a.want_dots) {
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) { S::rd_nrm(rxx, xo[e]); S::rd_re(ryx, yv[e], xo[e]); }
+                    }
+                    if (a.xi_mode == 1) {
+                        E xv2[EPT];
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) {
+                            typename S::Acc t2 = S::zero();
+                            S::axpy(t2, c0, xo[e]);
+                            S::axpy(t2, c1, yv[e]);
+                            xv2[e] = S::to(t2);
+                        }
+                        st<S, NP>(xi + roff, xv2, g, Gp, a.P);
+                    }
+                }
+                if (a.xi_mode == 2) {
+                    E xv2[EPT];
+                    ld_rw<S, NP>(xv2, xi + roff, g, Gp, a.P);
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        typename S::Acc t2 = S::from(xv2[e]);
+                        S::axpy(t2, c1, yv[e]);
+                        xv2[e] = S::to(t2);
+                    }
+                    st<S, NP>(xi + roff, xv2, g, Gp, a.P);
+                }
+            }
+            if (a.want_dots) { S::dot_add(dxx, rxx); S::dot_add(dyx, ryx); }
+        }
+    }
+    if (a.want_dots) {
+        block_reduce2<S>(dxx, dyx);
+        if (threadIdx.x == 0) {
+            a.partials[2 * blockIdx.x + 0] = S::dot_get(dxx);
+            a.partials[2 * blockIdx.x + 1] = S::dot_get(dyx);
+        }
+    }
+}
+
+// Sum over the Gp lanes of a row group (Gp a power of two <= 32, groups aligned in the warp).
+template <class S>
+__device__ __forceinline__ typename S::OAcc group_sum(typename S::OAcc v, int Gp) {
+    for (int off = Gp >> 1; off > 0; off >>= 1) v = S::oa_shfl_add(v, off);
+    return v;
+}
+
+// ---------------------------------------------------------------------------------
+// Adjoint (reverse-mode) step of autodiff_matrix, both recursions in one pass:
+//   alpha_{m-1} = 2 Hs alpha_m - alpha_{m+1}
+//   beta_m      = 2 Hs beta_{m+1} - beta_{m+2} + cA alpha_m + cAp alpha_{m+1} + cAn alpha_{m-1}
+// and, when Dacc != null (D's pattern is H's pattern), the outer-product epilogue
+//   D_k += dscale * sum_s alpha_m[b i + bi, s] conj(beta_{m+1}[b j + bj, s])
+// reusing the gathered beta_{m+1} rows of block k = (i, j).
+// Requires Gp to be a power of two <= 32 when the epilogue is on.
+// ---------------------------------------------------------------------------------
+template <class S, int B, int NP>
+__global__ void __launch_bounds__(kThreads) k_adjoint_step(AdjArgs a) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    constexpr int EPT = NP * S::EPP;
+    extern __shared__ __align__(16) unsigned char smem[];
+    H* s_h = reinterpret_cast<H*>(smem);
+    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int Gp = a.Gp;
+    const long long items = (long long)sd.n_b * Gp;
+    const E* A = reinterpret_cast<const E*>(a.A);
+    E* Ap = reinterpret_cast<E*>(a.Ap);
+    const E* Bv = reinterpret_cast<const E*>(a.Bv);
+    E* Bp = reinterpret_cast<E*>(a.Bp);
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef cA = S::coef(a.coef[sidx * a.cstride + 0]);
+    const typename S::Coef cAp = S::coef(a.coef[sidx * a.cstride + 1]);
+    const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
+    const bool fuse = a.Dacc != nullptr;
+
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const int r_lo = sd.row_base + (int)(t0 / Gp);
+        const long long t_last = min(t0 + kThreads, items) - 1;
+        const int r_hi = sd.row_base + (int)(t_last / Gp);
+        const int k_lo = a.row_ptr[r_lo];
+        const int nk = a.row_ptr[r_hi + 1] - k_lo;
+        const bool staged = nk <= a.stage_cap;
+        if (staged) {
+            __syncthreads();
+            stage_h<S, B>(s_col, s_h, a.colc, hval, k_lo, nk);
+            __syncthreads();
+        }
+        const long long t = t0 + threadIdx.x;
+        const bool active = t < items;
+        const int il = active ? (int)(t / Gp) : 0;
+        const int g = active ? (int)(t - (long long)il * Gp) : 0;
+        const int i = sd.row_base + il;
+        const int kb = active ? a.row_ptr[i] : 0;
+        const int ke = active ? a.row_ptr[i + 1] : 0;
+
+        E Ai[B][EPT];
+        if (active) {
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, g, Gp, a.P);
+        } else {
+#pragma unroll
+            for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) Ai[bi][e] = S::to(S::zero());
+        }
+        typename S::Acc accA[B][EPT], accB[B][EPT];
+#pragma unroll
+        for (int bi = 0; bi < B; bi++)
+#pragma unroll
+            for (int e = 0; e < EPT; e++) { accA[bi][e] = S::zero(); accB[bi][e] = S::zero(); }
+
+        if (fuse) {
+            // Every lane of the warp walks the longest row of the warp so that the
+            // group reductions see all 32 lanes; missing blocks contribute zero.
+            int nmax = ke - kb;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
+            for (int kk = 0; kk < nmax; kk++) {
+                const int k = kb + kk;
+                const bool has = kk < ke - kb;
+                unsigned cc = 0;
+                const H* hk = nullptr;
+                if (has) {
+                    cc = staged ? s_col[k - k_lo] : __ldg(a.colc + k);
+                    hk = staged ? s_h + (size_t)(k - k_lo) * B * B : hval + (size_t)k * B * B;
+                }
+                const int j = (int)(cc & kColMask);
+                typename S::OAcc o[B][B];
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    E av[EPT], bv[EPT];
+                    if (has) {
+                        ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
+                        ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) { av[e] = S::to(S::zero()); bv[e] = av[e]; }
+                    }
+#pragma unroll
+                    for (int bi = 0; bi < B; bi++) {
+                        o[bi][bj] = S::oa_zero();
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) S::oa_mac(o[bi][bj], Ai[bi][e], bv[e]);
+                    }
+                    if (has) {
+                        const unsigned cls = cc >> 30;
+                        if (cls == 2u) {
+                            const typename S::Hr h = S::hreal(hk[bj * B + bj]);
+#pragma unroll
+                            for (int e = 0; e < EPT; e++) { S::mac_re(accA[bj][e], h, av[e]); S::mac_re(accB[bj][e], h, bv[e]); }
+                        } else if (!S::CPLX || cls == 1u) {
+#pragma unroll
+                            for (int bi = 0; bi < B; bi++) {
+                                const typename S::Hr h = S::hreal(hk[bj * B + bi]);
+#pragma unroll
+                                for (int e = 0; e < EPT; e++) { S::mac_re(accA[bi][e], h, av[e]); S::mac_re(accB[bi][e], h, bv[e]); }
+                            }
+                        } else {
+#pragma unroll
+                            for (int bi = 0; bi < B; bi++) {
+                                const H h = hk[bj * B + bi];
+#pragma unroll
+                                for (int e = 0; e < EPT; e++) { S::mac(accA[bi][e], h, av[e]); S::mac(accB[bi][e], h, bv[e]); }
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int bj = 0; bj < B; bj++)
+#pragma unroll
+                    for (int bi = 0; bi < B; bi++) o[bi][bj] = group_sum<S>(o[bi][bj], Gp);
+                if (has && g == 0) {
+#pragma unroll
+                    for (int bj = 0; bj < B; bj++)
+#pragma unroll
+                        for (int bi = 0; bi < B; bi++) {
+                            const double2 v = S::oa_get(o[bi][bj]);
+                            const size_t q = ((size_t)k * B * B + bj * B + bi) * (S::CPLX ? 2 : 1);
+                            a.Dacc[q] += a.dscale * v.x;
+                            if (S::CPLX) a.Dacc[q + 1] += a.dscale * v.y;
+                        }
+                }
+            }
+        } else if (active) {
+            for (int k = kb; k < ke; k++) {
+                const unsigned cc = staged ? s_col[k - k_lo] : __ldg(a.colc + k);
+                const H* hk = staged ? s_h + (size_t)(k - k_lo) * B * B : hval + (size_t)k * B * B;
+                block_mac<S, B, NP>(accA, cc, hk, A, a.ld, g, Gp, a.P);
+                block_mac<S, B, NP>(accB, cc, hk, Bv, a.ld, g, Gp, a.P);
+            }
+        }
+        if (active) {
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                const size_t roff = (size_t)(B * i + bi) * a.ld;
+                E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
+                ld_rw<S, NP>(apv, Ap + roff, g, Gp, a.P);
+                ld_rw<S, NP>(bpv, Bp + roff, g, Gp, a.P);
+#pragma unroll
+                for (int e = 0; e < EPT; e++) {
+                    an[e] = S::fin(accA[bi][e], true, true, apv[e]);
+                    typename S::Acc tb = S::from(S::fin(accB[bi][e], true, true, bpv[e]));
+                    S::axpy(tb, cA, Ai[bi][e]);
+                    S::axpy(tb, cAp, apv[e]);
+                    S::axpy(tb, cAn, an[e]);
+                    bn[e] = S::to(tb);
+                }
+                st<S, NP>(Ap + roff, an, g, Gp, a.P);
+                st<S, NP>(Bp + roff, bn, g, Gp, a.P);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Sparsity-restricted outer product on D's pattern (the reference's
+// outer_product_kernel role, src/outer_product.cu:38-60, re-designed):
+//   D_k(bi,bj) += alpha1 sum_s A[b i+bi, s] conj(B[b j+bj, s])
+//              +  alpha2 sum_s B[b i+bi, s] conj(A[b j+bj, s])
+// One row group (Gp lanes) per block row of D; own rows held in registers,
+// partner rows gathered once per block, reduction over S by warp shuffles,
+// FP64 accumulation into Dacc. Gp must be a power of two <= 32.
+// ---------------------------------------------------------------------------------
+template <class S, int B, int NP>
+__global__ void __launch_bounds__(kThreads) k_outer(OuterArgs a) {
+    typedef typename S::E E;
+    constexpr int EPT = NP * S::EPP;
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int Gp = a.Gp;
+    const long long items = (long long)sd.n_b * Gp;
+    const E* A = reinterpret_cast<const E*>(a.A);
+    const E* Bv = reinterpret_cast<const E*>(a.Bv);
+    const bool two_terms = a.alpha2 != 0.0;
+
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const long long t = t0 + threadIdx.x;
+        const bool active = t < items;
+        const int il = active ? (int)(t / Gp) : 0;
+        const int g = active ? (int)(t - (long long)il * Gp) : 0;
+        const int i = sd.row_base + il;
+        const int kb = active ? a.row_ptr[i] : 0;
+        const int ke = active ? a.row_ptr[i + 1] : 0;
+        E Ai[B][EPT], Bi[B][EPT];
+#pragma unroll
+        for (int bi = 0; bi < B; bi++) {
+            if (active) {
+                ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, g, Gp, a.P);
+                if (two_terms) ld_nc<S, NP>(Bi[bi], Bv + (size_t)(B * i + bi) * a.ld, g, Gp, a.P);
+            } else {
+#pragma unroll
+                for (int e = 0; e < EPT; e++) { Ai[bi][e] = S::to(S::zero()); Bi[bi][e] = Ai[bi][e]; }
+            }
+        }
+        int nmax = ke - kb;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
+        for (int kk = 0; kk < nmax; kk++) {
+            const int k = kb + kk;
+            const bool has = kk < ke - kb;
+            const int j = has ? (int)(__ldg(a.colc + k) & kColMask) : 0;
+            typename S::OAcc o1[B][B], o2[B][B];
+#pragma unroll
+            for (int bj = 0; bj < B; bj++) {
+                E bv[EPT], av[EPT];
+                if (has) {
+                    ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
+                    if (two_terms) ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) { bv[e] = S::to(S::zero()); av[e] = bv[e]; }
+                }
+#pragma unroll
+                for (int bi = 0; bi < B; bi++) {
+                    o1[bi][bj] = S::oa_zero();
+                    o2[bi][bj] = S::oa_zero();
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        S::oa_mac(o1[bi][bj], Ai[bi][e], bv[e]);
+                        if (two_terms) S::oa_mac(o2[bi][bj], Bi[bi][e], av[e]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int bj = 0; bj < B; bj++)
+#pragma unroll
+                for (int bi = 0; bi < B; bi++) {
+                    o1[bi][bj] = group_sum<S>(o1[bi][bj], Gp);
+                    if (two_terms) o2[bi][bj] = group_sum<S>(o2[bi][bj], Gp);
+                }
+            if (has && g == 0) {
+#pragma unroll
+                for (int bj = 0; bj < B; bj++)
+#pragma unroll
+                    for (int bi = 0; bi < B; bi++) {
+                        const double2 v1 = S::oa_get(o1[bi][bj]);
+                        const double2 v2 = two_terms ? S::oa_get(o2[bi][bj]) : make_double2(0.0, 0.0);
+                        const size_t q = ((size_t)k * B * B + bj * B + bi) * (S::CPLX ? 2 : 1);
+                        a.Dacc[q] += a.alpha1 * v1.x + a.alpha2 * v2.x;
+                        if (S::CPLX) a.Dacc[q + 1] += a.alpha1 * v1.y + a.alpha2 * v2.y;
+                    }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------------
+
+// Column-major double (or interleaved complex double) n x ncols host block, already
+// on the device, -> row-major device vector columns [c0, c0+ncols) in system S.
+template <class S>
+__global__ void k_load_colmajor(const double* src, long long n, int ncols, int c0, long long ld, typename S::E* dst) {
+    const long long total = n * (long long)ncols;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        // q walks the destination row-major so that stores are coalesced
+        const long long r = q / ncols;
+        const int c = (int)(q - r * ncols);
+        const long long sidx = (long long)c * n + r;
+        double2 v = S::CPLX ? make_double2(src[2 * sidx], src[2 * sidx + 1]) : make_double2(src[sidx], 0.0);
+        dst[r * ld + c0 + c] = S::from_double2(v);
+    }
+}
+
+// Row-major device vector -> column-major double host layout (for reading back R / state).
+template <class S>
+__global__ void k_store_colmajor(const typename S::E* src, long long n, int ncols, long long ld, double* dst) {
+    const long long total = n * (long long)ncols;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const long long r = q / ncols;
+        const int c = (int)(q - r * ncols);
+        const double2 v = S::to_double2(src[r * ld + c]);
+        const long long didx = (long long)c * n + r;
+        if (S::CPLX) { dst[2 * didx] = v.x; dst[2 * didx + 1] = v.y; }
+        else dst[didx] = v.x;
+    }
+}
+
+// y = c * x over the whole vector (n_elems elements)
+template <class S>
+__global__ void k_scale(const typename S::E* x, typename S::E* y, long long n_elems, double c) {
+    const typename S::Coef cc = S::coef(c);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_elems; q += (long long)gridDim.x * blockDim.x)
+        y[q] = S::scale(cc, x[q]);
+}
+
+// Sum the per-CTA moment partials of every (system, step) in a fixed order:
+// raw[(step * n_sys + s) * 2 + {0,1}]. One warp per (system, step).
+static __global__ void k_reduce_partials(const double* partials, int grid, int nsteps, const SysDesc* sys, int n_sys,
+                                  double* raw) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nsteps * n_sys) return;
+    const int step = w / n_sys, s = w - step * n_sys;
+    const double* p = partials + (size_t)step * grid * 2;
+    double a = 0.0, b = 0.0;
+    for (int c = sys[s].cta_base + lane; c < sys[s].cta_base + sys[s].ctas; c += 32) {
+        a += p[2 * c];
+        b += p[2 * c + 1];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+    }
+    if (lane == 0) { raw[2 * w] = a; raw[2 * w + 1] = b; }
+}
+
+// D <- (D + D^T-pair^dagger)/2 blockwise, then * scale (SpMatBsr::symmetrize and
+// scale, src/spmat.cpp:171-198, done on the device). pair[k] is the block index of
+// (j, i) for k = (i, j). Each unordered pair is handled by the block with i >= j.
+static __global__ void k_symmetrize_scale(double* D, const int* rows, const int* cols, const int* pair, int nnzb, int b,
+                                   int cplx, double scale) {
+    const int bb = b * b;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)nnzb * bb;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(q / bb);
+        const int e = (int)(q - (long long)k * bb);
+        const int bj = e / b, bi = e - (e / b) * b;
+        const int i = rows[k], j = cols[k];
+        if (i < j) continue;
+        const int kt = pair[k];
+        const size_t q1 = (size_t)k * bb + bj * b + bi;    // (bi, bj) of block k
+        const size_t q2 = (size_t)kt * bb + bi * b + bj;   // (bj, bi) of block kt
+        if (i == j && bi < bj) continue;                   // diagonal block: each entry pair once
+        if (cplx) {
+            const double r1 = D[2 * q1], i1 = D[2 * q1 + 1], r2 = D[2 * q2], i2 = D[2 * q2 + 1];
+            const double sr = (r1 + r2) / 2.0, si = (i1 - i2) / 2.0;
+            D[2 * q1] = sr * scale; D[2 * q1 + 1] = si * scale;
+            D[2 * q2] = sr * scale; D[2 * q2 + 1] = -si * scale;
+        } else {
+            const double s = (D[q1] + D[q2]) / 2.0;
+            D[q1] = s * scale;
+            D[q2] = s * scale;
+        }
+    }
+}
+
+}  // namespace fk

@@ -1,0 +1,192 @@
+/*
+ * fastkpm_gb300.h -- C ABI of the GB300 stochastic Chebyshev (KPM) engine.
+ *
+ * Plain C types only: opaque handles, pointers, sizes, int status codes. Host
+ * buffers are caller-owned and only read/written during the call; device
+ * buffers are owned by the engine. Every call returns FK_OK or an FK_ERR_*
+ * code; nothing aborts. fk_engine_last_error() gives a one-line reason.
+ *
+ * Value arrays are real doubles, or interleaved (re, im) double pairs when the
+ * engine was created with FK_COMPLEX. Probe matrices are column-major n x s
+ * (the layout of arma::Mat<T> R, reference src/fastkpm.h:188). BSR blocks are
+ * column-major b x b (reference src/fastkpm.h:64-65).
+ *
+ * The reference has no C ABI of its own; its hot path is the C++ class
+ * fkpm::Engine<T> (reference src/fastkpm.h:185-234). Each entry point below
+ * names the Engine<T> member it carries out; include/fastkpm.h implements
+ * Engine<T> on top of these calls.
+ */
+#ifndef FASTKPM_GB300_H
+#define FASTKPM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define FK_OK              0
+#define FK_ERR_ARG         1   /* invalid argument (size, order, pointer)                 */
+#define FK_ERR_OOM         2   /* device allocation failed / admission refused by memory   */
+#define FK_ERR_PATTERN     3   /* malformed BSR pattern (unsorted, out of range, asymmetric D) */
+#define FK_ERR_TIMEOUT     4   /* bounded wait expired                                      */
+#define FK_ERR_CUDA        5   /* CUDA runtime error                                        */
+#define FK_ERR_STATE       6   /* call order violated (e.g. autodiff without moments(M))    */
+#define FK_ERR_NODEV       7   /* no usable CUDA device                                     */
+#define FK_ERR_UNSUPPORTED 8   /* valid request outside what this build implements          */
+
+/* ---- value kinds at the boundary ---- */
+#define FK_REAL    0   /* double                          */
+#define FK_COMPLEX 1   /* complex double, (re, im) pairs  */
+
+/* ---- recursion precision (what the kernels store and compute in) ---- */
+#define FK_PREC_FP64 0   /* native IEEE double                                              */
+#define FK_PREC_FP32 1   /* float vectors and SpMM; FP64 moment sums and D accumulation      */
+#define FK_PREC_DS   2   /* double-single (float-float, ~48-bit) on the FP32 pipe; FP64 sums */
+
+/* ---- kernel kinds for profiling ---- */
+#define FK_KERNEL_STEP    0   /* fused Chebyshev step (+ moments / stochastic sum)          */
+#define FK_KERNEL_ADJOINT 1   /* fused reverse-mode step (+ outer-product epilogue)         */
+#define FK_KERNEL_OUTER   2   /* sparsity-restricted outer product                          */
+#define FK_KERNEL_HELPER  3   /* layout, scaling, reduction and symmetrize helpers          */
+
+typedef struct fk_engine fk_engine;
+
+/* Library / device queries */
+const char* fk_version(void);
+const char* fk_status_string(int status);
+int fk_device_count(int* count);
+
+/* mk_engine<T>() / mk_engine_cuSPARSE<T>(devices) (reference src/engine.cpp:124-131,
+ * src/engine_cusparse.cpp:1170-1215): one engine bound to one device and one stream. */
+int  fk_engine_create(int device, int kind, int precision, fk_engine** out);
+int  fk_engine_destroy(fk_engine* e);
+const char* fk_engine_last_error(const fk_engine* e);
+/* Run on a caller-provided cudaStream_t (NULL: the engine's own stream). */
+int  fk_engine_set_stream(fk_engine* e, void* cuda_stream);
+int  fk_engine_synchronize(fk_engine* e);
+/* Engine options: FK_OPT_* below. */
+#define FK_OPT_FUSE_D      0   /* 1 (default): fuse the outer product into the adjoint step when D's pattern is H's */
+#define FK_OPT_NP          1   /* packets per lane: 0 auto, or 1, 2, 4                                           */
+#define FK_OPT_CTAS_PER_SM 2   /* 0 auto (occupancy), else a cap on CTAs per SM                                   */
+#define FK_OPT_STAGE_H     3   /* 1 (default): stage H blocks in shared memory                                    */
+#define FK_OPT_GRAPHS      4   /* 1: capture the M-step recursions in CUDA graphs and replay them                 */
+int  fk_engine_set_option(fk_engine* e, int option, int value);
+int  fk_engine_get_option(const fk_engine* e, int option, int* value);
+
+/* Engine<T>::set_H(H, es) (reference src/engine_cusparse.cpp:701-730, src/engine_cpu.cpp:189-197):
+ * Hs = (H - avg I)/mag with avg = (lo+hi)/2, mag = (hi-lo)/2. n_b block rows of b x b blocks;
+ * row_ptr[n_b+1], col_idx[nnzb] sorted within each row; val[nnzb*b*b] column-major blocks.
+ * Rows without a stored diagonal block receive one. b must be 1 or 2. */
+int  fk_engine_set_H(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
+                     const double* val, double es_lo, double es_hi);
+/* Engine<T>::transfer_R() (reference src/engine_cusparse.cpp:675-699): upload the column-major
+ * n x s probe block R. s must be >= 1 (the reference exits on an empty R). */
+int  fk_engine_set_R(fk_engine* e, int n, int s, const double* R);
+/* Read back the device copy of R (column-major n x s), converted to double. */
+int  fk_engine_get_R(fk_engine* e, double* R);
+
+/* Engine<T>::moments(M) (reference src/engine_cusparse.cpp:755-791, src/engine_cpu.cpp:199-220):
+ * mu[M] for even M >= 2. Leaves alpha_{M/2-1}, alpha_{M/2} on the device for autodiff. */
+int  fk_engine_moments(fk_engine* e, int M, double* mu);
+/* Same work, enqueued only; fk_engine_fetch_moments() waits and copies mu[M] out. */
+int  fk_engine_moments_async(fk_engine* e, int M);
+int  fk_engine_fetch_moments(fk_engine* e, double* mu);
+
+/* Engine<T>::stoch_matrix(c, D) (reference src/engine_cusparse.cpp:910-953, src/engine_cpu.cpp:365-389):
+ * D = (R xi^dag + xi R^dag)/2 on D's BSR pattern, xi = sum_{m<M} c_m T_m(Hs) R.
+ * D pattern: d_n_b block rows (= H's), d_nnzb blocks, row_ptr/col_idx; D_val[d_nnzb*b*b] out. */
+int  fk_engine_stoch_matrix(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb,
+                            const int* d_row_ptr, const int* d_col_idx, double* D_val);
+/* Engine<T>::autodiff_matrix(c, D) (reference src/engine_cusparse.cpp:955-1039,
+ * src/engine_cpu.cpp:391-440): reverse-mode derivative of tr g, symmetrized and divided by
+ * the energy scale. Requires fk_engine_moments with the same M first (FK_ERR_STATE otherwise).
+ * D's pattern must be symmetric (FK_ERR_PATTERN otherwise). */
+int  fk_engine_autodiff_matrix(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb,
+                               const int* d_row_ptr, const int* d_col_idx, double* D_val);
+/* Enqueue-only forms of the two D calls; fk_engine_fetch_D waits and copies D_val out. */
+int  fk_engine_stoch_matrix_async(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb,
+                                  const int* d_row_ptr, const int* d_col_idx);
+int  fk_engine_autodiff_matrix_async(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb,
+                                     const int* d_row_ptr, const int* d_col_idx);
+int  fk_engine_fetch_D(fk_engine* e, double* D_val);
+
+/* Engine<T>::energy_scale(H, extend, iters) (reference src/engine_cusparse.cpp:598-673,
+ * src/engine_cpu.cpp:150-187): Lanczos on the device (iters SpMV steps from the start vector
+ * v0[n], or a seeded start when v0 is NULL), extremal eigenvalues of the tridiagonal by
+ * bisection, widened by extend*(max-min) on each side. */
+int  fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr,
+                            const int* col_idx, const double* val, double extend, int iters,
+                            const double* v0, double* lo, double* hi);
+
+/* Profiling: when on, each kernel launch is bracketed by CUDA events on the engine's stream. */
+int  fk_engine_set_profiling(fk_engine* e, int on);
+int  fk_engine_profile_read(fk_engine* e, int kernel_kind, long long* launches, double* total_ms);
+int  fk_engine_profile_reset(fk_engine* e);
+/* Device-side timing on the engine's stream: start records a CUDA event; stop records a
+ * second one, waits for it and returns the elapsed milliseconds. */
+int  fk_engine_timer_start(fk_engine* e);
+int  fk_engine_timer_stop(fk_engine* e, double* ms);
+/* Page-lock (pin) a caller-owned host buffer so uploads from it run at full copy speed;
+ * fk_host_unregister undoes it. */
+int  fk_host_register(void* ptr, size_t bytes);
+int  fk_host_unregister(void* ptr);
+/* Device memory the engine holds, in bytes. */
+int  fk_engine_memory(const fk_engine* e, size_t* bytes);
+
+/* ---- batched engine: many Hamiltonians of uneven size in one launch per Chebyshev step ----
+ * No reference counterpart: the reference solves one Hamiltonian per Engine<T> call; this is the
+ * batched form of Engine<T>::moments (reference src/engine_cusparse.cpp:755-791) over independent
+ * systems that share the block size b and the probe count s. */
+typedef struct fk_batch fk_batch;
+int  fk_batch_create(int device, int kind, int precision, fk_batch** out);
+int  fk_batch_destroy(fk_batch* bt);
+const char* fk_batch_last_error(const fk_batch* bt);
+/* Add one system (its H as in fk_engine_set_H and its column-major n x s probe block R);
+ * *index receives its position. Takes effect at the next fk_batch_commit. */
+int  fk_batch_add(fk_batch* bt, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
+                  const double* val, double es_lo, double es_hi, int s, const double* R, int* index);
+/* Upload every added system and build the launch tables. */
+int  fk_batch_commit(fk_batch* bt);
+/* mu[index * M + m] for every system, even M >= 2: M/2 launches, each covering all systems,
+ * replayed from a CUDA graph when FK_OPT_GRAPHS is on. */
+int  fk_batch_moments(fk_batch* bt, int M, double* mu);
+int  fk_batch_set_option(fk_batch* bt, int option, int value);
+int  fk_batch_get_option(const fk_batch* bt, int option, int* value);
+/* Choose lanes per block row, packets per lane, CTA cap and H staging by timing trial_steps
+ * Chebyshev steps of this batch per candidate; the fastest is kept (and remembered per batch
+ * shape for later batches in this process). Returns the chosen mapping and its step time. */
+int  fk_batch_autotune(fk_batch* bt, int trial_steps, int* lanes_per_row, int* packets_per_lane,
+                       int* ctas_per_sm, int* stage_h, double* ms_per_step);
+int  fk_batch_timer_start(fk_batch* bt);
+int  fk_batch_timer_stop(fk_batch* bt, double* ms);
+int  fk_batch_info(const fk_batch* bt, int* n_systems, long long* total_rows, size_t* device_bytes);
+
+/* ---- host helpers of the drop-in layer (no device work) ---- */
+/* SpMatBsr::build (reference src/spmat.cpp:46-129): sort blocks by (row, col), sum duplicates.
+ * Out arrays sized for n_elems blocks; returns FK_OK and *nnzb_out. */
+int  fk_bsr_build(int kind, int n_rows, int b, int n_elems, const int* row_idx, const int* col_idx,
+                  const double* val, int* row_ptr_out, int* row_idx_out, int* col_idx_out,
+                  double* val_out, int* nnzb_out);
+/* SpMatBsr::symmetrize (reference src/spmat.cpp:171-190) */
+int  fk_bsr_symmetrize(int kind, int n_rows, int b, int nnzb, const int* row_ptr, const int* row_idx,
+                       const int* col_idx, double* val);
+/* Probe generation (reference src/engine.cpp:34-116) with std::mt19937 master generator
+ * state given as (seed, draws already taken). R column-major n x (j_end - j_start). */
+int  fk_probe_identity(int kind, int n, int j_start, int j_end, double* R);
+int  fk_probe_uncorrelated(int kind, int n, int s, uint32_t seed, unsigned long long discard,
+                           int j_start, int j_end, double* R);
+int  fk_probe_correlated(int kind, int n, const int* groups, uint32_t seed, unsigned long long discard,
+                         int j_start, int j_end, double* R);
+/* KPM coefficients (reference src/fastkpm.cpp:13-78, :375-393): f = fermi_density(., kT, mu)
+ * for f_kind 0 and fermi_energy(., kT, mu) for f_kind 1, expanded on [es_lo, es_hi]. */
+int  fk_jackson_kernel(int M, double* out);
+int  fk_expansion_coefficients(int M, int Mq, int f_kind, double kT, double mu, double es_lo,
+                               double es_hi, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FASTKPM_GB300_H */

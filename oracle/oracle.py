@@ -1,0 +1,200 @@
+"""ctypes loader of the oracle (TEST INFRASTRUCTURE ONLY).
+
+CPU restatement of the reference's CPU engine; used by tests/, the smoke test
+and bench.py's CPU-baseline leg as the checker. PARITY UNPINNED against the
+reference itself (no reference tests or golden vectors; the reference needs
+Armadillo/Boost and does not build here); pinned against analytic known
+answers in tests/.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_p = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+_SIG = {
+    "orc_engine_create": (_p, [_i, _i]),
+    "orc_engine_destroy": (None, [_p]),
+    "orc_engine_threads": (_i, [_p]),
+    "orc_set_H": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _d, _d]),
+    "orc_set_R": (_i, [_p, _i, _i, _dp]),
+    "orc_moments": (_i, [_p, _i, _dp]),
+    "orc_stoch_matrix": (_i, [_p, _i, _dp, _i, _ip, _ip, _dp]),
+    "orc_autodiff_matrix": (_i, [_p, _i, _dp, _i, _i, _ip, _ip, _ip, _dp]),
+    "orc_energy_scale": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _d, _i, _dp, _dp, _dp]),
+    "orc_tridiag_extremes": (None, [_i, _dp, _dp, _dp, _dp]),
+    "orc_R_identity": (_i, [_i, _i, _i, _i, _dp]),
+    "orc_R_uncorrelated": (_i, [_i, _i, _i, C.c_uint32, C.c_ulonglong, _i, _i, _dp]),
+    "orc_R_correlated": (_i, [_i, _i, _ip, C.c_uint32, C.c_ulonglong, _i, _i, _dp]),
+    "orc_bsr_build": (_i, [_i, _i, _i, _i, _ip, _ip, _dp, _ip, _ip, _ip, _dp]),
+    "orc_bsr_symmetrize": (_i, [_i, _i, _i, _i, _ip, _ip, _ip, _dp]),
+    "orc_jackson_kernel": (None, [_i, _dp]),
+    "orc_chebyshev_fill_array": (None, [_d, _i, _i, _dp]),
+    "orc_fermi_density": (_d, [_d, _d, _d]),
+    "orc_fermi_energy": (_d, [_d, _d, _d]),
+    "orc_expansion_coefficients": (None, [_i, _i, _i, _d, _d, _d, _d, _dp]),
+    "orc_moment_product": (_d, [_i, _dp, _dp]),
+}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        for k, (r, a) in _SIG.items():
+            f = getattr(L, k)
+            f.restype = r
+            f.argtypes = a
+        _lib = L
+    return _lib
+
+
+def _ip_(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _dp_(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _dbl(a):
+    a = np.asarray(a)
+    if np.iscomplexobj(a):
+        return np.ascontiguousarray(a, dtype=np.complex128).view(np.float64)
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class OracleEngine:
+    """Engine_CPU<T> restated (reference src/engine_cpu.cpp)."""
+
+    def __init__(self, complex_values=False, nthreads=0):
+        self.L = lib()
+        self.cplx = bool(complex_values)
+        self.h = self.L.orc_engine_create(int(self.cplx), int(nthreads))
+        self.threads = self.L.orc_engine_threads(self.h)
+        self.es = None
+
+    def __del__(self):
+        try:
+            self.L.orc_engine_destroy(self.h)
+        except Exception:
+            pass
+
+    def set_H(self, H, es):
+        self.es = es
+        self._H = H
+        v = _dbl(H.val)
+        st = self.L.orc_set_H(self.h, H.n_rows, H.b_len, H.n_blocks(), _ip_(H.row_ptr), _ip_(H.col_idx), _dp_(v),
+                              es.lo, es.hi)
+        assert st == 0, st
+
+    def set_R(self, R):
+        dt = np.complex128 if self.cplx else np.float64
+        n, s = R.shape
+        flat = np.ascontiguousarray(np.asarray(R, dt).reshape(-1, order="F"))
+        st = self.L.orc_set_R(self.h, n, s, _dp_(_dbl(flat)))
+        assert st == 0, st
+
+    def moments(self, M):
+        mu = np.zeros(M)
+        st = self.L.orc_moments(self.h, M, _dp_(mu))
+        assert st == 0, st
+        return mu
+
+    def stoch_matrix(self, c, D):
+        dt = np.complex128 if self.cplx else np.float64
+        out = np.zeros(D.n_blocks() * D.b_len ** 2, dt)
+        c = np.ascontiguousarray(c, np.float64)
+        st = self.L.orc_stoch_matrix(self.h, len(c), _dp_(c), D.n_blocks(), _ip_(D.row_idx), _ip_(D.col_idx),
+                                     _dp_(_dbl(out)))
+        assert st == 0, st
+        return out
+
+    def autodiff_matrix(self, c, D):
+        dt = np.complex128 if self.cplx else np.float64
+        out = np.zeros(D.n_blocks() * D.b_len ** 2, dt)
+        c = np.ascontiguousarray(c, np.float64)
+        st = self.L.orc_autodiff_matrix(self.h, len(c), _dp_(c), D.n_rows, D.n_blocks(), _ip_(D.row_ptr),
+                                        _ip_(D.row_idx), _ip_(D.col_idx), _dp_(_dbl(out)))
+        assert st == 0, st
+        return out
+
+    def energy_scale(self, H, extend, iters, v0):
+        lo, hi = C.c_double(), C.c_double()
+        st = self.L.orc_energy_scale(self.h, H.n_rows, H.b_len, H.n_blocks(), _ip_(H.row_ptr), _ip_(H.col_idx),
+                                     _dp_(_dbl(H.val)), extend, iters, _dp_(_dbl(v0)), C.byref(lo), C.byref(hi))
+        assert st == 0, st
+        return lo.value, hi.value
+
+
+def R_uncorrelated(n, s, seed, discard=0, j_start=0, j_end=None, complex_values=False):
+    j_end = s if j_end is None else j_end
+    dt = np.complex128 if complex_values else np.float64
+    flat = np.zeros(n * (j_end - j_start), dt)
+    st = lib().orc_R_uncorrelated(int(complex_values), n, s, seed, discard, j_start, j_end, _dp_(_dbl(flat)))
+    assert st == 0
+    return flat.reshape((n, j_end - j_start), order="F")
+
+
+def R_correlated(groups, seed, discard=0, j_start=0, j_end=None, complex_values=False):
+    g = np.ascontiguousarray(groups, np.int32)
+    n = len(g)
+    j_end = int(g.max()) + 1 if j_end is None else j_end
+    dt = np.complex128 if complex_values else np.float64
+    flat = np.zeros(n * (j_end - j_start), dt)
+    st = lib().orc_R_correlated(int(complex_values), n, _ip_(g), seed, discard, j_start, j_end, _dp_(_dbl(flat)))
+    assert st == 0
+    return flat.reshape((n, j_end - j_start), order="F")
+
+
+def R_identity(n, j_start=0, j_end=None, complex_values=False):
+    j_end = n if j_end is None else j_end
+    dt = np.complex128 if complex_values else np.float64
+    flat = np.zeros(n * (j_end - j_start), dt)
+    st = lib().orc_R_identity(int(complex_values), n, j_start, j_end, _dp_(_dbl(flat)))
+    assert st == 0
+    return flat.reshape((n, j_end - j_start), order="F")
+
+
+def bsr_build(n_rows, b, row_idx, col_idx, blocks, complex_values):
+    dt = np.complex128 if complex_values else np.float64
+    ne = len(row_idx)
+    v = np.ascontiguousarray(blocks, dt).reshape(-1)
+    rp = np.zeros(n_rows + 1, np.int32)
+    ri = np.zeros(max(ne, 1), np.int32)
+    ci = np.zeros(max(ne, 1), np.int32)
+    vo = np.zeros(max(ne, 1) * b * b, dt)
+    k = lib().orc_bsr_build(int(complex_values), n_rows, b, ne, _ip_(np.ascontiguousarray(row_idx, np.int32)),
+                            _ip_(np.ascontiguousarray(col_idx, np.int32)), _dp_(_dbl(v)), _ip_(rp), _ip_(ri),
+                            _ip_(ci), _dp_(_dbl(vo)))
+    return rp, ri[:k], ci[:k], vo[:k * b * b]
+
+
+def jackson_kernel(M):
+    out = np.zeros(M)
+    lib().orc_jackson_kernel(M, _dp_(out))
+    return out
+
+
+def expansion_coefficients(M, Mq, kind, kT, mu, lo, hi):
+    out = np.zeros(M)
+    lib().orc_expansion_coefficients(M, Mq, {"fermi_density": 0, "fermi_energy": 1}[kind], kT, mu, lo, hi, _dp_(out))
+    return out
+
+
+def tridiag_extremes(alpha, beta):
+    a = np.ascontiguousarray(alpha, np.float64)
+    b = np.ascontiguousarray(beta, np.float64)
+    lo, hi = C.c_double(), C.c_double()
+    lib().orc_tridiag_extremes(len(a), _dp_(a), _dp_(b), C.byref(lo), C.byref(hi))
+    return lo.value, hi.value

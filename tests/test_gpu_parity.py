@@ -1,0 +1,264 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same
+seeded H and R, plus analytic answers, edge cases and error behaviour.
+
+Tolerances (stated with every check):
+  FP64 and DS engines: moments max_m |mu_m - mu_m^ref| / |mu_0^ref| <= 1e-10,
+                       D ||D - D_ref||_F / ||D_ref||_F <= 1e-10.
+  FP32 engine:         moments <= 1e-5 (relative to mu_0), D <= 1e-4 (Frobenius).
+"""
+import numpy as np
+import pytest
+
+import fastkpm_gb300 as fk
+from fastkpm_gb300 import _lib as L
+from fastkpm_gb300 import workloads as W
+from oracle import oracle as O
+from tests.conftest import cheb_T, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_MU = {"fp64": 1e-10, "ds": 1e-10, "fp32": 1e-5}
+TOL_D = {"fp64": 1e-10, "ds": 1e-10, "fp32": 1e-4}
+
+
+def mu_err(mu, ref):
+    return float(np.max(np.abs(np.asarray(mu) - ref)) / abs(ref[0]))
+
+
+def small_complex_case(L_=4, S=16, seed=21):
+    H, es, _ = W.cubic_spin_lattice(L_, -1.0, 1.0, seed)
+    R = W.phase_probes(W.cubic_colour_groups(L_, 2), realisations=max(1, S // 16), seed=seed)
+    return H, es, R
+
+
+def small_real_case(L_=12, S=24, seed=31):
+    H, es = W.square_lattice(L_, -1.0, 1.0, seed)
+    R = fk.probe_uncorrelated(H.n_rows, S, fk.RNG(seed))
+    return H, es, R
+
+
+def run_pair(H, es, R, cplx, prec, M, c, kind, options=None):
+    eng = fk.Engine(cplx, prec)
+    for k, v in (options or {}).items():
+        eng.set_option(k, v)
+    eng.set_H(H, es)
+    eng.set_R(R)
+    orc = O.OracleEngine(cplx)
+    orc.set_H(H, es)
+    orc.set_R(R)
+    mu = eng.moments(M)
+    mu_ref = orc.moments(M)
+    D = H.pattern_like(cplx)
+    if kind == "autodiff":
+        eng.autodiff_matrix(c, D)
+        D_ref = orc.autodiff_matrix(c, D)
+    else:
+        eng.stoch_matrix(c, D)
+        D_ref = orc.stoch_matrix(c, D)
+    return mu, mu_ref, D.val, D_ref
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+def test_config1_moments_and_stoch(gpu, prec):
+    cfg = W.config1()
+    H, es = cfg["H"], cfg["es"]
+    R = fk.probe_uncorrelated(H.n_rows, cfg["S"], fk.RNG(cfg["probe_seed"]))
+    c = W.fermi_coefficients(cfg["M"], es)
+    mu, mu_ref, D, D_ref = run_pair(H, es, R, False, prec, cfg["M"], c, "stoch")
+    assert mu_err(mu, mu_ref) <= TOL_MU[prec]
+    assert rel_err(D, D_ref) <= TOL_D[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("kind", ["autodiff", "stoch"])
+def test_small_cases(gpu, prec, cplx, kind):
+    H, es, R = small_complex_case() if cplx else small_real_case()
+    M = 40
+    c = W.fermi_coefficients(M, es, "fermi_energy" if kind == "autodiff" else "fermi_density", 0.0, 0.3)
+    mu, mu_ref, D, D_ref = run_pair(H, es, R, cplx, prec, M, c, kind)
+    assert mu_err(mu, mu_ref) <= TOL_MU[prec]
+    assert rel_err(D, D_ref) <= TOL_D[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ds"])
+def test_identity_probes_exact_traces(gpu, prec):
+    H, es, _ = W.cubic_spin_lattice(3, -1.0, 1.0, seed=5)
+    A = (H.to_dense() - es.avg() * np.eye(54)) / es.mag()
+    lam = np.linalg.eigvalsh(A)
+    eng = fk.Engine(True, prec)
+    eng.set_H(H, es)
+    eng.set_R_identity(54)
+    M = 30
+    mu = eng.moments(M)
+    ref = np.array([cheb_T(m, lam).sum() for m in range(M)])
+    assert np.max(np.abs(mu - ref)) / 54 < 1e-10
+
+
+@pytest.mark.parametrize("opts", [
+    {L.FK_OPT_FUSE_D: 0},
+    {L.FK_OPT_STAGE_H: 0},
+    {L.FK_OPT_NP: 1},
+    {L.FK_OPT_NP: 2},
+    {L.FK_OPT_CTAS_PER_SM: 1},
+])
+def test_launch_options_do_not_change_results(gpu, opts):
+    # S = 80 complex -> 80 packets per row: exercises column slices when NP is capped
+    H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=3)
+    R = W.phase_probes(W.cubic_colour_groups(4, 2), realisations=5, seed=3)
+    M = 24
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    mu, mu_ref, D, D_ref = run_pair(H, es, R, True, "fp64", M, c, "autodiff", opts)
+    assert mu_err(mu, mu_ref) <= 1e-10
+    assert rel_err(D, D_ref) <= 1e-10
+
+
+@pytest.mark.parametrize("M", [2, 4, 6])
+def test_autodiff_small_orders(gpu, M):
+    H, es, R = small_real_case(6, 8, 2)
+    c = W.fermi_coefficients(M, es, "fermi_energy", 0.0, 0.1, Mq=2 * M)
+    mu, mu_ref, D, D_ref = run_pair(H, es, R, False, "fp64", M, c, "autodiff")
+    assert mu_err(mu, mu_ref) <= 1e-12
+    assert rel_err(D, D_ref) <= 1e-12
+
+
+@pytest.mark.parametrize("prec,S", [("fp64", 1), ("fp32", 3), ("ds", 5), ("fp32", 1)])
+def test_odd_and_single_probe_columns(gpu, prec, S):
+    H, es, R = small_real_case(7, S, 4)
+    M = 20
+    c = W.fermi_coefficients(M, es)
+    mu, mu_ref, D, D_ref = run_pair(H, es, R, False, prec, M, c, "stoch")
+    assert mu_err(mu, mu_ref) <= TOL_MU[prec]
+    assert rel_err(D, D_ref) <= TOL_D[prec] * 10
+
+
+def test_D_pattern_wider_than_H(gpu):
+    # D on second-neighbour pattern (not H's): exercises the standalone outer-product kernel
+    H, es, R = small_complex_case(4, 16, 8)
+    H2 = W.cubic_spin_lattice(4, -1.0, 1.0, seed=8)[0]
+    A = (np.abs(H2.to_dense()) > 0).astype(float)
+    P = ((A @ A) > 0)
+    b = 2
+    Pb = P[::b, ::b]
+    rows, cols = np.nonzero(Pb)
+    D = fk.SpMatBsr.build(Pb.shape[0], b, rows, cols, np.zeros((len(rows), 4), complex))
+    M = 20
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    eng = fk.Engine(True, "fp64")
+    eng.set_H(H, es)
+    eng.set_R(R)
+    orc = O.OracleEngine(True)
+    orc.set_H(H, es)
+    orc.set_R(R)
+    eng.moments(M)
+    orc.moments(M)
+    eng.autodiff_matrix(c, D)
+    assert rel_err(D.val, orc.autodiff_matrix(c, D)) <= 1e-10
+    eng.stoch_matrix(c, D)
+    assert rel_err(D.val, orc.stoch_matrix(c, D)) <= 1e-10
+
+
+def test_missing_diagonal_blocks_are_inserted(gpu):
+    H, _ = W.square_lattice(6, -1.0, 0.0, seed=0)
+    keep = H.row_idx != H.col_idx
+    H0 = fk.SpMatBsr.build(H.n_rows, 1, H.row_idx[keep], H.col_idx[keep], H.val[keep][:, None])
+    es = fk.EnergyScale(-3.0, 5.0)   # avg != 0: the diagonal shift needs the inserted blocks
+    R = fk.probe_uncorrelated(36, 8, fk.RNG(1))
+    M = 20
+    c = W.fermi_coefficients(M, es)
+    mu, mu_ref, D, D_ref = run_pair(H0, es, R, False, "fp64", M, c, "stoch")
+    assert mu_err(mu, mu_ref) <= 1e-12
+    assert rel_err(D, D_ref) <= 1e-12
+
+
+def test_results_are_deterministic(gpu):
+    H, es, R = small_complex_case(6, 32, 2)
+    eng = fk.Engine(True, "ds")
+    eng.set_H(H, es)
+    eng.set_R(R)
+    M = 50
+    a = eng.moments(M)
+    b = eng.moments(M)
+    assert np.array_equal(a, b)
+
+
+def test_error_behaviour(gpu):
+    H, es, R = small_real_case(6, 8, 1)
+    eng = fk.Engine(False, "fp64")
+    with pytest.raises(L.FkError) as ei:
+        eng.moments(10)
+    assert ei.value.status == L.FK_ERR_STATE
+    eng.set_H(H, es)
+    eng.set_R(R)
+    with pytest.raises(L.FkError) as ei:
+        eng.moments(7)
+    assert ei.value.status == L.FK_ERR_ARG
+    D = H.pattern_like()
+    c = W.fermi_coefficients(10, es)
+    with pytest.raises(L.FkError) as ei:
+        eng.autodiff_matrix(c, D)   # no moments(10) first
+    assert ei.value.status == L.FK_ERR_STATE
+    eng.moments(10)
+    # an asymmetric D pattern cannot be symmetrized
+    Dbad = fk.SpMatBsr(H.n_rows, 1, np.r_[0, np.ones(H.n_rows, np.int32)].cumsum().astype(np.int32),
+                       np.r_[1, np.arange(1, H.n_rows)].astype(np.int32))
+    with pytest.raises(L.FkError) as ei:
+        eng.autodiff_matrix(c, Dbad)
+    assert ei.value.status == L.FK_ERR_PATTERN
+    with pytest.raises(L.FkError) as ei:
+        eng.set_R(np.ones((H.n_rows + 1, 2)))
+        eng.moments(10)
+    assert ei.value.status == L.FK_ERR_ARG
+    with pytest.raises(L.FkError) as ei:
+        eng.set_R(np.ones((H.n_rows, 0)))
+    assert ei.value.status == L.FK_ERR_ARG
+    bad = H.copy()
+    bad.col_idx = bad.col_idx.copy()
+    bad.col_idx[0], bad.col_idx[1] = bad.col_idx[1], bad.col_idx[0]
+    with pytest.raises(L.FkError) as ei:
+        eng.set_H(bad, es)
+    assert ei.value.status == L.FK_ERR_PATTERN
+
+
+def test_energy_scale_lanczos(gpu):
+    H, _ = W.square_lattice(10, -1.0, 2.0, seed=4)
+    lam = np.linalg.eigvalsh(H.to_dense())
+    eng = fk.Engine(False, "fp64")
+    v0 = np.random.default_rng(0).standard_normal(100)
+    es = eng.energy_scale(H, 0.0, 100, v0=v0)
+    assert abs(es.lo - lam.min()) < 1e-8 and abs(es.hi - lam.max()) < 1e-8
+    lo, hi = O.OracleEngine(False).energy_scale(H, 0.05, 40, v0)
+    es2 = eng.energy_scale(H, 0.05, 40, v0=v0)
+    assert abs(es2.lo - lo) < 1e-9 and abs(es2.hi - hi) < 1e-9
+    es3 = eng.energy_scale(H, 0.01)   # seeded start vector
+    assert es3.lo <= lam.min() + 1e-6 and es3.hi >= lam.max() - 1e-6
+
+
+def test_complex_energy_scale(gpu):
+    H, _, _ = W.cubic_spin_lattice(3, -1.0, 1.0, seed=1)
+    lam = np.linalg.eigvalsh(H.to_dense())
+    es = fk.Engine(True, "fp64").energy_scale(H, 0.0, 54)
+    assert abs(es.lo - lam.min()) < 1e-7 and abs(es.hi - lam.max()) < 1e-7
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ds"])
+def test_probe_split_additivity_full_size(gpu, prec):
+    """Size-independent property at the full cubic L=64, S=256 shape: moments and D are sums
+    over probe columns, so the two halves of R must add up to the whole; mu_0 = ||R||^2."""
+    cfg = W.config2()
+    H, es = cfg["H"], cfg["es"]
+    R = W.phase_probes(cfg["groups"], cfg["realisations"], cfg["probe_seed"])
+    M = 8
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    D = H.pattern_like(True)
+    eng = fk.Engine(True, prec)
+    eng.set_H(H, es)
+    parts_mu, parts_D = [], []
+    for cols in [slice(0, 256), slice(0, 128), slice(128, 256)]:
+        eng.set_R(R[:, cols])
+        parts_mu.append(eng.moments(M))
+        eng.autodiff_matrix(c, D)
+        parts_D.append(D.val.copy())
+    assert abs(parts_mu[0][0] - np.vdot(R, R).real) / parts_mu[0][0] < 1e-12
+    assert mu_err(parts_mu[1] + parts_mu[2], parts_mu[0]) < 1e-12
+    assert rel_err(parts_D[1] + parts_D[2], parts_D[0]) < 1e-11
