@@ -175,11 +175,11 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     }
     if (!(Gp == 1 || Gp == 2 || Gp == 4 || Gp == 8 || Gp == 16 || Gp == 32)) return bt->fail(FK_ERR_ARG, "bad lanes per row %d", Gp);
     if (!(NP == 1 || NP == 2 || NP == 4)) return bt->fail(FK_ERR_ARG, "bad packets per lane %d", NP);
-    const int W = Gp * NP;
+    // the kernel walks the row's column chunks of Gp * NP packets itself: one launch per step
     bt->Gp = Gp;
     bt->NP = NP;
-    bt->W = std::min(W, P);
-    bt->slices = (P + W - 1) / W;
+    bt->W = P;
+    bt->slices = 1;
     // shared-memory stage: largest tile over all systems
     int nk_max = 0;
     for (int k = 0; k < bt->n_sys; k++) {
@@ -491,12 +491,11 @@ int fk_batch_autotune(fk_batch* bt, int trial_steps, int* lanes, int* np_out, in
     if (!bt->configured) return bt->fail(FK_ERR_STATE, "batch_autotune: commit the batch first");
     if (trial_steps < 1) trial_steps = 8;
     cudaSetDevice(bt->device);
-    // candidate mappings: every (Gp, NP) with Gp * NP >= P or NP = 4 (column slices), caps, staging
+    // candidate mappings: packets per lane (lanes per row follow), CTA caps, H staging
     std::vector<Mapping> cands;
     for (int np : {1, 2, 4}) {
         int gp = next_pow2((bt->P + np - 1) / np);
         if (gp > 32) gp = 32;
-        if (gp * np < bt->P && np != 4) continue;
         for (int cap : {0, 2, 4, 8})
             for (int st : {1, 0}) cands.push_back(Mapping{gp, np, cap, st});
     }

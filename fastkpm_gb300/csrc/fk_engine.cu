@@ -224,27 +224,20 @@ int configure(fk_engine* e) {
     for (auto& c : e->cfg) c.valid = false;
     if (e->n_b == 0 || e->s == 0 || e->n != e->n_b * e->b) return FK_OK;   // configured once both are set
     const int P = e->P;
-    int NP = 1, Gp = 1, slices = 1, W = P;
-    const int npmax = e->opt_np > 0 ? e->opt_np : 4;
-    if (P <= 32) {
-        Gp = next_pow2(P);
+    // Gp lanes per block row, NP packets per lane and column chunk; the kernels walk
+    // the row's ceil(P / (Gp * NP)) chunks themselves, so one launch covers all columns.
+    const int slices = 1, W = P;
+    int NP, Gp;
+    if (e->opt_np > 0) {
+        NP = e->opt_np;
+        Gp = std::min(32, next_pow2((P + NP - 1) / NP));
+    } else if (P <= 32) {
         NP = 1;
+        Gp = next_pow2(P);
     } else {
+        NP = 4;   // measured best (or tied) for the step and adjoint kernels at S >= 128
         Gp = 32;
-        NP = (P + 31) / 32;
-        if (NP > npmax) {
-            W = 32 * npmax;
-            slices = (P + W - 1) / W;
-            NP = npmax;
-        } else {
-            NP = NP <= 1 ? 1 : NP <= 2 ? 2 : 4;
-            if (NP > npmax) NP = npmax;
-            W = 32 * NP;
-            slices = (P + W - 1) / W;
-        }
     }
-    if (e->opt_np > 0 && P <= 32) NP = 1;
-    if (slices == 1) W = P;
     // H blocks per tile of kThreads items: the shared-memory stage size
     const long long items = (long long)e->n_b * Gp;
     const long long tiles = (items + fk::kThreads - 1) / fk::kThreads;
@@ -343,7 +336,7 @@ int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp,
     return FK_OK;
 }
 
-int run_outer(fk_engine* e, const void* A, const void* Bv, double alpha1, double alpha2) {
+int run_outer(fk_engine* e, const void* A, const void* Bv, double alpha, bool two_terms) {
     const KCfg& c = e->cfg[fk::kOuter];
     const size_t es = e->esize();
     for (int sl = 0; sl < c.slices; sl++) {
@@ -358,8 +351,8 @@ int run_outer(fk_engine* e, const void* A, const void* Bv, double alpha1, double
         a.colc = e->dd_colc.as<unsigned>();
         a.A = (const char*)A + off * es;
         a.Bv = (const char*)Bv + off * es;
-        a.alpha1 = alpha1;
-        a.alpha2 = alpha2;
+        a.alpha = alpha;
+        a.two_terms = two_terms ? 1 : 0;
         a.Dacc = e->dd_acc.as<double>();
         ProfScope ps(e, fk::kOuter);
         FK_TRY(prec_launch_outer(e, c.NP, a, fk::Launch{c.ctas, 0, e->stream}), "outer kernel launch");
@@ -540,7 +533,7 @@ int stoch_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, c
     const size_t dn = (size_t)d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
     FK_TRY(cudaMemsetAsync(e->dd_acc.p, 0, sizeof(double) * std::max<size_t>(dn, 1), e->stream), "clear D");
     if (d_nnzb > 0) {
-        rc = run_outer(e, e->d_R.p, xi, 0.5, 0.5);
+        rc = run_outer(e, e->d_R.p, xi, 0.5, true);
         if (rc != FK_OK) return rc;
     }
     e->mom_M = 0;   // the recursion state is no longer the one autodiff needs (reference clears a0, a1)
@@ -583,7 +576,7 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
         FK_TRY(cudaMemsetAsync(e->V(Bp), 0, e->vec_bytes(), e->stream), "clear beta");
         for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
             if (!fuse && d_nnzb > 0) {
-                rc = run_outer(e, e->V(A), e->V(Bv), 2.0, 0.0);   // D += 2 alpha_m beta_{m+1}^dag
+                rc = run_outer(e, e->V(A), e->V(Bv), 2.0, false);   // D += 2 alpha_m beta_{m+1}^dag
                 if (rc != FK_OK) return rc;
             }
             rc = run_adjoint(e, e->V(A), e->V(Ap), e->V(Bv), e->V(Bp), e->d_coef.as<double>() + 3 * q,
@@ -598,7 +591,7 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
     }
     // D += alpha_0 (beta_1 + diag alpha_0)^dag, then symmetrize and divide by mag
     if (d_nnzb > 0) {
-        rc = run_outer(e, e->V(A), e->V(Bv), 1.0, 0.0);
+        rc = run_outer(e, e->V(A), e->V(Bv), 1.0, false);
         if (rc != FK_OK) return rc;
         const double mag = (e->es_hi - e->es_lo) / 2.0;
         const long long work = (long long)d_nnzb * e->b * e->b;

@@ -2,8 +2,8 @@
 //
 // Data layout in HBM (all kernels):
 //   * Probe / recursion vectors: row-major N x ld elements (ld = S rounded up to
-//     a whole 16-byte packet); scalar row r = b*i + bi of block row i.
-//     Padding columns hold zeros and stay zero under the recursion.
+//     a whole 16-byte packet, P = ld / EPP packets per row); scalar row
+//     r = b*i + bi of block row i. Padding columns hold zeros and stay zero.
 //   * H: BSR. row_ptr[n_b+1]; colc[k] = block column | class << 30; hval holds
 //     b*b entries per block, column-major (the reference's BSR block order,
 //     src/fastkpm.h:64-65). Class 0: general entries, 1: real entries, 2: real
@@ -14,10 +14,14 @@
 //     system gets depends on that system alone, so every per-system reduction is
 //     the same whether the system runs alone or in a batch.
 //
-// Thread mapping: a block row is served by Gp lanes; lane g owns packets
-// g, g+Gp, ..., g+(NP-1)Gp of each scalar row (coalesced 16-byte accesses).
-// Items (row, lane) are cut into tiles of kThreads; each CTA walks the tiles of
-// its system with a CTA-count stride.
+// Thread mapping: a block row is served by Gp lanes (a power of two <= 32,
+// aligned inside the warp). Items (row, lane) are cut into tiles of kThreads;
+// each CTA walks the tiles of its system with a CTA-count stride, stages the
+// tile's H blocks in shared memory once, and then walks the row's columns in
+// chunks of W = Gp * NP packets: in chunk c lane g owns packets
+// c*W + g + q*Gp (q < NP), so every access is a coalesced 16-byte packet and NP
+// sets the registers each thread holds. Sums that span columns (moment dots,
+// D entries) are accumulated across chunks in a fixed order by the same thread.
 #pragma once
 #include "fk_sys.cuh"
 
@@ -36,7 +40,7 @@ struct SysDesc {
 struct StepArgs {
     const SysDesc* sys;
     const int* cta_sys;        // CTA -> system index
-    int Gp, P;                 // lanes per block row, packets per row in this launch
+    int Gp, P;                 // lanes per block row, packets per row
     long long ld;              // elements per scalar row
     const int* row_ptr;
     const unsigned* colc;
@@ -80,7 +84,8 @@ struct OuterArgs {
     const unsigned* colc;      // D pattern columns (class bits ignored)
     const void* A;
     const void* Bv;
-    double alpha1, alpha2;     // D += alpha1 A B^dagger + alpha2 B A^dagger
+    double alpha;              // D += alpha (A B^dagger [+ B A^dagger when two_terms])
+    int two_terms;
     double* Dacc;
 };
 
@@ -90,13 +95,15 @@ union Packet {
     E e[EPP];
 };
 
-// Gathered (read-only for the whole kernel) packets go through the non-coherent path.
+// Packets base + g + q*Gp (q < NP) of one row, masked to pk < P.
+// Gathered rows are read-only for the whole kernel: non-coherent path.
 template <class S, int NP>
-__device__ __forceinline__ void ld_nc(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int g, int Gp, int P) {
+__device__ __forceinline__ void ld_nc(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int base, int g,
+                                      int Gp, int P) {
     constexpr int EPP = S::EPP;
 #pragma unroll
     for (int q = 0; q < NP; q++) {
-        const int pk = g + Gp * q;
+        const int pk = base + g + Gp * q;
         Packet<typename S::E, EPP> pkt;
         pkt.u = make_uint4(0u, 0u, 0u, 0u);
         if (pk < P) pkt.u = __ldg(reinterpret_cast<const uint4*>(row) + pk);
@@ -105,11 +112,12 @@ __device__ __forceinline__ void ld_nc(typename S::E (&v)[NP * S::EPP], const typ
     }
 }
 template <class S, int NP>
-__device__ __forceinline__ void ld_rw(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int g, int Gp, int P) {
+__device__ __forceinline__ void ld_rw(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int base, int g,
+                                      int Gp, int P) {
     constexpr int EPP = S::EPP;
 #pragma unroll
     for (int q = 0; q < NP; q++) {
-        const int pk = g + Gp * q;
+        const int pk = base + g + Gp * q;
         Packet<typename S::E, EPP> pkt;
         pkt.u = make_uint4(0u, 0u, 0u, 0u);
         if (pk < P) pkt.u = reinterpret_cast<const uint4*>(row)[pk];
@@ -118,11 +126,12 @@ __device__ __forceinline__ void ld_rw(typename S::E (&v)[NP * S::EPP], const typ
     }
 }
 template <class S, int NP>
-__device__ __forceinline__ void st(typename S::E* row, const typename S::E (&v)[NP * S::EPP], int g, int Gp, int P) {
+__device__ __forceinline__ void st(typename S::E* row, const typename S::E (&v)[NP * S::EPP], int base, int g, int Gp,
+                                   int P) {
     constexpr int EPP = S::EPP;
 #pragma unroll
     for (int q = 0; q < NP; q++) {
-        const int pk = g + Gp * q;
+        const int pk = base + g + Gp * q;
         Packet<typename S::E, EPP> pkt;
 #pragma unroll
         for (int e = 0; e < EPP; e++) pkt.e[e] = v[q * EPP + e];
@@ -154,7 +163,7 @@ __device__ __forceinline__ void block_reduce2(typename S::Dot& a, typename S::Do
     }
 }
 
-// Stage the H blocks of global block rows [r_lo, r_hi] into shared memory.
+// Stage H blocks [k_lo, k_lo + nk) into shared memory.
 template <class S, int B>
 __device__ __forceinline__ void stage_h(unsigned* s_col, typename S::H* s_h, const unsigned* colc,
                                         const typename S::H* hval, int k_lo, int nk) {
@@ -164,38 +173,47 @@ __device__ __forceinline__ void stage_h(unsigned* s_col, typename S::H* s_h, con
     for (int q = threadIdx.x; q < nh; q += blockDim.x) s_h[q] = src[q];
 }
 
-// Accumulate one H block (column block j, entries hk) into acc for B output rows.
+// acc[bi] += sum_bj H_k(bi, bj) x[b j + bj] for one block (class-specialised).
 template <class S, int B, int NP>
-__device__ __forceinline__ void block_mac(typename S::Acc (&acc)[B][NP * S::EPP], unsigned cc,
-                                          const typename S::H* hk, const typename S::E* xbase,
-                                          long long ld, int g, int Gp, int P) {
+__device__ __forceinline__ void mac_block(typename S::Acc (&acc)[B][NP * S::EPP], unsigned cls, const typename S::H* hk,
+                                          const typename S::E (&xv)[NP * S::EPP], int bj) {
     constexpr int EPT = NP * S::EPP;
-    const int j = (int)(cc & kColMask);
-    const unsigned cls = cc >> 30;
+    if (cls == 2u) {
+        const typename S::Hr h = S::hreal(hk[bj * B + bj]);
 #pragma unroll
-    for (int bj = 0; bj < B; bj++) {
-        typename S::E xv[EPT];
-        ld_nc<S, NP>(xv, xbase + (size_t)(B * j + bj) * ld, g, Gp, P);
-        if (cls == 2u) {
-            const typename S::Hr h = S::hreal(hk[bj * B + bj]);
+        for (int e = 0; e < EPT; e++) S::mac_re(acc[bj][e], h, xv[e]);
+    } else if (!S::CPLX || cls == 1u) {
 #pragma unroll
-            for (int e = 0; e < EPT; e++) S::mac_re(acc[bj][e], h, xv[e]);
-        } else if (!S::CPLX || cls == 1u) {
+        for (int bi = 0; bi < B; bi++) {
+            const typename S::Hr h = S::hreal(hk[bj * B + bi]);
 #pragma unroll
-            for (int bi = 0; bi < B; bi++) {
-                const typename S::Hr h = S::hreal(hk[bj * B + bi]);
+            for (int e = 0; e < EPT; e++) S::mac_re(acc[bi][e], h, xv[e]);
+        }
+    } else {
 #pragma unroll
-                for (int e = 0; e < EPT; e++) S::mac_re(acc[bi][e], h, xv[e]);
-            }
-        } else {
+        for (int bi = 0; bi < B; bi++) {
+            const typename S::H h = hk[bj * B + bi];
 #pragma unroll
-            for (int bi = 0; bi < B; bi++) {
-                const typename S::H h = hk[bj * B + bi];
-#pragma unroll
-                for (int e = 0; e < EPT; e++) S::mac(acc[bi][e], h, xv[e]);
-            }
+            for (int e = 0; e < EPT; e++) S::mac(acc[bi][e], h, xv[e]);
         }
     }
+}
+
+// Tile bookkeeping shared by the kernels: rows of tile t0 and their H block range.
+struct Tile {
+    int k_lo, nk;
+    bool staged;
+};
+__device__ __forceinline__ Tile tile_range(const int* row_ptr, const SysDesc& sd, long long t0, long long items, int Gp,
+                                           int stage_cap) {
+    const int r_lo = sd.row_base + (int)(t0 / Gp);
+    const long long t_last = min(t0 + kThreads, items) - 1;
+    const int r_hi = sd.row_base + (int)(t_last / Gp);
+    Tile t;
+    t.k_lo = row_ptr[r_lo];
+    t.nk = row_ptr[r_hi + 1] - t.k_lo;
+    t.staged = t.nk <= stage_cap;
+    return t;
 }
 
 // ---------------------------------------------------------------------------------
@@ -203,7 +221,7 @@ __device__ __forceinline__ void block_mac(typename S::Acc (&acc)[B][NP * S::EPP]
 // <x,x>, Re<y,x> over own rows and with the stochastic sum xi.
 // ---------------------------------------------------------------------------------
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads) k_cheb_step(StepArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_cheb_step(StepArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
     constexpr int EPT = NP * S::EPP;
@@ -214,7 +232,8 @@ __global__ void __launch_bounds__(kThreads) k_cheb_step(StepArgs a) {
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp;
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* x = reinterpret_cast<const E*>(a.x);
     const E* z = reinterpret_cast<const E*>(a.z);
@@ -226,53 +245,53 @@ __global__ void __launch_bounds__(kThreads) k_cheb_step(StepArgs a) {
 
     typename S::Dot dxx = S::dot_zero(), dyx = S::dot_zero();
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
-        const int r_lo = sd.row_base + (int)(t0 / Gp);
-        const long long t_last = min(t0 + kThreads, items) - 1;
-        const int r_hi = sd.row_base + (int)(t_last / Gp);
-        const int k_lo = a.row_ptr[r_lo];
-        const int nk = a.row_ptr[r_hi + 1] - k_lo;
-        const bool staged = nk <= a.stage_cap;
-        if (staged) {
+        const Tile tl = tile_range(a.row_ptr, sd, t0, items, Gp, a.stage_cap);
+        if (tl.staged) {
             __syncthreads();
-            stage_h<S, B>(s_col, s_h, a.colc, hval, k_lo, nk);
+            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
             __syncthreads();
         }
         const long long t = t0 + threadIdx.x;
-        if (t < items) {
-            const int il = (int)(t / Gp);
-            const int g = (int)(t - (long long)il * Gp);
-            const int i = sd.row_base + il;
+        if (t >= items) continue;
+        const int il = (int)(t / Gp);
+        const int g = (int)(t - (long long)il * Gp);
+        const int i = sd.row_base + il;
+        const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];
+        for (int c = 0; c < nch; c++) {
+            const int base = c * W;
             typename S::Acc acc[B][EPT];
 #pragma unroll
             for (int bi = 0; bi < B; bi++)
 #pragma unroll
                 for (int e = 0; e < EPT; e++) acc[bi][e] = S::zero();
-            const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];
-            if (staged) {
 #pragma unroll 2
-                for (int k = kb; k < ke; k++)
-                    block_mac<S, B, NP>(acc, s_col[k - k_lo], s_h + (size_t)(k - k_lo) * B * B, x, a.ld, g, Gp, a.P);
-            } else {
-#pragma unroll 2
-                for (int k = kb; k < ke; k++)
-                    block_mac<S, B, NP>(acc, __ldg(a.colc + k), hval + (size_t)k * B * B, x, a.ld, g, Gp, a.P);
+            for (int k = kb; k < ke; k++) {
+                const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
+                const H* hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
+                const int j = (int)(cc & kColMask);
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    E xv[EPT];
+                    ld_nc<S, NP>(xv, x + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                    mac_block<S, B, NP>(acc, cc >> 30, hk, xv, bj);
+                }
             }
             typename S::RowDot rxx = S::rd_zero(), ryx = S::rd_zero();
 #pragma unroll
             for (int bi = 0; bi < B; bi++) {
                 const size_t roff = (size_t)(B * i + bi) * a.ld;
                 E zv[EPT], yv[EPT];
-                if (a.has_z) ld_rw<S, NP>(zv, z + roff, g, Gp, a.P);
+                if (a.has_z) ld_rw<S, NP>(zv, z + roff, base, g, Gp, P);
                 else {
 #pragma unroll
                     for (int e = 0; e < EPT; e++) zv[e] = S::to(S::zero());
                 }
 #pragma unroll
                 for (int e = 0; e < EPT; e++) yv[e] = S::fin(acc[bi][e], a.two != 0, a.has_z != 0, zv[e]);
-                st<S, NP>(y + roff, yv, g, Gp, a.P);
+                st<S, NP>(y + roff, yv, base, g, Gp, P);
                 if (a.want_dots || a.xi_mode == 1) {
                     E xo[EPT];
-                    ld_nc<S, NP>(xo, x + roff, g, Gp, a.P);
+                    ld_nc<S, NP>(xo, x + roff, base, g, Gp, P);
                     if (a.want_dots) {
 #pragma unroll
                         for (int e = 0; e < EPT; e++) { S::rd_nrm(rxx, xo[e]); S::rd_re(ryx, yv[e], xo[e]); }
@@ -286,19 +305,19 @@ __global__ void __launch_bounds__(kThreads) k_cheb_step(StepArgs a) {
                             S::axpy(t2, c1, yv[e]);
                             xv2[e] = S::to(t2);
                         }
-                        st<S, NP>(xi + roff, xv2, g, Gp, a.P);
+                        st<S, NP>(xi + roff, xv2, base, g, Gp, P);
                     }
                 }
                 if (a.xi_mode == 2) {
                     E xv2[EPT];
-                    ld_rw<S, NP>(xv2, xi + roff, g, Gp, a.P);
+                    ld_rw<S, NP>(xv2, xi + roff, base, g, Gp, P);
 #pragma unroll
                     for (int e = 0; e < EPT; e++) {
                         typename S::Acc t2 = S::from(xv2[e]);
                         S::axpy(t2, c1, yv[e]);
                         xv2[e] = S::to(t2);
                     }
-                    st<S, NP>(xi + roff, xv2, g, Gp, a.P);
+                    st<S, NP>(xi + roff, xv2, base, g, Gp, P);
                 }
             }
             if (a.want_dots) { S::dot_add(dxx, rxx); S::dot_add(dyx, ryx); }
@@ -313,11 +332,61 @@ __global__ void __launch_bounds__(kThreads) k_cheb_step(StepArgs a) {
     }
 }
 
-// Sum over the Gp lanes of a row group (Gp a power of two <= 32, groups aligned in the warp).
-template <class S>
-__device__ __forceinline__ typename S::OAcc group_sum(typename S::OAcc v, int Gp) {
-    for (int off = Gp >> 1; off > 0; off >>= 1) v = S::oa_shfl_add(v, off);
-    return v;
+// Transposed reduction of V = 2^k values over the Gp lanes of a row group: at each of
+// the first min(k, log2 Gp) levels a lane keeps one half of its values and adds the
+// partner's copy of that half, so the live values halve while the reduction proceeds;
+// the remaining levels are plain butterflies. On return v[0..count) holds the complete
+// sums of values [first, first + count), and `writer` marks the one lane (of those
+// holding the same values) that stores them. The lane that stores a value depends
+// only on g, so successive chunks update each D entry from the same thread.
+template <class S, int V>
+__device__ __forceinline__ void group_sum_transposed(typename S::OAcc (&v)[V], int Gp, int g, int& first, int& count,
+                                                     bool& writer) {
+    int off = Gp >> 1, sel = 0, cur = V;
+#pragma unroll
+    for (int h = V >> 1; h >= 1; h >>= 1) {
+        if (off > 0) {
+            const bool up = (g & off) != 0;
+#pragma unroll
+            for (int i = 0; i < h; i++) {
+                const typename S::OAcc send = up ? v[i] : v[i + h];
+                const typename S::OAcc keep = up ? v[i + h] : v[i];
+                v[i] = S::oa_add(keep, S::oa_shfl(send, off));
+            }
+            sel = (sel << 1) | (up ? 1 : 0);
+            cur = h;
+            off >>= 1;
+        }
+    }
+    for (; off > 0; off >>= 1) {
+#pragma unroll
+        for (int i = 0; i < V; i++)
+            if (i < cur) v[i] = S::oa_add(v[i], S::oa_shfl(v[i], off));
+    }
+    count = cur;
+    first = sel * cur;
+    const int span = Gp / (V / cur);   // lanes holding the same values
+    writer = (g & (span - 1)) == 0;
+}
+
+// Reduce a block's per-lane D partials over the row group and add them to Dacc[k].
+template <class S, int B>
+__device__ __forceinline__ void flush_block(typename S::OAcc (&of)[B * B], int Gp, int g, bool has, size_t k,
+                                            double scale, double* Dacc) {
+    int first, count;
+    bool writer;
+    group_sum_transposed<S, B * B>(of, Gp, g, first, count, writer);
+    if (has && writer) {
+#pragma unroll
+        for (int t = 0; t < B * B; t++) {
+            if (t < count) {
+                const double2 v = S::oa_get(of[t]);
+                const size_t q = (k * B * B + first + t) * (S::CPLX ? 2 : 1);
+                Dacc[q] += scale * v.x;
+                if (S::CPLX) Dacc[q + 1] += scale * v.y;
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -327,10 +396,9 @@ __device__ __forceinline__ typename S::OAcc group_sum(typename S::OAcc v, int Gp
 // and, when Dacc != null (D's pattern is H's pattern), the outer-product epilogue
 //   D_k += dscale * sum_s alpha_m[b i + bi, s] conj(beta_{m+1}[b j + bj, s])
 // reusing the gathered beta_{m+1} rows of block k = (i, j).
-// Requires Gp to be a power of two <= 32 when the epilogue is on.
 // ---------------------------------------------------------------------------------
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads) k_adjoint_step(AdjArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_adjoint_step(AdjArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
     constexpr int EPT = NP * S::EPP;
@@ -341,7 +409,8 @@ __global__ void __launch_bounds__(kThreads) k_adjoint_step(AdjArgs a) {
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp;
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);
     E* Ap = reinterpret_cast<E*>(a.Ap);
@@ -354,139 +423,98 @@ __global__ void __launch_bounds__(kThreads) k_adjoint_step(AdjArgs a) {
     const bool fuse = a.Dacc != nullptr;
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
-        const int r_lo = sd.row_base + (int)(t0 / Gp);
-        const long long t_last = min(t0 + kThreads, items) - 1;
-        const int r_hi = sd.row_base + (int)(t_last / Gp);
-        const int k_lo = a.row_ptr[r_lo];
-        const int nk = a.row_ptr[r_hi + 1] - k_lo;
-        const bool staged = nk <= a.stage_cap;
-        if (staged) {
+        const Tile tl = tile_range(a.row_ptr, sd, t0, items, Gp, a.stage_cap);
+        if (tl.staged) {
             __syncthreads();
-            stage_h<S, B>(s_col, s_h, a.colc, hval, k_lo, nk);
+            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
             __syncthreads();
         }
         const long long t = t0 + threadIdx.x;
         const bool active = t < items;
         const int il = active ? (int)(t / Gp) : 0;
-        const int g = active ? (int)(t - (long long)il * Gp) : 0;
+        const int g = active ? (int)(t - (long long)il * Gp) : (int)(threadIdx.x % Gp);
         const int i = sd.row_base + il;
         const int kb = active ? a.row_ptr[i] : 0;
         const int ke = active ? a.row_ptr[i + 1] : 0;
-
-        E Ai[B][EPT];
-        if (active) {
+        // With the epilogue every lane of the warp walks the longest row of the warp so
+        // that the group reductions see all 32 lanes; missing blocks contribute zero.
+        int nmax = ke - kb;
+        if (fuse) {
 #pragma unroll
-            for (int bi = 0; bi < B; bi++) ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, g, Gp, a.P);
-        } else {
+            for (int off = 16; off > 0; off >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
+        } else if (!active) {
+            continue;
+        }
+        for (int c = 0; c < nch; c++) {
+            const int base = c * W;
+            E Ai[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                if (active) ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                else {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) Ai[bi][e] = S::to(S::zero());
+                }
+            }
+            typename S::Acc accA[B][EPT], accB[B][EPT];
 #pragma unroll
             for (int bi = 0; bi < B; bi++)
 #pragma unroll
-                for (int e = 0; e < EPT; e++) Ai[bi][e] = S::to(S::zero());
-        }
-        typename S::Acc accA[B][EPT], accB[B][EPT];
-#pragma unroll
-        for (int bi = 0; bi < B; bi++)
-#pragma unroll
-            for (int e = 0; e < EPT; e++) { accA[bi][e] = S::zero(); accB[bi][e] = S::zero(); }
+                for (int e = 0; e < EPT; e++) { accA[bi][e] = S::zero(); accB[bi][e] = S::zero(); }
 
-        if (fuse) {
-            // Every lane of the warp walks the longest row of the warp so that the
-            // group reductions see all 32 lanes; missing blocks contribute zero.
-            int nmax = ke - kb;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
             for (int kk = 0; kk < nmax; kk++) {
                 const int k = kb + kk;
                 const bool has = kk < ke - kb;
                 unsigned cc = 0;
-                const H* hk = nullptr;
+                const H* hk = hval;
                 if (has) {
-                    cc = staged ? s_col[k - k_lo] : __ldg(a.colc + k);
-                    hk = staged ? s_h + (size_t)(k - k_lo) * B * B : hval + (size_t)k * B * B;
+                    cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
+                    hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
                 }
                 const int j = (int)(cc & kColMask);
-                typename S::OAcc o[B][B];
+                typename S::OAcc of[B * B];
+#pragma unroll
+                for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
 #pragma unroll
                 for (int bj = 0; bj < B; bj++) {
                     E av[EPT], bv[EPT];
                     if (has) {
-                        ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
-                        ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
+                        ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        mac_block<S, B, NP>(accA, cc >> 30, hk, av, bj);
+                        mac_block<S, B, NP>(accB, cc >> 30, hk, bv, bj);
                     } else {
 #pragma unroll
-                        for (int e = 0; e < EPT; e++) { av[e] = S::to(S::zero()); bv[e] = av[e]; }
+                        for (int e = 0; e < EPT; e++) bv[e] = S::to(S::zero());
                     }
+                    if (fuse) {
 #pragma unroll
-                    for (int bi = 0; bi < B; bi++) {
-                        o[bi][bj] = S::oa_zero();
+                        for (int bi = 0; bi < B; bi++)
 #pragma unroll
-                        for (int e = 0; e < EPT; e++) S::oa_mac(o[bi][bj], Ai[bi][e], bv[e]);
-                    }
-                    if (has) {
-                        const unsigned cls = cc >> 30;
-                        if (cls == 2u) {
-                            const typename S::Hr h = S::hreal(hk[bj * B + bj]);
-#pragma unroll
-                            for (int e = 0; e < EPT; e++) { S::mac_re(accA[bj][e], h, av[e]); S::mac_re(accB[bj][e], h, bv[e]); }
-                        } else if (!S::CPLX || cls == 1u) {
-#pragma unroll
-                            for (int bi = 0; bi < B; bi++) {
-                                const typename S::Hr h = S::hreal(hk[bj * B + bi]);
-#pragma unroll
-                                for (int e = 0; e < EPT; e++) { S::mac_re(accA[bi][e], h, av[e]); S::mac_re(accB[bi][e], h, bv[e]); }
-                            }
-                        } else {
-#pragma unroll
-                            for (int bi = 0; bi < B; bi++) {
-                                const H h = hk[bj * B + bi];
-#pragma unroll
-                                for (int e = 0; e < EPT; e++) { S::mac(accA[bi][e], h, av[e]); S::mac(accB[bi][e], h, bv[e]); }
-                            }
-                        }
+                            for (int e = 0; e < EPT; e++) S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
                     }
                 }
-#pragma unroll
-                for (int bj = 0; bj < B; bj++)
-#pragma unroll
-                    for (int bi = 0; bi < B; bi++) o[bi][bj] = group_sum<S>(o[bi][bj], Gp);
-                if (has && g == 0) {
-#pragma unroll
-                    for (int bj = 0; bj < B; bj++)
-#pragma unroll
-                        for (int bi = 0; bi < B; bi++) {
-                            const double2 v = S::oa_get(o[bi][bj]);
-                            const size_t q = ((size_t)k * B * B + bj * B + bi) * (S::CPLX ? 2 : 1);
-                            a.Dacc[q] += a.dscale * v.x;
-                            if (S::CPLX) a.Dacc[q + 1] += a.dscale * v.y;
-                        }
-                }
+                if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, a.Dacc);
             }
-        } else if (active) {
-            for (int k = kb; k < ke; k++) {
-                const unsigned cc = staged ? s_col[k - k_lo] : __ldg(a.colc + k);
-                const H* hk = staged ? s_h + (size_t)(k - k_lo) * B * B : hval + (size_t)k * B * B;
-                block_mac<S, B, NP>(accA, cc, hk, A, a.ld, g, Gp, a.P);
-                block_mac<S, B, NP>(accB, cc, hk, Bv, a.ld, g, Gp, a.P);
-            }
-        }
-        if (active) {
+            if (active) {
 #pragma unroll
-            for (int bi = 0; bi < B; bi++) {
-                const size_t roff = (size_t)(B * i + bi) * a.ld;
-                E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
-                ld_rw<S, NP>(apv, Ap + roff, g, Gp, a.P);
-                ld_rw<S, NP>(bpv, Bp + roff, g, Gp, a.P);
+                for (int bi = 0; bi < B; bi++) {
+                    const size_t roff = (size_t)(B * i + bi) * a.ld;
+                    E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
+                    ld_rw<S, NP>(apv, Ap + roff, base, g, Gp, P);
+                    ld_rw<S, NP>(bpv, Bp + roff, base, g, Gp, P);
 #pragma unroll
-                for (int e = 0; e < EPT; e++) {
-                    an[e] = S::fin(accA[bi][e], true, true, apv[e]);
-                    typename S::Acc tb = S::from(S::fin(accB[bi][e], true, true, bpv[e]));
-                    S::axpy(tb, cA, Ai[bi][e]);
-                    S::axpy(tb, cAp, apv[e]);
-                    S::axpy(tb, cAn, an[e]);
-                    bn[e] = S::to(tb);
+                    for (int e = 0; e < EPT; e++) {
+                        an[e] = S::fin(accA[bi][e], true, true, apv[e]);
+                        typename S::Acc tb = S::from(S::fin(accB[bi][e], true, true, bpv[e]));
+                        S::axpy(tb, cA, Ai[bi][e]);
+                        S::axpy(tb, cAp, apv[e]);
+                        S::axpy(tb, cAn, an[e]);
+                        bn[e] = S::to(tb);
+                    }
+                    st<S, NP>(Ap + roff, an, base, g, Gp, P);
+                    st<S, NP>(Bp + roff, bn, base, g, Gp, P);
                 }
-                st<S, NP>(Ap + roff, an, g, Gp, a.P);
-                st<S, NP>(Bp + roff, bn, g, Gp, a.P);
             }
         }
     }
@@ -495,91 +523,84 @@ __global__ void __launch_bounds__(kThreads) k_adjoint_step(AdjArgs a) {
 // ---------------------------------------------------------------------------------
 // Sparsity-restricted outer product on D's pattern (the reference's
 // outer_product_kernel role, src/outer_product.cu:38-60, re-designed):
-//   D_k(bi,bj) += alpha1 sum_s A[b i+bi, s] conj(B[b j+bj, s])
-//              +  alpha2 sum_s B[b i+bi, s] conj(A[b j+bj, s])
-// One row group (Gp lanes) per block row of D; own rows held in registers,
-// partner rows gathered once per block, reduction over S by warp shuffles,
-// FP64 accumulation into Dacc. Gp must be a power of two <= 32.
+//   D_k(bi,bj) += alpha sum_s ( A[b i+bi, s] conj(B[b j+bj, s])
+//                             [+ B[b i+bi, s] conj(A[b j+bj, s])] )
+// One row group (Gp lanes) per block row of D; own rows held in registers per
+// column chunk, partner rows gathered once per block, transposed reduction over
+// the lanes, FP64 accumulation into Dacc.
 // ---------------------------------------------------------------------------------
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads) k_outer(OuterArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
     typedef typename S::E E;
     constexpr int EPT = NP * S::EPP;
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp;
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);
     const E* Bv = reinterpret_cast<const E*>(a.Bv);
-    const bool two_terms = a.alpha2 != 0.0;
+    const bool two_terms = a.two_terms != 0;
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
         const long long t = t0 + threadIdx.x;
         const bool active = t < items;
         const int il = active ? (int)(t / Gp) : 0;
-        const int g = active ? (int)(t - (long long)il * Gp) : 0;
+        const int g = active ? (int)(t - (long long)il * Gp) : (int)(threadIdx.x % Gp);
         const int i = sd.row_base + il;
         const int kb = active ? a.row_ptr[i] : 0;
         const int ke = active ? a.row_ptr[i + 1] : 0;
-        E Ai[B][EPT], Bi[B][EPT];
-#pragma unroll
-        for (int bi = 0; bi < B; bi++) {
-            if (active) {
-                ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, g, Gp, a.P);
-                if (two_terms) ld_nc<S, NP>(Bi[bi], Bv + (size_t)(B * i + bi) * a.ld, g, Gp, a.P);
-            } else {
-#pragma unroll
-                for (int e = 0; e < EPT; e++) { Ai[bi][e] = S::to(S::zero()); Bi[bi][e] = Ai[bi][e]; }
-            }
-        }
         int nmax = ke - kb;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
-        for (int kk = 0; kk < nmax; kk++) {
-            const int k = kb + kk;
-            const bool has = kk < ke - kb;
-            const int j = has ? (int)(__ldg(a.colc + k) & kColMask) : 0;
-            typename S::OAcc o1[B][B], o2[B][B];
+        for (int c = 0; c < nch; c++) {
+            const int base = c * W;
+            E Ai[B][EPT], Bi[B][EPT];
 #pragma unroll
-            for (int bj = 0; bj < B; bj++) {
-                E bv[EPT], av[EPT];
-                if (has) {
-                    ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
-                    if (two_terms) ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, g, Gp, a.P);
+            for (int bi = 0; bi < B; bi++) {
+                if (active) {
+                    ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                    if (two_terms) ld_nc<S, NP>(Bi[bi], Bv + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                    else {
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) Bi[bi][e] = S::to(S::zero());
+                    }
                 } else {
 #pragma unroll
-                    for (int e = 0; e < EPT; e++) { bv[e] = S::to(S::zero()); av[e] = bv[e]; }
-                }
-#pragma unroll
-                for (int bi = 0; bi < B; bi++) {
-                    o1[bi][bj] = S::oa_zero();
-                    o2[bi][bj] = S::oa_zero();
-#pragma unroll
-                    for (int e = 0; e < EPT; e++) {
-                        S::oa_mac(o1[bi][bj], Ai[bi][e], bv[e]);
-                        if (two_terms) S::oa_mac(o2[bi][bj], Bi[bi][e], av[e]);
-                    }
+                    for (int e = 0; e < EPT; e++) { Ai[bi][e] = S::to(S::zero()); Bi[bi][e] = Ai[bi][e]; }
                 }
             }
+            for (int kk = 0; kk < nmax; kk++) {
+                const int k = kb + kk;
+                const bool has = kk < ke - kb;
+                const int j = has ? (int)(__ldg(a.colc + k) & kColMask) : 0;
+                typename S::OAcc of[B * B];
 #pragma unroll
-            for (int bj = 0; bj < B; bj++)
+                for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
 #pragma unroll
-                for (int bi = 0; bi < B; bi++) {
-                    o1[bi][bj] = group_sum<S>(o1[bi][bj], Gp);
-                    if (two_terms) o2[bi][bj] = group_sum<S>(o2[bi][bj], Gp);
-                }
-            if (has && g == 0) {
+                for (int bj = 0; bj < B; bj++) {
+                    E bv[EPT], av[EPT];
+                    if (has) {
+                        ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        if (two_terms) ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        else {
 #pragma unroll
-                for (int bj = 0; bj < B; bj++)
+                            for (int e = 0; e < EPT; e++) av[e] = S::to(S::zero());
+                        }
+                    } else {
 #pragma unroll
-                    for (int bi = 0; bi < B; bi++) {
-                        const double2 v1 = S::oa_get(o1[bi][bj]);
-                        const double2 v2 = two_terms ? S::oa_get(o2[bi][bj]) : make_double2(0.0, 0.0);
-                        const size_t q = ((size_t)k * B * B + bj * B + bi) * (S::CPLX ? 2 : 1);
-                        a.Dacc[q] += a.alpha1 * v1.x + a.alpha2 * v2.x;
-                        if (S::CPLX) a.Dacc[q + 1] += a.alpha1 * v1.y + a.alpha2 * v2.y;
+                        for (int e = 0; e < EPT; e++) { bv[e] = S::to(S::zero()); av[e] = bv[e]; }
                     }
+#pragma unroll
+                    for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) {
+                            S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
+                            if (two_terms) S::oa_mac(of[bj * B + bi], Bi[bi][e], av[e]);
+                        }
+                }
+                flush_block<S, B>(of, Gp, g, has, (size_t)k, a.alpha, a.Dacc);
             }
         }
     }
@@ -626,33 +647,11 @@ __global__ void k_scale(const typename S::E* x, typename S::E* y, long long n_el
         y[q] = S::scale(cc, x[q]);
 }
 
-// Sum the per-CTA moment partials of every (system, step) in a fixed order:
-// raw[(step * n_sys + s) * 2 + {0,1}]. One warp per (system, step).
-static __global__ void k_reduce_partials(const double* partials, int grid, int nsteps, const SysDesc* sys, int n_sys,
-                                  double* raw) {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (w >= nsteps * n_sys) return;
-    const int step = w / n_sys, s = w - step * n_sys;
-    const double* p = partials + (size_t)step * grid * 2;
-    double a = 0.0, b = 0.0;
-    for (int c = sys[s].cta_base + lane; c < sys[s].cta_base + sys[s].ctas; c += 32) {
-        a += p[2 * c];
-        b += p[2 * c + 1];
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, off);
-        b += __shfl_xor_sync(0xffffffffu, b, off);
-    }
-    if (lane == 0) { raw[2 * w] = a; raw[2 * w + 1] = b; }
-}
-
 // D <- (D + D^T-pair^dagger)/2 blockwise, then * scale (SpMatBsr::symmetrize and
 // scale, src/spmat.cpp:171-198, done on the device). pair[k] is the block index of
 // (j, i) for k = (i, j). Each unordered pair is handled by the block with i >= j.
 static __global__ void k_symmetrize_scale(double* D, const int* rows, const int* cols, const int* pair, int nnzb, int b,
-                                   int cplx, double scale) {
+                                          int cplx, double scale) {
     const int bb = b * b;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)nnzb * bb;
          q += (long long)gridDim.x * blockDim.x) {

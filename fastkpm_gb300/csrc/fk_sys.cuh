@@ -95,6 +95,8 @@ struct SysF64R {
     __device__ static void oa_mac(OAcc& o, E a, E b) { o = fma(a, b, o); }          // o += a conj(b)
     __device__ static OAcc oa_shfl_add(OAcc o, int off) { return o + __shfl_xor_sync(0xffffffffu, o, off); }
     __device__ static double2 oa_get(OAcc o) { return make_double2(o, 0.0); }
+    __device__ static OAcc oa_add(OAcc a, OAcc b) { return a + b; }
+    __device__ static OAcc oa_shfl(OAcc o, int off) { return __shfl_xor_sync(0xffffffffu, o, off); }
     __device__ static E from_double2(double2 v) { return v.x; }
     __device__ static double2 to_double2(E x) { return make_double2(x, 0.0); }
 };
@@ -136,6 +138,10 @@ struct SysF64C {
                             o.y + __shfl_xor_sync(0xffffffffu, o.y, off));
     }
     __device__ static double2 oa_get(OAcc o) { return o; }
+    __device__ static OAcc oa_add(OAcc a, OAcc b) { return make_double2(a.x + b.x, a.y + b.y); }
+    __device__ static OAcc oa_shfl(OAcc o, int off) {
+        return make_double2(__shfl_xor_sync(0xffffffffu, o.x, off), __shfl_xor_sync(0xffffffffu, o.y, off));
+    }
     __device__ static E from_double2(double2 v) { return v; }
     __device__ static double2 to_double2(E x) { return x; }
 };
@@ -172,6 +178,8 @@ struct SysF32R {
     __device__ static void oa_mac(OAcc& o, E a, E b) { o = fmaf(a, b, o); }
     __device__ static OAcc oa_shfl_add(OAcc o, int off) { return o + __shfl_xor_sync(0xffffffffu, o, off); }
     __device__ static double2 oa_get(OAcc o) { return make_double2((double)o, 0.0); }
+    __device__ static OAcc oa_add(OAcc a, OAcc b) { return a + b; }
+    __device__ static OAcc oa_shfl(OAcc o, int off) { return __shfl_xor_sync(0xffffffffu, o, off); }
     __device__ static E from_double2(double2 v) { return __double2float_rn(v.x); }
     __device__ static double2 to_double2(E x) { return make_double2((double)x, 0.0); }
 };
@@ -217,6 +225,10 @@ struct SysF32C {
                            o.y + __shfl_xor_sync(0xffffffffu, o.y, off));
     }
     __device__ static double2 oa_get(OAcc o) { return make_double2((double)o.x, (double)o.y); }
+    __device__ static OAcc oa_add(OAcc a, OAcc b) { return make_float2(a.x + b.x, a.y + b.y); }
+    __device__ static OAcc oa_shfl(OAcc o, int off) {
+        return make_float2(__shfl_xor_sync(0xffffffffu, o.x, off), __shfl_xor_sync(0xffffffffu, o.y, off));
+    }
     __device__ static E from_double2(double2 v) { return make_float2(__double2float_rn(v.x), __double2float_rn(v.y)); }
     __device__ static double2 to_double2(E x) { return make_double2((double)x.x, (double)x.y); }
 };
@@ -260,6 +272,10 @@ struct SysDSR {
         return ds_norm(o);
     }
     __device__ static double2 oa_get(OAcc o) { return make_double2(ds_to_double(o), 0.0); }
+    __device__ static OAcc oa_add(OAcc a, OAcc b) { ds_add(a, b); return a; }
+    __device__ static OAcc oa_shfl(OAcc o, int off) {
+        return make_float2(__shfl_xor_sync(0xffffffffu, o.x, off), __shfl_xor_sync(0xffffffffu, o.y, off));
+    }
     __device__ static E from_double2(double2 v) { return ds_from_double(v.x); }
     __device__ static double2 to_double2(E x) { return make_double2(ds_to_double(x), 0.0); }
 };
@@ -321,6 +337,16 @@ struct SysDSC {
         return pack(SysDSR::oa_shfl_add(re(o), off), SysDSR::oa_shfl_add(im(o), off));
     }
     __device__ static double2 oa_get(OAcc o) { return make_double2(ds_to_double(re(o)), ds_to_double(im(o))); }
+    __device__ static OAcc oa_add(OAcc a, OAcc b) {
+        float2 r = re(a), i = im(a);
+        ds_add(r, re(b));
+        ds_add(i, im(b));
+        return pack(r, i);
+    }
+    __device__ static OAcc oa_shfl(OAcc o, int off) {
+        return make_float4(__shfl_xor_sync(0xffffffffu, o.x, off), __shfl_xor_sync(0xffffffffu, o.y, off),
+                           __shfl_xor_sync(0xffffffffu, o.z, off), __shfl_xor_sync(0xffffffffu, o.w, off));
+    }
     __device__ static E from_double2(double2 v) { return pack(ds_from_double(v.x), ds_from_double(v.y)); }
     __device__ static double2 to_double2(E x) { return make_double2(ds_to_double(re(x)), ds_to_double(im(x))); }
 };

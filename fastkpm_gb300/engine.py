@@ -437,6 +437,8 @@ class Batch:
         dt = np.complex128 if self.complex_values else np.float64
         R = np.asarray(R, dtype=dt)
         n, s = R.shape
+        if n != H.n_rows * H.b_len:
+            raise ValueError("R has %d rows; H has %d scalar rows" % (n, H.n_rows * H.b_len))
         flat = np.ascontiguousarray(R.reshape(-1, order="F"))
         idx = C.c_int(0)
         self._check(self.lib.fk_batch_add(self.h, H.n_rows, H.b_len, H.n_blocks(), _ip(H.row_ptr), _ip(H.col_idx),

@@ -1,0 +1,262 @@
+"""Serving loop: continuous batching of KPM solves (moments + D on H's pattern).
+
+Requests are queued as they arrive. A dispatcher admits them into slots while
+device memory and slots allow (first fit in arrival order, with a guard so a
+large request at the head is not starved); each slot is a worker thread with
+its own GB300 engine and CUDA stream, so admitted solves of different sizes
+run concurrently on the device, and a request that arrives while others are
+running starts as soon as a slot and its memory are free. Probe and recursion
+state stay on the device for the whole solve (moments -> autodiff_matrix).
+Every kernel's per-system reduction order depends only on that system, so a
+request's result is the same alone and in any mix.
+
+    srv = Server(max_slots=8, memory_budget=100 << 30)
+    t = srv.submit(Request(H, es, R, M, c))
+    srv.wait(t)  ->  t.mu, t.D, t.latency
+"""
+import collections
+import threading
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .engine import Engine
+
+
+class Request:
+    """One KPM solve: moments(M), then autodiff_matrix(c, D) ("autodiff") or
+    stoch_matrix(c, D) ("stoch") on H's pattern."""
+
+    _next = 0
+    _lock = threading.Lock()
+
+    def __init__(self, H, es, R, M, c, kind="autodiff", precision="fp32", arrival=None):
+        with Request._lock:
+            self.id = Request._next
+            Request._next += 1
+        self.H, self.es, self.R, self.M, self.c = H, es, np.asfortranarray(R), int(M), np.asarray(c, float)
+        self.kind = kind
+        self.precision = precision
+        self.complex_values = bool(np.iscomplexobj(R) or H.is_complex)
+        self.arrival = time.perf_counter() if arrival is None else arrival
+        self.admitted = None
+        self.finished = None
+        self.mu = None
+        self.D = None
+        self.error = None
+        self.done = threading.Event()
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+    def probe_steps(self):
+        return float(self.R.shape[0]) * self.M * self.R.shape[1]
+
+    def footprint(self):
+        """Device bytes an engine needs for this solve (vectors, H, D, scratch)."""
+        n, s = self.R.shape
+        es = {"fp64": 8, "ds": 8, "fp32": 4}[self.precision] * (2 if self.complex_values else 1)
+        epp = 16 // es
+        ld = (s + epp - 1) // epp * epp
+        vec = 5 * n * ld * es
+        nnzb = self.H.n_blocks() + self.H.n_rows
+        b2 = self.H.b_len ** 2
+        h = nnzb * (b2 * es + 4) + 4 * (self.H.n_rows + 1)
+        d = nnzb * b2 * 16 * 2 + nnzb * 16
+        stage = min(256 << 20, n * s * 16)
+        scratch = self.M * 8 * 2 * 152 * 8 + (1 << 20)
+        return vec + h + d + stage + scratch
+
+
+class _Slot:
+    def __init__(self, server, idx):
+        self.server = server
+        self.idx = idx
+        self.engines = {}
+        self.req = None
+        self.wake = threading.Event()
+        self.thread = threading.Thread(target=self._run, name="fkpm-slot-%d" % idx, daemon=True)
+        self.thread.start()
+
+    def capacity(self):
+        return sum(e.memory() for e in self.engines.values())
+
+    def engine(self, req):
+        key = (req.complex_values, req.precision)
+        e = self.engines.get(key)
+        if e is None:
+            e = Engine(req.complex_values, req.precision, device=self.server.device)
+            self.engines[key] = e
+        return e
+
+    def _run(self):
+        while True:
+            self.wake.wait()
+            self.wake.clear()
+            req = self.req
+            if req is None:
+                if self.server._stopping:
+                    return
+                continue
+            try:
+                eng = self.engine(req)
+                eng.set_H(req.H, req.es)
+                eng.set_R(req.R)
+                req.mu = eng.moments(req.M)
+                D = req.H.pattern_like(req.complex_values)
+                if req.kind == "autodiff":
+                    eng.autodiff_matrix(req.c, D)
+                elif req.kind == "stoch":
+                    eng.stoch_matrix(req.c, D)
+                req.D = D.val
+            except Exception as ex:   # the request fails, the server keeps serving
+                req.error = ex
+            req.finished = time.perf_counter()
+            self.req = None
+            self.server._slot_done(self, req)
+
+
+class Server:
+    def __init__(self, device=0, max_slots=8, memory_budget=None, lookahead=64, max_bypass=16):
+        self.device = device
+        lib = L.load()
+        if memory_budget is None:
+            import ctypes as C
+            free = C.c_size_t(0)
+            total = C.c_size_t(0)
+            memory_budget = 0
+            try:
+                from . import engine as _e   # noqa: F401
+                memory_budget = int(0.8 * self._device_free())
+            except Exception:
+                memory_budget = 64 << 30
+        self.budget = int(memory_budget)
+        self.lookahead = lookahead
+        self.max_bypass = max_bypass
+        self._lock = threading.Condition()
+        self._queue = collections.deque()
+        self._stopping = False
+        self._slots = [_Slot(self, k) for k in range(max_slots)]
+        self._reserved = {}           # slot idx -> bytes reserved by its request
+        self.completed = []
+        self.rejected = []
+        self.max_concurrent = 0
+        self._head_bypassed = 0
+        self._dispatcher = threading.Thread(target=self._dispatch, name="fkpm-dispatch", daemon=True)
+        self._dispatcher.start()
+
+    @staticmethod
+    def _device_free():
+        import ctypes as C
+        import ctypes.util
+        cudart = None
+        for name in ("libcudart.so", "libcudart.so.13", "libcudart.so.12"):
+            try:
+                cudart = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        if cudart is None:
+            raise OSError("no libcudart")
+        free = C.c_size_t()
+        total = C.c_size_t()
+        cudart.cudaMemGetInfo(C.byref(free), C.byref(total))
+        return free.value
+
+    # -- client side --
+    def submit(self, req):
+        if req.footprint() > self.budget:
+            req.error = L.FkError(L.FK_ERR_OOM, "admission", "request needs %d bytes, budget %d" % (req.footprint(), self.budget))
+            req.finished = time.perf_counter()
+            req.done.set()
+            with self._lock:
+                self.rejected.append(req)
+            return req
+        with self._lock:
+            self._queue.append(req)
+            self._lock.notify_all()
+        return req
+
+    def wait(self, req, timeout=None):
+        if not req.done.wait(timeout):
+            raise TimeoutError("request %d not finished" % req.id)
+        if req.error is not None:
+            raise req.error
+        return req
+
+    def drain(self, timeout=None):
+        t_end = None if timeout is None else time.perf_counter() + timeout
+        with self._lock:
+            while self._queue or any(s.req is not None for s in self._slots):
+                left = None if t_end is None else t_end - time.perf_counter()
+                if left is not None and left <= 0:
+                    raise TimeoutError("server did not drain")
+                self._lock.wait(left if left is not None else 1.0)
+
+    def stop(self):
+        self.drain()
+        with self._lock:
+            self._stopping = True
+            self._lock.notify_all()
+        for s in self._slots:
+            s.wake.set()
+        for s in self._slots:
+            s.thread.join(timeout=30)
+            for e in s.engines.values():
+                e.close()
+
+    # -- server side --
+    def _used(self):
+        return sum(self._reserved.values())
+
+    def _need(self, slot, req):
+        """Bytes this slot would hold with req admitted (engine buffers only grow)."""
+        return max(slot.capacity(), req.footprint())
+
+    def _dispatch(self):
+        with self._lock:
+            while not self._stopping:
+                admitted = False
+                free_slots = [s for s in self._slots if s.req is None]
+                if self._queue and free_slots:
+                    # first fit in arrival order; the head may be bypassed at most max_bypass times
+                    for qi, req in enumerate(list(self._queue)[:self.lookahead]):
+                        if qi > 0 and self._head_bypassed >= self.max_bypass:
+                            break
+                        slot = min(free_slots, key=lambda s: abs(s.capacity() - req.footprint()))
+                        need = self._need(slot, req)
+                        if self._used() - self._reserved.get(slot.idx, 0) + need <= self.budget:
+                            self._queue.remove(req)
+                            self._head_bypassed = self._head_bypassed + 1 if qi > 0 else 0
+                            self._reserved[slot.idx] = need
+                            req.admitted = time.perf_counter()
+                            slot.req = req
+                            slot.wake.set()
+                            admitted = True
+                            busy = sum(1 for s in self._slots if s.req is not None)
+                            self.max_concurrent = max(self.max_concurrent, busy)
+                            break
+                if not admitted:
+                    self._lock.wait(0.05)
+
+    def _slot_done(self, slot, req):
+        with self._lock:
+            self._reserved[slot.idx] = slot.capacity()
+            if req.error is None:
+                self.completed.append(req)
+            else:
+                self.rejected.append(req)
+            req.done.set()
+            self._lock.notify_all()
+
+    def stats(self):
+        lat = np.array([r.latency for r in self.completed]) if self.completed else np.zeros(1)
+        t0 = min((r.arrival for r in self.completed), default=0.0)
+        t1 = max((r.finished for r in self.completed), default=0.0)
+        work = sum(r.probe_steps() for r in self.completed)
+        return {"completed": len(self.completed), "rejected": len(self.rejected),
+                "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "probe_steps_per_s": work / max(t1 - t0, 1e-9), "wall_s": t1 - t0,
+                "max_concurrent": self.max_concurrent, "budget_bytes": self.budget}

@@ -144,7 +144,7 @@ typedef struct fk_batch fk_batch;
 int  fk_batch_create(int device, int kind, int precision, fk_batch** out);
 int  fk_batch_destroy(fk_batch* bt);
 const char* fk_batch_last_error(const fk_batch* bt);
-/* Add one system (its H as in fk_engine_set_H and its column-major n x s probe block R);
+/* Add one system (its H as in fk_engine_set_H and its column-major (n_b*b) x s probe block R);
  * *index receives its position. Takes effect at the next fk_batch_commit. */
 int  fk_batch_add(fk_batch* bt, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
                   const double* val, double es_lo, double es_hi, int s, const double* R, int* index);

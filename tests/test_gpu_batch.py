@@ -65,7 +65,7 @@ def test_batch_complex_spin_blocks(gpu):
     systems = []
     for k, L_ in enumerate([3, 4, 2]):
         H, es, _ = W.cubic_spin_lattice(L_, -1.0, 1.0, seed=k)
-        R = W.phase_probes(np.arange(H.n_rows) % 8, 1, seed=k)
+        R = W.phase_probes(np.arange(2 * H.n_rows) % 8, 1, seed=k)
         systems.append((H, es, R))
     M = 30
     bt = fk.Batch(True, "ds")
@@ -103,6 +103,8 @@ def test_batch_rejects_mixed_shapes(gpu):
     with pytest.raises(L.FkError) as ei:
         bt.add(H, es, fk.probe_uncorrelated(16, 4, fk.RNG(1)))
     assert ei.value.status == L.FK_ERR_ARG
+    with pytest.raises(ValueError):
+        bt.add(H, es, fk.probe_uncorrelated(15, 8, fk.RNG(1)))   # R rows must be b * n_b
     with pytest.raises(L.FkError) as ei:
         fk.Batch(False, "fp32").moments(10)
     assert ei.value.status == L.FK_ERR_STATE
