@@ -68,6 +68,7 @@ SIGNATURES = {
     "fk_batch_timer_start": (_i, [_p]),
     "fk_batch_timer_stop": (_i, [_p, _dp]),
     "fk_batch_info": (_i, [_p, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_size_t)]),
+    "fk_moments_noalloc": (_i, [_i, _i, _i, _p, _p, _p, C.c_longlong, _i, _p, _p, _i, _dp, _p]),
     "fk_bsr_build": (_i, [_i, _i, _i, _i, _ip, _ip, _dp, _ip, _ip, _ip, _dp, _ip]),
     "fk_bsr_symmetrize": (_i, [_i, _i, _i, _i, _ip, _ip, _ip, _dp]),
     "fk_probe_identity": (_i, [_i, _i, _i, _i, _dp]),

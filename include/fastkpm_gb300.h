@@ -164,6 +164,33 @@ int  fk_batch_timer_start(fk_batch* bt);
 int  fk_batch_timer_stop(fk_batch* bt, double* ms);
 int  fk_batch_info(const fk_batch* bt, int* n_systems, long long* total_rows, size_t* device_bytes);
 
+/* ---- moments without device allocation ----
+ * No counterpart in the reference (its engines cudaMalloc inside every call). For callers
+ * that cannot allocate device memory: their device memory is owned by another allocator
+ * (a host application's pool, or a fixed reservation made at start-up that nothing else may
+ * grow), or they must not trigger the device-wide synchronisation that cudaFree implies while
+ * their other streams run. Same result as fk_engine_moments in native FP64, on buffers the
+ * caller already holds; the kernels' scratch (moment partials, per-step sums, launch tables)
+ * is one static device array of under 300 KiB in the library, held by every GPU that loads it
+ * until the process exits. Nothing is allocated: no cudaMalloc, cudaFree or allocating library
+ * routine is called.
+ *   d_row_ptr[n_b+1], d_col_idx[nnzb] (each < 2^30), d_hs_val[nnzb*b*b]: the SCALED matrix
+ *     Hs = (H - avg I)/mag as device BSR (column-major b x b blocks; interleaved (re, im) for
+ *     FK_COMPLEX); the pattern is trusted, not checked.
+ *   d_R: device, row-major (n_b*b) x ld doubles (complex: pairs), zero in columns s..ld-1;
+ *     ld a multiple of 2 for FK_REAL; 16-byte aligned.  d_work: device, 2 * (n_b*b) * ld
+ *     elements for the two recursion vectors (overwritten).  mu: host, M doubles out.
+ *   stream: a cudaStream_t or NULL (the legacy default stream); the call waits for it.
+ * Limits: even M with 2 <= M <= 32768; larger M returns FK_ERR_UNSUPPORTED (the static
+ * scratch holds 16384 steps); malformed arguments return FK_ERR_ARG.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture. All calls share
+ * the array and it keeps the last call's contents, so calls that overlap on the GPU (from
+ * different streams or threads) race with each other: serialise them. */
+int  fk_moments_noalloc(int kind, int n_b, int b, const int* d_row_ptr, const int* d_col_idx,
+                        const double* d_hs_val, long long ld, int s, const double* d_R, double* d_work,
+                        int M, double* mu, void* stream);
+
 /* ---- host helpers of the drop-in layer (no device work) ---- */
 /* SpMatBsr::build (reference src/spmat.cpp:46-129): sort blocks by (row, col), sum duplicates.
  * Out arrays sized for n_elems blocks; returns FK_OK and *nnzb_out. */
