@@ -47,6 +47,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-M", type=int, default=8)
+    p.add_argument("--workload", default="solve", choices=["solve", "precision", "batch", "serve", "cfg1"])
+    p.add_argument("--serve-requests", type=int, default=24)
+    p.add_argument("--serve-max-sites", type=float, default=1e6)
     return p.parse_args()
 
 
@@ -324,11 +327,284 @@ def run_reference(args, rank, ws, dist):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------- other configurations
+def _mu_err(mu, ref):
+    return float(np.max(np.abs(np.asarray(mu) - ref)) / abs(ref[0]))
+
+
+def _d_err(d, ref):
+    return float(np.linalg.norm(d - ref) / np.linalg.norm(ref))
+
+
+def _solve_timed(eng, M, c, D, steps, warmup):
+    for _ in range(warmup):
+        eng.moments_async(M)
+        eng.autodiff_matrix_async(c, D)
+    eng.synchronize()
+    eng.timer_start()
+    for _ in range(steps):
+        eng.moments_async(M)
+        eng.autodiff_matrix_async(c, D)
+    return eng.timer_stop() / steps
+
+
+def run_precision(args):
+    """Triangular L=512 spin lattice, M=2000, S=128: FP32 recursion vs native FP64 (and DS)."""
+    import fastkpm_gb300 as fk
+    from fastkpm_gb300 import workloads as W
+    cfg = W.config3(L=args.L if args.L != 64 else 512)
+    H, es = cfg["H"], cfg["es"]
+    R = W.phase_probes(cfg["groups"], 1, cfg["probe_seed"])
+    M = args.M if args.M != 1000 else cfg["M"]
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    N, S = R.shape
+    out = {}
+    for prec in ["fp64", "ds", "fp32"]:
+        eng = fk.Engine(True, prec)
+        eng.set_H(H, es)
+        eng.set_R(R)
+        D = H.pattern_like(True)
+        ms = _solve_timed(eng, M, c, D, 1, 1)
+        mu = eng.fetch_moments(M)
+        eng.fetch_D(D)
+        out[prec] = dict(ms=ms, mu=mu, D=D.val.copy())
+        eng.close()
+    ref = out["fp64"]
+    res = {}
+    for prec in ["ds", "fp32"]:
+        res[prec] = {"moments_max_rel_mu0": _mu_err(out[prec]["mu"], ref["mu"]),
+                     "D_rel_fro": _d_err(out[prec]["D"], ref["D"]),
+                     "ms_per_solve": out[prec]["ms"], "speedup_vs_fp64": ref["ms"] / out[prec]["ms"]}
+    per = float(N) * M * S
+    line = {"metric": METRIC, "value": per / (out["fp32"]["ms"] / 1e3), "unit": UNIT, "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": out["fp32"]["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 recursion, f64 accumulation", "data": "synthetic",
+            "config": {"workload": "triangular L=%d spin-block lattice, J=2, M=%d, S=%d colour probes: "
+                                   "moments + autodiff_matrix" % (cfg["H"].n_rows ** 0.5, M, S),
+                       "N": N, "M": M, "S": S, "nnzb": H.n_blocks()},
+            "fp64_ms_per_solve": ref["ms"], "precision": res}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args):
+    """64 square lattices (L ~ U{32..256}, W ~ U[0,4]), M=500, S=32: one FP32 launch per step for all
+    systems, recursion replayed from a CUDA graph, autotuned mapping; vs 64 sequential FP64 solves."""
+    import fastkpm_gb300 as fk
+    from fastkpm_gb300 import _lib as Lb
+    from fastkpm_gb300 import workloads as W
+    systems = W.config4()
+    M = 500
+    Rs = [fk.probe_uncorrelated(s["H"].n_rows, s["S"], fk.RNG(s["probe_seed"])) for s in systems]
+    total_rows = sum(s["H"].n_rows for s in systems)
+    S = systems[0]["S"]
+    bt = fk.Batch(False, "fp32")
+    for s, R in zip(systems, Rs):
+        bt.add(s["H"], s["es"], R)
+    bt.commit()
+    tune = bt.autotune(8)
+    bt.set_option(Lb.FK_OPT_GRAPHS, 1)
+    for _ in range(max(args.warmup, 1)):
+        mu_b = bt.moments(M)
+    with ClockSampler(0) as clk:
+        bt.timer_start()
+        for _ in range(args.steps):
+            mu_b = bt.moments(M)
+        ms_b = bt.timer_stop() / args.steps
+    # sequential plain FP64 solves (moments only, the batched output)
+    eng = fk.Engine(False, "fp64")
+    t_seq = 0.0
+    err = 0.0
+    for k, (s, R) in enumerate(zip(systems, Rs)):
+        eng.set_H(s["H"], s["es"])
+        eng.set_R(R)
+        eng.moments(M)
+        eng.timer_start()
+        mu = eng.moments(M)
+        t_seq += eng.timer_stop()
+        err = max(err, _mu_err(mu_b[k], mu))
+    eng.close()
+    per = float(total_rows) * M * S
+    bytes_step = 3 * total_rows * S * 4 + sum(s["H"].n_blocks() * 8 + 4 * (s["H"].n_rows + 1) for s in systems)
+    achieved = bytes_step / (ms_b / (M // 2) * 1e-3) / 1e9
+    peak, kind = peaks()
+    line = {"metric": METRIC, "value": per / (ms_b / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 recursion, f64 accumulation", "data": "synthetic",
+            "config": {"workload": "64 square lattices L~U{32..256}, W~U[0,4], b=1 real, M=500, S=32: "
+                                   "batched moments, CUDA graph, autotuned", "total_rows": total_rows, "M": M, "S": S,
+                       "systems": len(systems)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "kernel": "k_cheb_step (batched)", "peak_source": kind},
+            "sequential_fp64_ms": t_seq, "speedup_vs_sequential_fp64": t_seq / ms_b,
+            "moments_max_rel_mu0_vs_fp64": err, "autotune": tune, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def serve_requests(n_req, seed, max_sites):
+    """Mixed-size KPM solve requests: cubic or square lattice (50/50), sites log-uniform over
+    10^3 .. max_sites, b=1 real or b=2 complex spin-exchange (50/50), M in {200,500,1000,2000},
+    S in {32,64,128} by colour probing; Poisson arrival offsets (rate 4/s)."""
+    from fastkpm_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    reqs = []
+    t = 0.0
+    for k in range(n_req):
+        t += rng.exponential(0.25)
+        cubic = rng.random() < 0.5
+        spin = rng.random() < 0.5
+        sites = 10 ** rng.uniform(3, np.log10(max_sites))
+        M = int(rng.choice([200, 500, 1000, 2000]))
+        S = int(rng.choice([32, 64, 128]))
+        if cubic:
+            L = max(8, int(round(sites ** (1 / 3) / 8)) * 8)
+            if spin:
+                H, es, _ = W.cubic_spin_lattice(L, -1.0, 1.0, seed + k)
+                p = {32: (2, 2, 4), 64: (4, 4, 2), 128: (4, 4, 4)}[S]
+                idx = np.arange(L ** 3)
+                col = idx % L % p[0] + p[0] * ((idx // L % L) % p[1] + p[1] * ((idx // (L * L)) % p[2]))
+                groups = np.stack([2 * col, 2 * col + 1], 1).reshape(-1)
+            else:
+                H, es = _cubic_real(L, seed + k)
+                p = {32: (4, 4, 2), 64: (4, 4, 4), 128: (8, 4, 4)}[S]
+                idx = np.arange(L ** 3)
+                groups = idx % L % p[0] + p[0] * ((idx // L % L) % p[1] + p[1] * ((idx // (L * L)) % p[2]))
+        else:
+            L = max(8, int(round(sites ** 0.5 / 8)) * 8)
+            if spin:
+                H, es, _ = W.triangular_spin_lattice(L, -1.0, 1.0, seed + k)
+                px, py = {32: (4, 4), 64: (8, 4), 128: (8, 8)}[S]
+                groups = W.square_colour_groups(L, px, py, spin=True)
+            else:
+                H, es = W.square_lattice(L, -1.0, 1.0, seed + k)
+                px, py = {32: (8, 4), 64: (8, 8), 128: (16, 8)}[S]
+                groups = W.square_colour_groups(L, px, py)
+        R = W.phase_probes(groups, 1, seed + k, complex_values=spin)
+        c = W.fermi_coefficients(M, es, "fermi_energy")
+        reqs.append(dict(H=H, es=es, R=R, M=M, c=c, t=t, spin=spin))
+    return reqs
+
+
+def _cubic_real(L, seed):
+    from fastkpm_gb300 import workloads as W
+    from fastkpm_gb300.engine import EnergyScale
+    rng = np.random.default_rng(seed)
+    n = L ** 3
+    idx = np.arange(n)
+    x, y, z = idx % L, (idx // L) % L, idx // (L * L)
+    site = lambda a, b_, c_: (a % L) + L * ((b_ % L) + L * (c_ % L))
+    nbrs = [site(x + 1, y, z), site(x - 1, y, z), site(x, y + 1, z), site(x, y - 1, z), site(x, y, z + 1),
+            site(x, y, z - 1)]
+    rows = np.concatenate([idx] * 7)
+    cols = np.concatenate(nbrs + [idx])
+    vals = np.concatenate([np.full(n, -1.0)] * 6 + [rng.uniform(-0.5, 0.5, n)])
+    H = W._bsr_from_coo(n, 1, rows, cols, vals[:, None], False)
+    return H, EnergyScale(-6.3, 6.3)
+
+
+def run_serve(args):
+    """Continuous-batching server (FP32 recursion) on a Poisson stream of mixed-size requests;
+    p50/p99 latency and aggregate probe-steps/s vs the same requests solved one by one with the
+    plain FP64 engine; each request's result checked against its FP64 solve."""
+    import fastkpm_gb300 as fk
+    from fastkpm_gb300.serve import Request, Server
+    reqs = serve_requests(args.serve_requests, 5, args.serve_max_sites)
+    srv = Server(max_slots=8, memory_budget=int(120e9))
+    t0 = time.perf_counter()
+    tickets = []
+    for r in reqs:
+        now = time.perf_counter() - t0
+        if r["t"] > now:
+            time.sleep(r["t"] - now)
+        tickets.append(srv.submit(Request(r["H"], r["es"], r["R"], r["M"], r["c"], "autodiff", "fp32")))
+    srv.drain()
+    st = srv.stats()
+    srv.stop()
+    # serial plain FP64 engine on the same requests (in arrival order, for at most ~90 s of solves;
+    # its rate is taken over the requests it finished)
+    t_ser = 0.0
+    worst = 0.0
+    work_ser = 0.0
+    n_ser = 0
+    for r, tk in zip(reqs, tickets):
+        if t_ser > 90.0:
+            break
+        eng = fk.Engine(r["spin"], "fp64")
+        eng.set_H(r["H"], r["es"])
+        eng.set_R(r["R"])
+        t = time.perf_counter()
+        mu = eng.moments(r["M"])
+        D = r["H"].pattern_like(r["spin"])
+        eng.autodiff_matrix(r["c"], D)
+        t_ser += time.perf_counter() - t
+        eng.close()
+        work_ser += float(r["R"].shape[0]) * r["M"] * r["R"].shape[1]
+        n_ser += 1
+        if tk.error is None:
+            worst = max(worst, _mu_err(tk.mu, mu))
+    work = work_ser
+    line = {"metric": METRIC, "value": st["probe_steps_per_s"], "unit": UNIT, "n_gpus": 1, "steps": len(reqs),
+            "warmup": 0, "ms_per_step": st["wall_s"] * 1e3 / max(len(reqs), 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 recursion, f64 accumulation", "data": "synthetic",
+            "config": {"workload": "Poisson stream of %d mixed KPM solves (moments + autodiff D), sites 1e3..%g"
+                                   % (len(reqs), args.serve_max_sites), "slots": 8},
+            "latency_p50_s": st["p50_s"], "latency_p99_s": st["p99_s"], "completed": st["completed"],
+            "rejected": st["rejected"], "max_concurrent": st["max_concurrent"],
+            "serial_fp64_probe_steps_per_s": work / t_ser, "speedup_vs_serial_fp64": (work / t_ser and
+                                                                                  st["probe_steps_per_s"] / (work / t_ser)),
+            "moments_max_rel_mu0_vs_fp64": worst, "serial_fp64_requests": n_ser}
+    print(json.dumps(line), flush=True)
+
+
+def run_cfg1(args):
+    """32x32 square lattice, M=200, S=64, FP64: moments + stoch_matrix; oracle timed beside it."""
+    import fastkpm_gb300 as fk
+    from fastkpm_gb300 import workloads as W
+    from oracle import oracle as O
+    cfg = W.config1()
+    H, es, M, S = cfg["H"], cfg["es"], cfg["M"], cfg["S"]
+    R = fk.probe_uncorrelated(H.n_rows, S, fk.RNG(cfg["probe_seed"]))
+    c = W.fermi_coefficients(M, es)
+    D = H.pattern_like()
+    eng = fk.Engine(False, "fp64")
+    eng.set_H(H, es)
+    eng.set_R(R)
+    for _ in range(3):
+        eng.moments(M)
+        eng.stoch_matrix(c, D)
+    eng.timer_start()
+    for _ in range(args.steps):
+        eng.moments_async(M)
+        eng.stoch_matrix_async(c, D)
+    ms = eng.timer_stop() / args.steps
+    mu = eng.fetch_moments(M)
+    eng.fetch_D(D)
+    orc = O.OracleEngine(False)
+    orc.set_H(H, es)
+    orc.set_R(R)
+    t = time.perf_counter()
+    mu_r = orc.moments(M)
+    D_r = orc.stoch_matrix(c, D)
+    t_cpu = time.perf_counter() - t
+    per = float(H.n_rows) * M * S
+    line = {"metric": METRIC, "value": per / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": 3, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "square L=32, M=200, S=64: moments + stoch_matrix (L2-resident)"},
+            "moments_max_rel_mu0_vs_oracle": _mu_err(mu, mu_r), "D_rel_fro_vs_oracle": _d_err(D.val, D_r),
+            "cpu_baseline": {"value": per / t_cpu, "unit": UNIT, "cores": orc.threads, "kind": "port",
+                             "sample": "the same solve on the oracle port"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init()
     if args.impl == "reference":
         run_reference(args, rank, ws, dist)
+        return
+    if args.workload != "solve":
+        if rank == 0:
+            {"precision": run_precision, "batch": run_batch, "serve": run_serve, "cfg1": run_cfg1}[args.workload](args)
         return
     r = run_gb300(args, rank, ws, dist)
     cpu = None

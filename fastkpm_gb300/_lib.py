@@ -15,6 +15,7 @@ FK_REAL, FK_COMPLEX = 0, 1
 FK_PREC_FP64, FK_PREC_FP32, FK_PREC_DS = 0, 1, 2
 FK_KERNEL_STEP, FK_KERNEL_ADJOINT, FK_KERNEL_OUTER, FK_KERNEL_HELPER = 0, 1, 2, 3
 FK_OPT_FUSE_D, FK_OPT_NP, FK_OPT_CTAS_PER_SM, FK_OPT_STAGE_H, FK_OPT_GRAPHS = 0, 1, 2, 3, 4
+FK_OPT_NP_STEP, FK_OPT_NP_ADJOINT, FK_OPT_NP_OUTER = 5, 6, 7
 
 PRECISIONS = {"fp64": FK_PREC_FP64, "fp32": FK_PREC_FP32, "ds": FK_PREC_DS}
 
@@ -29,6 +30,7 @@ SIGNATURES = {
     "fk_version": (C.c_char_p, []),
     "fk_status_string": (C.c_char_p, [_i]),
     "fk_device_count": (_i, [_ip]),
+    "fk_device_memory": (_i, [_i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "fk_engine_create": (_i, [_i, _i, _i, C.POINTER(_p)]),
     "fk_engine_destroy": (_i, [_p]),
     "fk_engine_last_error": (C.c_char_p, [_p]),

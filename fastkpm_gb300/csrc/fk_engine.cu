@@ -69,7 +69,8 @@ struct fk_engine {
     std::string err;
 
     // options
-    int opt_fuse_d = 1, opt_np = 0, opt_ctas_per_sm = 0, opt_stage = 1, opt_graphs = 0;
+    int opt_fuse_d = 2, opt_np = 0, opt_ctas_per_sm = 0, opt_stage = 1, opt_graphs = 0;
+    int opt_np_kind[3] = {0, 0, 0};   // per kernel kind (step, adjoint, outer); 0 = opt_np / default
 
     // H (scaled, augmented with diagonal blocks)
     int n_b = 0, b = 0, nnzb = 0;
@@ -226,25 +227,31 @@ int configure(fk_engine* e) {
     const int P = e->P;
     // Gp lanes per block row, NP packets per lane and column chunk; the kernels walk
     // the row's ceil(P / (Gp * NP)) chunks themselves, so one launch covers all columns.
+    // Each kernel kind has its own NP (register use vs. loads in flight): defaults measured
+    // on the cubic L=64, S=256 workload are 4 for the step and outer kernels and 2 for the
+    // adjoint kernel, whose fused epilogue holds the most live values.
     const int slices = 1, W = P;
-    int NP, Gp;
-    if (e->opt_np > 0) {
-        NP = e->opt_np;
-        Gp = std::min(32, next_pow2((P + NP - 1) / NP));
-    } else if (P <= 32) {
-        NP = 1;
-        Gp = next_pow2(P);
-    } else {
-        NP = 4;   // measured best (or tied) for the step and adjoint kernels at S >= 128
-        Gp = 32;
-    }
-    // H blocks per tile of kThreads items: the shared-memory stage size
-    const long long items = (long long)e->n_b * Gp;
-    const long long tiles = (items + fk::kThreads - 1) / fk::kThreads;
-    const int nk_max = fk::max_tile_blocks(e->h_row_ptr.data(), e->n_b, Gp);
+    // {step, adjoint, outer}; the FP64 adjoint (FP64-pipe bound) prefers the lightest threads
+    const int kDefaultNP[fk::kHelper] = {4, e->prec == fk::kF64 ? 1 : 2, 4};
     const size_t per_blk = (size_t)e->b * e->b * e->hsize() + sizeof(unsigned);
-    int stage_cap = (e->opt_stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
     for (int kind = 0; kind < fk::kHelper; kind++) {
+        int NP, Gp;
+        const int want = e->opt_np_kind[kind] > 0 ? e->opt_np_kind[kind] : e->opt_np;
+        if (want > 0) {
+            NP = want;
+            Gp = std::min(32, next_pow2((P + NP - 1) / NP));
+        } else if (P <= 32) {
+            NP = 1;
+            Gp = next_pow2(P);
+        } else {
+            NP = kDefaultNP[kind];
+            Gp = 32;
+        }
+        // H blocks per tile of kThreads items: the shared-memory stage size
+        const long long items = (long long)e->n_b * Gp;
+        const long long tiles = (items + fk::kThreads - 1) / fk::kThreads;
+        const int nk_max = fk::max_tile_blocks(e->h_row_ptr.data(), e->n_b, Gp);
+        const int stage_cap = (e->opt_stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
         KCfg& c = e->cfg[kind];
         c.Gp = Gp; c.NP = NP; c.slices = slices; c.W = W;
         c.stage_cap = kind == fk::kOuter ? 0 : stage_cap;
@@ -422,6 +429,16 @@ int set_D_pattern(fk_engine* e, int d_n_b, int d_nnzb, const int* rp, const int*
     return FK_OK;
 }
 
+// FP32 and DS engines accumulate D as float-float pairs; turn them into doubles in place.
+int finish_D_accumulator(fk_engine* e, size_t n_reals) {
+    if (e->prec == fk::kF64 || n_reals == 0) return FK_OK;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(((long long)n_reals + 255) / 256, 152LL * 16));
+    ProfScope ps(e, fk::kHelper);
+    fk::k_ds_to_double<<<grid, 256, 0, e->stream>>>(e->dd_acc.as<double>(), (long long)n_reals);
+    FK_TRY(cudaGetLastError(), "accumulator conversion");
+    return FK_OK;
+}
+
 int ensure_coef(fk_engine* e, size_t ndoubles) {
     FK_TRY(e->d_coef.ensure(sizeof(double) * std::max<size_t>(ndoubles, 1)), "alloc coefficients");
     return FK_OK;
@@ -535,6 +552,8 @@ int stoch_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, c
     if (d_nnzb > 0) {
         rc = run_outer(e, e->d_R.p, xi, 0.5, true);
         if (rc != FK_OK) return rc;
+        rc = finish_D_accumulator(e, dn);
+        if (rc != FK_OK) return rc;
     }
     e->mom_M = 0;   // the recursion state is no longer the one autodiff needs (reference clears a0, a1)
     e->mom_a0 = e->mom_a1 = -2;
@@ -564,7 +583,11 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
     }
     FK_TRY(cudaMemcpyAsync(e->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, e->stream),
            "upload coefficients");
-    const bool fuse = e->opt_fuse_d && e->d_same_as_H;
+    // FK_OPT_FUSE_D: 1 always fuse (when D's pattern is H's), 0 never, 2 (default) by precision:
+    // fusing saves two gathered vector reads per step, which pays when the step is memory-bound
+    // (FP32); the FP64-class systems are arithmetic-bound and run the two kernels faster apart.
+    const bool fuse_pref = e->opt_fuse_d == 2 ? e->prec == fk::kF32 : e->opt_fuse_d != 0;
+    const bool fuse = fuse_pref && e->d_same_as_H;
     // buffers: alpha_m in A, alpha_{m+1} in Ap (moments left alpha_{M/2-1}, alpha_{M/2})
     int A = e->mom_a0, Ap = e->mom_a1;
     int freeb[4], nf = 0;
@@ -592,6 +615,8 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
     // D += alpha_0 (beta_1 + diag alpha_0)^dag, then symmetrize and divide by mag
     if (d_nnzb > 0) {
         rc = run_outer(e, e->V(A), e->V(Bv), 1.0, false);
+        if (rc != FK_OK) return rc;
+        rc = finish_D_accumulator(e, dn);
         if (rc != FK_OK) return rc;
         const double mag = (e->es_hi - e->es_lo) / 2.0;
         const long long work = (long long)d_nnzb * e->b * e->b;
@@ -708,6 +733,20 @@ int fk_device_count(int* count) {
     return FK_OK;
 }
 
+int fk_device_memory(int device, size_t* free_bytes, size_t* total_bytes) {
+    if (!free_bytes || !total_bytes) return FK_ERR_ARG;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) { cudaGetLastError(); return FK_ERR_NODEV; }
+    if (device < 0 || device >= count) return FK_ERR_ARG;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    cudaError_t ce = cudaMemGetInfo(free_bytes, total_bytes);
+    cudaSetDevice(prev);
+    if (ce != cudaSuccess) { cudaGetLastError(); return FK_ERR_CUDA; }
+    return FK_OK;
+}
+
 int fk_engine_create(int device, int kind, int precision, fk_engine** out) {
     if (!out) return FK_ERR_ARG;
     *out = nullptr;
@@ -774,10 +813,21 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
     if (!e) return FK_ERR_ARG;
     cudaSetDevice(e->device);
     switch (option) {
-        case FK_OPT_FUSE_D: e->opt_fuse_d = value ? 1 : 0; return FK_OK;
+        case FK_OPT_FUSE_D:
+            if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "FUSE_D must be 0, 1 or 2");
+            e->opt_fuse_d = value;
+            return FK_OK;
         case FK_OPT_NP:
             if (value != 0 && value != 1 && value != 2 && value != 4) return e->fail(FK_ERR_ARG, "NP must be 0, 1, 2 or 4");
-            e->opt_np = value; return configure(e);
+            e->opt_np = value;
+            for (int& v : e->opt_np_kind) v = 0;
+            return configure(e);
+        case FK_OPT_NP_STEP:
+        case FK_OPT_NP_ADJOINT:
+        case FK_OPT_NP_OUTER:
+            if (value != 0 && value != 1 && value != 2 && value != 4) return e->fail(FK_ERR_ARG, "NP must be 0, 1, 2 or 4");
+            e->opt_np_kind[option - FK_OPT_NP_STEP] = value;
+            return configure(e);
         case FK_OPT_CTAS_PER_SM:
             if (value < 0) return e->fail(FK_ERR_ARG, "negative CTA cap");
             e->opt_ctas_per_sm = value; return configure(e);
@@ -792,6 +842,13 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
     switch (option) {
         case FK_OPT_FUSE_D: *value = e->opt_fuse_d; return FK_OK;
         case FK_OPT_NP: *value = e->cfg[0].valid ? e->cfg[0].NP : e->opt_np; return FK_OK;
+        case FK_OPT_NP_STEP:
+        case FK_OPT_NP_ADJOINT:
+        case FK_OPT_NP_OUTER: {
+            const int k = option - FK_OPT_NP_STEP;
+            *value = e->cfg[k].valid ? e->cfg[k].NP : e->opt_np_kind[k];
+            return FK_OK;
+        }
         case FK_OPT_CTAS_PER_SM: *value = e->opt_ctas_per_sm; return FK_OK;
         case FK_OPT_STAGE_H: *value = e->opt_stage; return FK_OK;
         case FK_OPT_GRAPHS: *value = e->opt_graphs; return FK_OK;

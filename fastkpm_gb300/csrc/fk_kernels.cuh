@@ -370,9 +370,12 @@ __device__ __forceinline__ void group_sum_transposed(typename S::OAcc (&v)[V], i
 }
 
 // Reduce a block's per-lane D partials over the row group and add them to Dacc[k].
+// FP64 systems accumulate in double; FP32 and DS systems keep the accumulator as
+// float-float pairs (same 8 bytes per real) on the FP32 pipe and convert it to
+// double once at the end (k_ds_to_double).
 template <class S, int B>
 __device__ __forceinline__ void flush_block(typename S::OAcc (&of)[B * B], int Gp, int g, bool has, size_t k,
-                                            double scale, double* Dacc) {
+                                            double scale, float2 scale_ds, double* Dacc) {
     int first, count;
     bool writer;
     group_sum_transposed<S, B * B>(of, Gp, g, first, count, writer);
@@ -380,12 +383,30 @@ __device__ __forceinline__ void flush_block(typename S::OAcc (&of)[B * B], int G
 #pragma unroll
         for (int t = 0; t < B * B; t++) {
             if (t < count) {
-                const double2 v = S::oa_get(of[t]);
                 const size_t q = (k * B * B + first + t) * (S::CPLX ? 2 : 1);
-                Dacc[q] += scale * v.x;
-                if (S::CPLX) Dacc[q + 1] += scale * v.y;
+                if constexpr (S::DACC_DS) {
+                    float2* D2 = reinterpret_cast<float2*>(Dacc);
+#pragma unroll
+                    for (int comp = 0; comp < (S::CPLX ? 2 : 1); comp++) {
+                        float2 cur = D2[q + comp];
+                        ds_mac(cur, scale_ds, S::oa_ds(of[t], comp));
+                        D2[q + comp] = ds_norm(cur);
+                    }
+                } else {
+                    const double2 v = S::oa_get(of[t]);
+                    Dacc[q] += scale * v.x;
+                    if (S::CPLX) Dacc[q + 1] += scale * v.y;
+                }
             }
         }
+    }
+}
+
+// Float-float accumulator -> double, in place (both are 8 bytes per real).
+static __global__ void k_ds_to_double(double* D, long long n_reals) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_reals; q += (long long)gridDim.x * blockDim.x) {
+        const float2 v = reinterpret_cast<const float2*>(D)[q];
+        D[q] = (double)v.x + (double)v.y;
     }
 }
 
@@ -421,6 +442,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_step(AdjArgs a) {
     const typename S::Coef cAp = S::coef(a.coef[sidx * a.cstride + 1]);
     const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
     const bool fuse = a.Dacc != nullptr;
+    const float2 dscale_ds = ds_from_double(a.dscale);
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
         const Tile tl = tile_range(a.row_ptr, sd, t0, items, Gp, a.stage_cap);
@@ -494,7 +516,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_step(AdjArgs a) {
                             for (int e = 0; e < EPT; e++) S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
                     }
                 }
-                if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, a.Dacc);
+                if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, dscale_ds, a.Dacc);
             }
             if (active) {
 #pragma unroll
@@ -542,6 +564,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
     const E* A = reinterpret_cast<const E*>(a.A);
     const E* Bv = reinterpret_cast<const E*>(a.Bv);
     const bool two_terms = a.two_terms != 0;
+    const float2 alpha_ds = ds_from_double(a.alpha);
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
         const long long t = t0 + threadIdx.x;
@@ -600,7 +623,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
                             if (two_terms) S::oa_mac(of[bj * B + bi], Bi[bi][e], av[e]);
                         }
                 }
-                flush_block<S, B>(of, Gp, g, has, (size_t)k, a.alpha, a.Dacc);
+                flush_block<S, B>(of, Gp, g, has, (size_t)k, a.alpha, alpha_ds, a.Dacc);
             }
         }
     }

@@ -1,0 +1,266 @@
+// fk_staged.cuh -- Chebyshev step with the neighbour gathers staged by TMA bulk copies.
+//
+// The plain step kernel gathers x rows with per-thread loads and stalls on their
+// latency (long-scoreboard is its top stall; registers cap it at 16 warps/SM).
+// Here a tile of kThreads (row, lane) items is served from shared memory:
+//   * the host lists, per tile, the distinct block columns its rows touch (own
+//     rows included), sorted, and for every H block its slot in that list;
+//   * per column chunk of W = Gp * NP packets, warp 0 issues one 1-D
+//     cp.async.bulk copy per (distinct column, bj) row chunk into one of two
+//     shared buffers, completing on that buffer's mbarrier (expect_tx bytes);
+//   * while a chunk is computed from shared memory, the next chunk (of this or
+//     the CTA's next tile) is already in flight.
+// Every wait is bounded: after kWaitLimit polls the CTA records the failure in
+// *err and stops (the host turns that into FK_ERR_TIMEOUT).
+// All copies start on 16-byte boundaries and move multiples of 16 bytes.
+#pragma once
+#include "fk_kernels.cuh"
+
+namespace fk {
+
+struct StageTables {
+    const int* tile_base;           // per system: global index of its first tile
+    const int* uoff;                // [tiles + 1]: offsets into ucol
+    const int* ucol;                // distinct global block columns of each tile, sorted
+    const int* own;                 // [tiles]: slot of the tile's first own row
+    const unsigned short* kslot;    // per H block: slot of its column in its tile's list
+    int umax;                       // largest list
+    int* err;                       // set to 1 by a CTA whose wait ran out
+};
+
+constexpr unsigned kWaitLimit = 1u << 26;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: true when the phase with this parity completed
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+    for (unsigned it = 0; it < kWaitLimit; it++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Shared-memory bytes the staged step kernel needs.
+__host__ __device__ inline size_t staged_smem_bytes(int umax, int B, int W, int stage_cap, int hsize) {
+    const size_t buf = (size_t)umax * B * W * 16;
+    return 128 + 2 * buf + (size_t)stage_cap * ((size_t)B * B * hsize + 4 + 2) + 16;
+}
+
+template <class S, int B, int NP>
+__global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, StageTables tb) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    constexpr int EPP = S::EPP;
+    constexpr int EPT = NP * EPP;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int nch = (P + W - 1) / W;
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem);
+    __shared__ int s_fail;
+    uint4* buf0 = reinterpret_cast<uint4*>(smem + 128);
+    const size_t buf_packets = (size_t)tb.umax * B * W;
+    H* s_h = reinterpret_cast<H*>(smem + 128 + 2 * buf_packets * 16);
+    unsigned* s_col = reinterpret_cast<unsigned*>(s_h + (size_t)a.stage_cap * B * B);
+    unsigned short* s_slot = reinterpret_cast<unsigned short*>(s_col + a.stage_cap);
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const long long items = (long long)sd.n_b * Gp;
+    const int tiles = (int)((items + kThreads - 1) / kThreads);
+    const int my_tiles = lc < tiles ? (tiles - 1 - lc) / sd.ctas + 1 : 0;
+    const int n_units = my_tiles * nch;
+    const int tbase = tb.tile_base[sidx];
+    const E* x = reinterpret_cast<const E*>(a.x);
+    const E* z = reinterpret_cast<const E*>(a.z);
+    E* y = reinterpret_cast<E*>(a.y);
+    E* xi = reinterpret_cast<E*>(a.xi);
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef c0 = S::coef(a.xi_mode ? a.coef[sidx * a.cstride + 0] : 0.0);
+    const typename S::Coef c1 = S::coef(a.xi_mode ? a.coef[sidx * a.cstride + 1] : 0.0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_fence_init();
+        s_fail = 0;
+    }
+    __syncthreads();
+
+    // warp 0: put the row chunks of `unit` in flight into buffer unit & 1
+    auto issue = [&](int unit) {
+        const int lt = lc + (unit / nch) * sd.ctas;
+        const int c = unit % nch;
+        const int gt = tbase + lt;
+        const int u0 = tb.uoff[gt];
+        const int nu = tb.uoff[gt + 1] - u0;
+        const int pk = min(W, P - c * W);
+        const unsigned row_bytes = (unsigned)pk * 16u;
+        uint4* dstb = buf0 + (size_t)(unit & 1) * buf_packets;
+        // the generic-proxy reads of this buffer (two units ago, ordered by the CTA barrier)
+        // must precede this lane's async-proxy writes into it
+        fence_proxy_async_smem();
+        if (lane == 0) mbar_expect_tx(&mbar[unit & 1], row_bytes * (unsigned)(nu * B));
+        __syncwarp();
+        for (int q = lane; q < nu * B; q += 32) {
+            const int ui = q / B, bj = q - (q / B) * B;
+            const int col = tb.ucol[u0 + ui];
+            const E* src = x + (size_t)(B * col + bj) * a.ld + (size_t)c * W * EPP;
+            bulk_g2s(dstb + (size_t)(ui * B + bj) * W, src, row_bytes, &mbar[unit & 1]);
+        }
+    };
+
+    typename S::Dot dxx = S::dot_zero(), dyx = S::dot_zero();
+    if (warp == 0 && n_units > 0) issue(0);
+    int k_lo = 0;
+    for (int unit = 0; unit < n_units; unit++) {
+        const int lt = lc + (unit / nch) * sd.ctas;
+        const int c = unit % nch;
+        const long long t0 = (long long)lt * kThreads;
+        const int r_lo = sd.row_base + (int)(t0 / Gp);
+        if (warp == 0 && unit + 1 < n_units) issue(unit + 1);
+        if (c == 0) {
+            // H blocks, their columns and their slots for this tile
+            const long long t_last = min(t0 + kThreads, items) - 1;
+            const int r_hi = sd.row_base + (int)(t_last / Gp);
+            k_lo = a.row_ptr[r_lo];
+            const int nk = a.row_ptr[r_hi + 1] - k_lo;
+            for (int q = threadIdx.x; q < nk; q += blockDim.x) {
+                s_col[q] = __ldg(a.colc + k_lo + q);
+                s_slot[q] = __ldg(tb.kslot + k_lo + q);
+            }
+            for (int q = threadIdx.x; q < nk * B * B; q += blockDim.x) s_h[q] = hval[(size_t)k_lo * B * B + q];
+        }
+        // wait for this unit's row chunks: thread 0 with a bound, then everyone acquires
+        if (threadIdx.x == 0 && !mbar_wait_bounded(&mbar[unit & 1], (unsigned)(unit >> 1) & 1u)) s_fail = 1;
+        __syncthreads();
+        if (s_fail) {
+            if (threadIdx.x == 0) {
+                atomicExch(tb.err, 1);
+                // the next unit's copies may be in flight: wait for them (bounded) before leaving
+                if (unit + 1 < n_units) mbar_wait_bounded(&mbar[(unit + 1) & 1], (unsigned)((unit + 1) >> 1) & 1u);
+            }
+            return;
+        }
+        mbar_wait_bounded(&mbar[unit & 1], (unsigned)(unit >> 1) & 1u);   // completed: returns at once
+        const uint4* sb = buf0 + (size_t)(unit & 1) * buf_packets;
+        const long long t = t0 + threadIdx.x;
+        if (t < items) {
+            const int il = (int)(t / Gp);
+            const int g = (int)(t - (long long)il * Gp);
+            const int i = sd.row_base + il;
+            const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];
+            const int base = c * W;
+            typename S::Acc acc[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) acc[bi][e] = S::zero();
+            for (int k = kb; k < ke; k++) {
+                const int kk = k - k_lo;
+                const unsigned cc = s_col[kk];
+                const int slot = s_slot[kk];
+                const H* hk = s_h + (size_t)kk * B * B;
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    E xv[EPT];
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        Packet<E, EPP> pkt;
+                        const int pk = g + Gp * q;
+                        pkt.u = make_uint4(0u, 0u, 0u, 0u);
+                        if (base + pk < P) pkt.u = sb[(size_t)(slot * B + bj) * W + pk];
+#pragma unroll
+                        for (int e = 0; e < EPP; e++) xv[q * EPP + e] = pkt.e[e];
+                    }
+                    mac_block<S, B, NP>(acc, cc >> 30, hk, xv, bj);
+                }
+            }
+            const int own_slot = tb.own[tbase + lt] + (i - r_lo);
+            typename S::RowDot rxx = S::rd_zero(), ryx = S::rd_zero();
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                const size_t roff = (size_t)(B * i + bi) * a.ld;
+                E zv[EPT], yv[EPT], xo[EPT];
+                if (a.has_z) ld_rw<S, NP>(zv, z + roff, base, g, Gp, P);
+                else {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) zv[e] = S::to(S::zero());
+                }
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    Packet<E, EPP> pkt;
+                    const int pk = g + Gp * q;
+                    pkt.u = make_uint4(0u, 0u, 0u, 0u);
+                    if (base + pk < P) pkt.u = sb[(size_t)(own_slot * B + bi) * W + pk];
+#pragma unroll
+                    for (int e = 0; e < EPP; e++) xo[q * EPP + e] = pkt.e[e];
+                }
+#pragma unroll
+                for (int e = 0; e < EPT; e++) yv[e] = S::fin(acc[bi][e], a.two != 0, a.has_z != 0, zv[e]);
+                st<S, NP>(y + roff, yv, base, g, Gp, P);
+                if (a.want_dots) {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) { S::rd_nrm(rxx, xo[e]); S::rd_re(ryx, yv[e], xo[e]); }
+                }
+                if (a.xi_mode == 1) {
+                    E xv2[EPT];
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        typename S::Acc t2 = S::zero();
+                        S::axpy(t2, c0, xo[e]);
+                        S::axpy(t2, c1, yv[e]);
+                        xv2[e] = S::to(t2);
+                    }
+                    st<S, NP>(xi + roff, xv2, base, g, Gp, P);
+                } else if (a.xi_mode == 2) {
+                    E xv2[EPT];
+                    ld_rw<S, NP>(xv2, xi + roff, base, g, Gp, P);
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        typename S::Acc t2 = S::from(xv2[e]);
+                        S::axpy(t2, c1, yv[e]);
+                        xv2[e] = S::to(t2);
+                    }
+                    st<S, NP>(xi + roff, xv2, base, g, Gp, P);
+                }
+            }
+            if (a.want_dots) { S::dot_add(dxx, rxx); S::dot_add(dyx, ryx); }
+        }
+        __syncthreads();   // buffer unit & 1 and the H stage are free again
+    }
+    if (a.want_dots) {
+        block_reduce2<S>(dxx, dyx);
+        if (threadIdx.x == 0) {
+            a.partials[2 * blockIdx.x + 0] = S::dot_get(dxx);
+            a.partials[2 * blockIdx.x + 1] = S::dot_get(dyx);
+        }
+    }
+}
+
+}  // namespace fk

@@ -94,6 +94,8 @@ struct SysF64R {
     __device__ static OAcc oa_zero() { return 0.0; }
     __device__ static void oa_mac(OAcc& o, E a, E b) { o = fma(a, b, o); }          // o += a conj(b)
     __device__ static OAcc oa_shfl_add(OAcc o, int off) { return o + __shfl_xor_sync(0xffffffffu, o, off); }
+    static constexpr bool DACC_DS = false;   // D accumulated in FP64
+    __device__ static float2 oa_ds(OAcc, int) { return make_float2(0.f, 0.f); }
     __device__ static double2 oa_get(OAcc o) { return make_double2(o, 0.0); }
     __device__ static OAcc oa_add(OAcc a, OAcc b) { return a + b; }
     __device__ static OAcc oa_shfl(OAcc o, int off) { return __shfl_xor_sync(0xffffffffu, o, off); }
@@ -137,6 +139,8 @@ struct SysF64C {
         return make_double2(o.x + __shfl_xor_sync(0xffffffffu, o.x, off),
                             o.y + __shfl_xor_sync(0xffffffffu, o.y, off));
     }
+    static constexpr bool DACC_DS = false;
+    __device__ static float2 oa_ds(OAcc, int) { return make_float2(0.f, 0.f); }
     __device__ static double2 oa_get(OAcc o) { return o; }
     __device__ static OAcc oa_add(OAcc a, OAcc b) { return make_double2(a.x + b.x, a.y + b.y); }
     __device__ static OAcc oa_shfl(OAcc o, int off) {
@@ -177,6 +181,9 @@ struct SysF32R {
     __device__ static OAcc oa_zero() { return 0.f; }
     __device__ static void oa_mac(OAcc& o, E a, E b) { o = fmaf(a, b, o); }
     __device__ static OAcc oa_shfl_add(OAcc o, int off) { return o + __shfl_xor_sync(0xffffffffu, o, off); }
+    // D accumulated as float-float on the FP32 pipe (the FP64 pipe is ~1/58 of it)
+    static constexpr bool DACC_DS = true;
+    __device__ static float2 oa_ds(OAcc o, int) { return make_float2(o, 0.f); }
     __device__ static double2 oa_get(OAcc o) { return make_double2((double)o, 0.0); }
     __device__ static OAcc oa_add(OAcc a, OAcc b) { return a + b; }
     __device__ static OAcc oa_shfl(OAcc o, int off) { return __shfl_xor_sync(0xffffffffu, o, off); }
@@ -224,6 +231,8 @@ struct SysF32C {
         return make_float2(o.x + __shfl_xor_sync(0xffffffffu, o.x, off),
                            o.y + __shfl_xor_sync(0xffffffffu, o.y, off));
     }
+    static constexpr bool DACC_DS = true;
+    __device__ static float2 oa_ds(OAcc o, int comp) { return make_float2(comp ? o.y : o.x, 0.f); }
     __device__ static double2 oa_get(OAcc o) { return make_double2((double)o.x, (double)o.y); }
     __device__ static OAcc oa_add(OAcc a, OAcc b) { return make_float2(a.x + b.x, a.y + b.y); }
     __device__ static OAcc oa_shfl(OAcc o, int off) {
@@ -271,6 +280,8 @@ struct SysDSR {
         ds_add(o, t);
         return ds_norm(o);
     }
+    static constexpr bool DACC_DS = true;
+    __device__ static float2 oa_ds(OAcc o, int) { return o; }
     __device__ static double2 oa_get(OAcc o) { return make_double2(ds_to_double(o), 0.0); }
     __device__ static OAcc oa_add(OAcc a, OAcc b) { ds_add(a, b); return a; }
     __device__ static OAcc oa_shfl(OAcc o, int off) {
@@ -336,6 +347,8 @@ struct SysDSC {
     __device__ static OAcc oa_shfl_add(OAcc o, int off) {
         return pack(SysDSR::oa_shfl_add(re(o), off), SysDSR::oa_shfl_add(im(o), off));
     }
+    static constexpr bool DACC_DS = true;
+    __device__ static float2 oa_ds(OAcc o, int comp) { return comp ? im(o) : re(o); }
     __device__ static double2 oa_get(OAcc o) { return make_double2(ds_to_double(re(o)), ds_to_double(im(o))); }
     __device__ static OAcc oa_add(OAcc a, OAcc b) {
         float2 r = re(a), i = im(a);

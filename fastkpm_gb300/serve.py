@@ -121,17 +121,8 @@ class _Slot:
 class Server:
     def __init__(self, device=0, max_slots=8, memory_budget=None, lookahead=64, max_bypass=16):
         self.device = device
-        lib = L.load()
         if memory_budget is None:
-            import ctypes as C
-            free = C.c_size_t(0)
-            total = C.c_size_t(0)
-            memory_budget = 0
-            try:
-                from . import engine as _e   # noqa: F401
-                memory_budget = int(0.8 * self._device_free())
-            except Exception:
-                memory_budget = 64 << 30
+            memory_budget = int(0.8 * self.device_free(device))
         self.budget = int(memory_budget)
         self.lookahead = lookahead
         self.max_bypass = max_bypass
@@ -148,21 +139,13 @@ class Server:
         self._dispatcher.start()
 
     @staticmethod
-    def _device_free():
+    def device_free(device=0):
         import ctypes as C
-        import ctypes.util
-        cudart = None
-        for name in ("libcudart.so", "libcudart.so.13", "libcudart.so.12"):
-            try:
-                cudart = C.CDLL(name)
-                break
-            except OSError:
-                continue
-        if cudart is None:
-            raise OSError("no libcudart")
-        free = C.c_size_t()
-        total = C.c_size_t()
-        cudart.cudaMemGetInfo(C.byref(free), C.byref(total))
+        free = C.c_size_t(0)
+        total = C.c_size_t(0)
+        st = L.load().fk_device_memory(device, C.byref(free), C.byref(total))
+        if st != L.FK_OK:
+            raise L.FkError(st, "device_memory")
         return free.value
 
     # -- client side --

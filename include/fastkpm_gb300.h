@@ -58,6 +58,8 @@ typedef struct fk_engine fk_engine;
 const char* fk_version(void);
 const char* fk_status_string(int status);
 int fk_device_count(int* count);
+/* Free and total device memory of `device` in bytes (admission control of the serving loop). */
+int fk_device_memory(int device, size_t* free_bytes, size_t* total_bytes);
 
 /* mk_engine<T>() / mk_engine_cuSPARSE<T>(devices) (reference src/engine.cpp:124-131,
  * src/engine_cusparse.cpp:1170-1215): one engine bound to one device and one stream. */
@@ -68,11 +70,14 @@ const char* fk_engine_last_error(const fk_engine* e);
 int  fk_engine_set_stream(fk_engine* e, void* cuda_stream);
 int  fk_engine_synchronize(fk_engine* e);
 /* Engine options: FK_OPT_* below. */
-#define FK_OPT_FUSE_D      0   /* 1 (default): fuse the outer product into the adjoint step when D's pattern is H's */
+#define FK_OPT_FUSE_D      0   /* fuse the outer product into the adjoint step when D's pattern is H's: 1 always, 0 never, 2 (default) for FP32 only */
 #define FK_OPT_NP          1   /* packets per lane: 0 auto, or 1, 2, 4                                           */
 #define FK_OPT_CTAS_PER_SM 2   /* 0 auto (occupancy), else a cap on CTAs per SM                                   */
 #define FK_OPT_STAGE_H     3   /* 1 (default): stage H blocks in shared memory                                    */
 #define FK_OPT_GRAPHS      4   /* 1: capture the M-step recursions in CUDA graphs and replay them                 */
+#define FK_OPT_NP_STEP     5   /* packets per lane of the step kernel only (0: FK_OPT_NP / default)               */
+#define FK_OPT_NP_ADJOINT  6   /* ... of the adjoint kernel only                                                  */
+#define FK_OPT_NP_OUTER    7   /* ... of the outer-product kernel only                                            */
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 
