@@ -15,7 +15,7 @@ FK_REAL, FK_COMPLEX = 0, 1
 FK_PREC_FP64, FK_PREC_FP32, FK_PREC_DS = 0, 1, 2
 FK_KERNEL_STEP, FK_KERNEL_ADJOINT, FK_KERNEL_OUTER, FK_KERNEL_HELPER = 0, 1, 2, 3
 FK_OPT_FUSE_D, FK_OPT_NP, FK_OPT_CTAS_PER_SM, FK_OPT_STAGE_H, FK_OPT_GRAPHS = 0, 1, 2, 3, 4
-FK_OPT_NP_STEP, FK_OPT_NP_ADJOINT, FK_OPT_NP_OUTER = 5, 6, 7
+FK_OPT_NP_STEP, FK_OPT_NP_ADJOINT, FK_OPT_NP_OUTER, FK_OPT_TMA = 5, 6, 7, 8
 
 PRECISIONS = {"fp64": FK_PREC_FP64, "fp32": FK_PREC_FP32, "ds": FK_PREC_DS}
 
@@ -50,6 +50,7 @@ SIGNATURES = {
     "fk_engine_autodiff_matrix_async": (_i, [_p, _i, _dp, _i, _i, _ip, _ip]),
     "fk_engine_fetch_D": (_i, [_p, _dp]),
     "fk_engine_energy_scale": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _d, _i, _dp, _dp, _dp]),
+    "fk_engine_expansion_coefficients": (_i, [_p, _i, _i, _i, _d, _d, _d, _d, _dp]),
     "fk_engine_set_profiling": (_i, [_p, _i]),
     "fk_engine_profile_read": (_i, [_p, _i, C.POINTER(C.c_longlong), _dp]),
     "fk_engine_profile_reset": (_i, [_p]),

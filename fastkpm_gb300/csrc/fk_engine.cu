@@ -51,6 +51,8 @@ struct KCfg {
     int ctas = 1;
     DevBuf sys, cta_sys;
     bool valid = false;
+    bool staged = false;   // step kind only: TMA-staged gathers (k_cheb_step_staged)
+    int umax = 0;          // largest per-tile gather list
 };
 
 struct ProfEvent { int kind; cudaEvent_t a, b; };
@@ -71,6 +73,11 @@ struct fk_engine {
     // options
     int opt_fuse_d = 2, opt_np = 0, opt_ctas_per_sm = 0, opt_stage = 1, opt_graphs = 0;
     int opt_np_kind[3] = {0, 0, 0};   // per kernel kind (step, adjoint, outer); 0 = opt_np / default
+    // Stage the step kernel's gathers with TMA bulk copies when they fit. Off by default: on the
+    // cubic L=64 workload the per-copy cost of its 512-byte row chunks made it 2-3x slower than
+    // per-thread gathers, whose DRAM traffic is already at the algorithmic minimum.
+    int opt_tma = 0;
+    DevBuf d_t_uoff, d_t_ucol, d_t_own, d_t_kslot, d_t_base, d_err;   // per-tile gather lists, error flag
 
     // H (scaled, augmented with diagonal blocks)
     int n_b = 0, b = 0, nnzb = 0;
@@ -221,6 +228,62 @@ void prof_flush(fk_engine* e) {
 }
 
 // ---- launch configuration ----
+
+// Staged (TMA bulk-copy) step kernel: build the per-tile gather lists for this Gp and pick
+// the widest column chunk whose double buffer keeps two CTAs on an SM (or one, at most).
+int configure_staged(fk_engine* e, KCfg& c, int Gp, int nk_max, size_t per_blk) {
+    fk::TileTables t;
+    if (!fk::append_tile_tables(e->h_row_ptr.data(), e->h_col.data(), e->n_b, Gp, 0, 0, t)) return FK_OK;
+    const int hs = (int)e->hsize();
+    int NP = 0;
+    size_t smem = 0;
+    for (int np : {2, 1}) {
+        if (np == 2 && Gp >= e->P) continue;   // one chunk already covers the row
+        const size_t s = fk::staged_smem_bytes(t.umax, e->b, Gp * np, nk_max, hs);
+        const size_t tx = (size_t)t.umax * e->b * Gp * np * 16;
+        if (tx < (1u << 20) && s <= (np == 2 ? 110u * 1024 : 200u * 1024)) { NP = np; smem = s; break; }
+    }
+    if (NP == 0) return FK_OK;
+    const size_t tiles = t.own.size();
+    FK_TRY(e->d_t_uoff.ensure(sizeof(int) * t.uoff.size()), "alloc gather lists");
+    FK_TRY(e->d_t_ucol.ensure(sizeof(int) * std::max<size_t>(t.ucol.size(), 1)), "alloc gather lists");
+    FK_TRY(e->d_t_own.ensure(sizeof(int) * std::max<size_t>(tiles, 1)), "alloc gather lists");
+    FK_TRY(e->d_t_kslot.ensure(sizeof(unsigned short) * std::max<size_t>(t.kslot.size(), 1)), "alloc gather lists");
+    FK_TRY(e->d_t_base.ensure(sizeof(int)), "alloc gather lists");
+    FK_TRY(e->d_err.ensure(sizeof(int)), "alloc error flag");
+    FK_TRY(cudaMemcpy(e->d_t_uoff.p, t.uoff.data(), sizeof(int) * t.uoff.size(), cudaMemcpyHostToDevice), "upload lists");
+    FK_TRY(cudaMemcpy(e->d_t_ucol.p, t.ucol.data(), sizeof(int) * t.ucol.size(), cudaMemcpyHostToDevice), "upload lists");
+    FK_TRY(cudaMemcpy(e->d_t_own.p, t.own.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice), "upload lists");
+    FK_TRY(cudaMemcpy(e->d_t_kslot.p, t.kslot.data(), sizeof(unsigned short) * t.kslot.size(), cudaMemcpyHostToDevice),
+           "upload lists");
+    FK_TRY(cudaMemset(e->d_t_base.p, 0, sizeof(int)), "clear tile base");
+    FK_TRY(cudaMemset(e->d_err.p, 0, sizeof(int)), "clear error flag");
+    c.staged = true;
+    c.NP = NP;
+    c.stage_cap = nk_max;
+    c.smem = smem;
+    c.umax = t.umax;
+    (void)per_blk;
+    return FK_OK;
+}
+
+fk::StageTables stage_tables(fk_engine* e, const KCfg& c) {
+    return fk::StageTables{e->d_t_base.as<int>(), e->d_t_uoff.as<int>(), e->d_t_ucol.as<int>(), e->d_t_own.as<int>(),
+                           e->d_t_kslot.as<unsigned short>(), c.umax, e->d_err.as<int>()};
+}
+
+// A staged kernel that ran out of its bounded wait left a mark: report and clear it.
+int check_staged_error(fk_engine* e) {
+    if (!e->cfg[fk::kStep].staged || !e->d_err.p) return FK_OK;
+    int flag = 0;
+    FK_TRY(cudaMemcpy(&flag, e->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+    if (flag) {
+        cudaMemset(e->d_err.p, 0, sizeof(int));
+        return e->fail(FK_ERR_TIMEOUT, "a staged step kernel gave up waiting for its row copies");
+    }
+    return FK_OK;
+}
+
 int configure(fk_engine* e) {
     for (auto& c : e->cfg) c.valid = false;
     if (e->n_b == 0 || e->s == 0 || e->n != e->n_b * e->b) return FK_OK;   // configured once both are set
@@ -256,8 +319,13 @@ int configure(fk_engine* e) {
         c.Gp = Gp; c.NP = NP; c.slices = slices; c.W = W;
         c.stage_cap = kind == fk::kOuter ? 0 : stage_cap;
         c.smem = c.stage_cap ? ((size_t)c.stage_cap * per_blk + 15) / 16 * 16 : 0;
+        c.staged = false;
+        if (kind == fk::kStep && e->opt_tma) {
+            int rc = configure_staged(e, c, Gp, nk_max, per_blk);
+            if (rc != FK_OK) return rc;
+        }
         int occ = 0;
-        FK_TRY(prec_occupancy(e, kind, NP, c.smem, &occ), "occupancy query");
+        FK_TRY(prec_occupancy(e, c.staged ? (int)fk::kStepStaged : kind, c.NP, c.smem, &occ), "occupancy query");
         if (occ < 1) return e->fail(FK_ERR_UNSUPPORTED, "kernel kind %d does not fit on an SM", kind);
         if (e->opt_ctas_per_sm > 0) occ = std::min(occ, e->opt_ctas_per_sm);
         c.ctas = (int)std::max<long long>(1, std::min<long long>(tiles, (long long)occ * e->num_sms));
@@ -309,7 +377,19 @@ int run_step(fk_engine* e, const void* x, const void* z, void* y, bool two, bool
         a.partials = want_dots ? partials_step + (size_t)sl * c.ctas * 2 : nullptr;
         a.stage_cap = c.stage_cap;
         ProfScope ps(e, fk::kStep);
-        FK_TRY(prec_launch_step(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "step kernel launch");
+        if (c.staged) {
+            const fk::StageTables tb = stage_tables(e, c);
+            const fk::Launch l{c.ctas, c.smem, e->stream};
+            cudaError_t ce;
+            switch (e->prec) {
+                case fk::kF64: ce = fk::launch_step_staged_f64(e->cplx, e->b, c.NP, a, tb, l); break;
+                case fk::kF32: ce = fk::launch_step_staged_f32(e->cplx, e->b, c.NP, a, tb, l); break;
+                default: ce = fk::launch_step_staged_ds(e->cplx, e->b, c.NP, a, tb, l); break;
+            }
+            FK_TRY(ce, "staged step kernel launch");
+        } else {
+            FK_TRY(prec_launch_step(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "step kernel launch");
+        }
     }
     return FK_OK;
 }
@@ -507,6 +587,7 @@ int moments_fetch(fk_engine* e, double* mu) {
     FK_TRY(cudaMemcpyAsync(e->h_raw.data(), e->d_raw.p, sizeof(double) * 2 * nsteps, cudaMemcpyDeviceToHost, e->stream),
            "copy moment sums");
     FK_TRY(cudaStreamSynchronize(e->stream), "moments");
+    if (int rc = check_staged_error(e)) return rc;
     // mu_0 = <a0,a0>, mu_1 = Re<a1,a0>, mu_2m = 2<a_m,a_m> - mu_0, mu_2m+1 = 2 Re<a_m+1,a_m> - mu_1
     mu[0] = e->h_raw[0];
     mu[1] = e->h_raw[1];
@@ -637,8 +718,51 @@ int fetch_D(fk_engine* e, double* D) {
     const size_t dn = (size_t)e->d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
     if (dn) FK_TRY(cudaMemcpyAsync(D, e->dd_acc.p, sizeof(double) * dn, cudaMemcpyDeviceToHost, e->stream), "copy D");
     FK_TRY(cudaStreamSynchronize(e->stream), "D calculation");
+    if (int rc = check_staged_error(e)) return rc;
     if (e->profiling) prof_flush(e);
     return FK_OK;
+}
+
+}  // namespace
+
+// ===================================================================================
+// Jackson-damped expansion coefficients in FP64 on the device
+// (expansion_coefficients, reference src/fastkpm.cpp:41-78; jackson_kernel :13-20;
+//  fermi_density / fermi_energy :375-393)
+// ===================================================================================
+namespace {
+
+__device__ double dev_fermi(int kind, double x, double kT, double mu) {
+    const double a = (x - mu) / fabs(kT);
+    if (kT < 1e-15 || fabs(a) > 20) return kind == 0 ? (x < mu ? 1.0 : 0.0) : (x < mu ? (x - mu) : 0.0);
+    return kind == 0 ? 1.0 / (exp(a) + 1.0) : -kT * log(1.0 + exp(-a));
+}
+
+// One CTA per order m: c_m = (m == 0 ? 1 : 2) g_m (1/Mq) sum_i f(E_i) T_m(x_i), x_i = cos(pi (i + 1/2) / Mq),
+// T_m(x_i) = cos(m pi (i + 1/2) / Mq); the node sum is reduced in a fixed order.
+__global__ void k_expansion_coefficients(int M, int Mq, int kind, double kT, double mu, double avg, double mag,
+                                         double* out) {
+    const int m = blockIdx.x;
+    if (m >= M) return;
+    const double pi = 3.141592653589793238463;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < Mq; i += blockDim.x) {
+        const double th = pi * (i + 0.5) / Mq;
+        const double f = dev_fermi(kind, cos(th) * mag + avg, kT, mu);
+        acc += f * cos(m * th);
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double Mp = M + 1.0;
+        const double g = ((Mp - m) * cos(pi * m / Mp) + sin(pi * m / Mp) / tan(pi / Mp)) / Mp;
+        out[m] = (m == 0 ? 1.0 : 2.0) * g * red[0] / Mq;
+    }
 }
 
 }  // namespace
@@ -781,7 +905,8 @@ int fk_engine_destroy(fk_engine* e) {
     if (e->t_stop) cudaEventDestroy(e->t_stop);
     DevBuf* bufs[] = {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2], &e->d_V[3],
                       &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc, &e->d_partials, &e->d_raw,
-                      &e->d_coef, &e->d_stage};
+                      &e->d_coef, &e->d_stage, &e->d_t_uoff, &e->d_t_ucol, &e->d_t_own, &e->d_t_kslot,
+                      &e->d_t_base, &e->d_err};
     for (auto* b : bufs) b->release();
     for (auto& c : e->cfg) { c.sys.release(); c.cta_sys.release(); }
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
@@ -833,6 +958,7 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             e->opt_ctas_per_sm = value; return configure(e);
         case FK_OPT_STAGE_H: e->opt_stage = value ? 1 : 0; return configure(e);
         case FK_OPT_GRAPHS: e->opt_graphs = value ? 1 : 0; return FK_OK;
+        case FK_OPT_TMA: e->opt_tma = value ? 1 : 0; return configure(e);
         default: return e->fail(FK_ERR_ARG, "unknown option %d", option);
     }
 }
@@ -852,6 +978,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_CTAS_PER_SM: *value = e->opt_ctas_per_sm; return FK_OK;
         case FK_OPT_STAGE_H: *value = e->opt_stage; return FK_OK;
         case FK_OPT_GRAPHS: *value = e->opt_graphs; return FK_OK;
+        case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? 1 : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }
 }
@@ -1059,6 +1186,24 @@ int fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* ro
     *hi = emax + slack;
     ab.release();
     part.release();
+    return FK_OK;
+}
+
+int fk_engine_expansion_coefficients(fk_engine* e, int M, int Mq, int f_kind, double kT, double mu, double es_lo,
+                                     double es_hi, double* out) {
+    if (!e || !out) return FK_ERR_ARG;
+    if (M < 1 || Mq < M || (f_kind != 0 && f_kind != 1) || !(es_hi > es_lo))
+        return e->fail(FK_ERR_ARG, "expansion_coefficients: need 1 <= M <= Mq, f_kind 0/1, hi > lo");
+    cudaSetDevice(e->device);
+    DevBuf d;
+    FK_TRY(d.ensure(sizeof(double) * M), "alloc coefficients");
+    k_expansion_coefficients<<<M, 256, 0, e->stream>>>(M, Mq, f_kind, kT, mu, (es_hi + es_lo) / 2.0,
+                                                       (es_hi - es_lo) / 2.0, d.as<double>());
+    cudaError_t ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(out, d.p, sizeof(double) * M, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    d.release();
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "expansion coefficients");
     return FK_OK;
 }
 

@@ -6,6 +6,7 @@
 // none, classifies every block (2: real multiple of the identity, 1: real entries,
 // 0: general) and converts the entries to the engine precision.
 #pragma once
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -117,6 +118,48 @@ inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* ro
         }
     }
     return FK_OK;
+}
+
+// Per-tile gather lists of the staged step kernel: for every tile of kThreads (row, lane)
+// items, the distinct block columns its rows touch plus the tile's own rows, sorted; the
+// slot of the tile's first own row; and for every H block the slot of its column.
+struct TileTables {
+    std::vector<int> uoff{0};             // tiles + 1 offsets into ucol
+    std::vector<int> ucol;                // global block columns
+    std::vector<int> own;                 // per tile
+    std::vector<unsigned short> kslot;    // per H block (global block index)
+    int umax = 0;
+};
+
+// Append one system's tiles. rp/col: the system's BSR (local rows, local columns); its
+// blocks sit at global block index kslot_off + k and its columns at col_off + col.
+inline bool append_tile_tables(const int* rp, const int* col, int n_b, int Gp, int col_off, size_t kslot_off,
+                               TileTables& t) {
+    const long long items = (long long)n_b * Gp;
+    const long long tiles = (items + kThreads - 1) / kThreads;
+    if (t.kslot.size() < kslot_off + (size_t)rp[n_b]) t.kslot.resize(kslot_off + (size_t)rp[n_b]);
+    std::vector<int> u;
+    for (long long tt = 0; tt < tiles; tt++) {
+        const int r_lo = (int)(tt * kThreads / Gp);
+        const long long tl = (tt + 1) * kThreads < items ? (tt + 1) * kThreads - 1 : items - 1;
+        const int r_hi = (int)(tl / Gp);
+        u.clear();
+        for (int r = r_lo; r <= r_hi; r++) {
+            u.push_back(r);
+            for (int k = rp[r]; k < rp[r + 1]; k++) u.push_back(col[k]);
+        }
+        std::sort(u.begin(), u.end());
+        u.erase(std::unique(u.begin(), u.end()), u.end());
+        if (u.size() >= 65535) return false;
+        t.own.push_back((int)(std::lower_bound(u.begin(), u.end(), r_lo) - u.begin()));
+        for (int r = r_lo; r <= r_hi; r++)
+            for (int k = rp[r]; k < rp[r + 1]; k++)
+                t.kslot[kslot_off + k] = (unsigned short)(std::lower_bound(u.begin(), u.end(), col[k]) - u.begin());
+        for (int c : u) t.ucol.push_back(c + col_off);
+        t.uoff.push_back((int)t.ucol.size());
+        if ((int)u.size() > t.umax) t.umax = (int)u.size();
+    }
+    return true;
 }
 
 // Largest number of H blocks one tile of kThreads (row, lane) items touches.

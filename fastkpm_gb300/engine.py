@@ -397,6 +397,14 @@ class Engine:
         self._check(self.lib.fk_engine_fetch_D(self.h, _dp(out.view(np.float64))), "fetch_D")
         D.val = out
 
+    def expansion_coefficients(self, M, Mq, f, kT, mu, es):
+        """Jackson-damped Fermi expansion computed in FP64 on this engine's device."""
+        kind = {"fermi_density": 0, "fermi_energy": 1}[f]
+        out = np.zeros(M)
+        self._check(self.lib.fk_engine_expansion_coefficients(self.h, M, Mq, kind, kT, mu, es.lo, es.hi, _dp(out)),
+                    "expansion_coefficients")
+        return out
+
     def moments2_v1(self, *a, **k):
         raise NotImplementedError("moments2_v1 (conductivity) is not part of the GB300 build")
 

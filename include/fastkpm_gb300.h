@@ -78,6 +78,8 @@ int  fk_engine_synchronize(fk_engine* e);
 #define FK_OPT_NP_STEP     5   /* packets per lane of the step kernel only (0: FK_OPT_NP / default)               */
 #define FK_OPT_NP_ADJOINT  6   /* ... of the adjoint kernel only                                                  */
 #define FK_OPT_NP_OUTER    7   /* ... of the outer-product kernel only                                            */
+#define FK_OPT_TMA         8   /* 1: stage the step kernel's neighbour rows with TMA bulk copies when the per-tile
+                                * gather lists fit shared memory; 0 (default): per-thread gathers                 */
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 
@@ -125,6 +127,13 @@ int  fk_engine_fetch_D(fk_engine* e, double* D_val);
 int  fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr,
                             const int* col_idx, const double* val, double extend, int iters,
                             const double* v0, double* lo, double* hi);
+
+/* expansion_coefficients(M, Mq, f, es) with f = fermi_density(., kT, mu) (f_kind 0) or
+ * fermi_energy(., kT, mu) (f_kind 1) and the Jackson kernel (reference src/fastkpm.cpp:13-78,
+ * :375-393), computed in FP64 on the engine's device: T_m at the Mq Chebyshev nodes as
+ * cos(m theta_i), node sums reduced in a fixed order. out[M] on the host. */
+int  fk_engine_expansion_coefficients(fk_engine* e, int M, int Mq, int f_kind, double kT, double mu,
+                                      double es_lo, double es_hi, double* out);
 
 /* Profiling: when on, each kernel launch is bracketed by CUDA events on the engine's stream. */
 int  fk_engine_set_profiling(fk_engine* e, int on);

@@ -96,6 +96,8 @@ def test_identity_probes_exact_traces(gpu, prec):
 
 
 @pytest.mark.parametrize("opts", [
+    {L.FK_OPT_TMA: 0},
+    {L.FK_OPT_FUSE_D: 1},
     {L.FK_OPT_FUSE_D: 0},
     {L.FK_OPT_STAGE_H: 0},
     {L.FK_OPT_NP: 1},
@@ -169,6 +171,34 @@ def test_missing_diagonal_blocks_are_inserted(gpu):
     mu, mu_ref, D, D_ref = run_pair(H0, es, R, False, "fp64", M, c, "stoch")
     assert mu_err(mu, mu_ref) <= 1e-12
     assert rel_err(D, D_ref) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+def test_staged_and_plain_step_agree(gpu, prec):
+    """The TMA-staged step kernel (default when its gather lists fit) and the per-thread-gather
+    kernel compute the same rows in the same order: moments agree to rounding of the CTA sums."""
+    H, es, R = small_complex_case(6, 32, 4)
+    M = 30
+    mus = []
+    for tma in (1, 0):
+        eng = fk.Engine(True, prec)
+        eng.set_option(L.FK_OPT_TMA, tma)
+        eng.set_H(H, es)
+        eng.set_R(R)
+        assert eng.get_option(L.FK_OPT_TMA) == tma
+        mus.append(eng.moments(M))
+        eng.close()
+    assert np.max(np.abs(mus[0] - mus[1])) / abs(mus[1][0]) <= 1e-13
+
+
+def test_device_expansion_coefficients(gpu):
+    """FP64 coefficients on the device match the host restatement (<= 1e-13 absolute)."""
+    eng = fk.Engine(False, "fp64")
+    for kind in ["fermi_density", "fermi_energy"]:
+        for (M, Mq, kT, mu, lo, hi) in [(200, 400, 0.0, 0.0, -4.5, 4.5), (1000, 2000, 0.05, 0.3, -7.07, 7.07)]:
+            c = eng.expansion_coefficients(M, Mq, kind, kT, mu, fk.EnergyScale(lo, hi))
+            ref = O.expansion_coefficients(M, Mq, kind, kT, mu, lo, hi)
+            assert np.max(np.abs(c - ref)) <= 1e-13
 
 
 def test_results_are_deterministic(gpu):
