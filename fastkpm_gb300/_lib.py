@@ -89,7 +89,7 @@ def load(path=None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("FKPM_LIB_PATH") or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError(
             "libfastkpm_gb300.so is not built (%s); run `python -c 'import __graft_entry__ as g; g.build()'`"

@@ -10,7 +10,7 @@
 namespace fk {
 
 enum Prec { kF64 = 0, kF32 = 1, kDS = 2 };
-enum KernelKind { kStep = 0, kAdjoint = 1, kOuter = 2, kHelper = 3, kNumKinds = 4, kStepStaged = 5 };
+enum KernelKind { kStep = 0, kAdjoint = 1, kOuter = 2, kHelper = 3, kNumKinds = 4, kStepStaged = 5, kStepStagedAsync = 6 };
 
 struct Launch {
     int grid;
@@ -28,8 +28,8 @@ inline int elems_per_packet(int prec, int cplx) { return 16 / elem_bytes(prec, c
 // Per-precision entry points (defined in fk_inst_<prec>.cu)
 #define FK_DECLARE_PREC(P)                                                                                  \
     cudaError_t launch_step_##P(int cplx, int B, int NP, const StepArgs& a, const Launch& l);              \
-    cudaError_t launch_step_staged_##P(int cplx, int B, int NP, const StepArgs& a, const StageTables& t,   \
-                                       const Launch& l);                                                  \
+    cudaError_t launch_step_staged_##P(int cplx, int B, int NP, int tma, const StepArgs& a,                \
+                                       const StageTables& t, const Launch& l);                            \
     cudaError_t launch_adjoint_##P(int cplx, int B, int NP, const AdjArgs& a, const Launch& l);            \
     cudaError_t launch_outer_##P(int cplx, int B, int NP, const OuterArgs& a, const Launch& l);            \
     cudaError_t occupancy_##P(int kind, int cplx, int B, int NP, size_t smem, int* blocks_per_sm);         \

@@ -325,7 +325,8 @@ int configure(fk_engine* e) {
             if (rc != FK_OK) return rc;
         }
         int occ = 0;
-        FK_TRY(prec_occupancy(e, c.staged ? (int)fk::kStepStaged : kind, c.NP, c.smem, &occ), "occupancy query");
+        const int okind = !c.staged ? kind : (e->opt_tma == 1 ? (int)fk::kStepStaged : (int)fk::kStepStagedAsync);
+        FK_TRY(prec_occupancy(e, okind, c.NP, c.smem, &occ), "occupancy query");
         if (occ < 1) return e->fail(FK_ERR_UNSUPPORTED, "kernel kind %d does not fit on an SM", kind);
         if (e->opt_ctas_per_sm > 0) occ = std::min(occ, e->opt_ctas_per_sm);
         c.ctas = (int)std::max<long long>(1, std::min<long long>(tiles, (long long)occ * e->num_sms));
@@ -382,9 +383,9 @@ int run_step(fk_engine* e, const void* x, const void* z, void* y, bool two, bool
             const fk::Launch l{c.ctas, c.smem, e->stream};
             cudaError_t ce;
             switch (e->prec) {
-                case fk::kF64: ce = fk::launch_step_staged_f64(e->cplx, e->b, c.NP, a, tb, l); break;
-                case fk::kF32: ce = fk::launch_step_staged_f32(e->cplx, e->b, c.NP, a, tb, l); break;
-                default: ce = fk::launch_step_staged_ds(e->cplx, e->b, c.NP, a, tb, l); break;
+                case fk::kF64: ce = fk::launch_step_staged_f64(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l); break;
+                case fk::kF32: ce = fk::launch_step_staged_f32(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l); break;
+                default: ce = fk::launch_step_staged_ds(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l); break;
             }
             FK_TRY(ce, "staged step kernel launch");
         } else {
@@ -958,7 +959,10 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             e->opt_ctas_per_sm = value; return configure(e);
         case FK_OPT_STAGE_H: e->opt_stage = value ? 1 : 0; return configure(e);
         case FK_OPT_GRAPHS: e->opt_graphs = value ? 1 : 0; return FK_OK;
-        case FK_OPT_TMA: e->opt_tma = value ? 1 : 0; return configure(e);
+        case FK_OPT_TMA:
+            if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "TMA must be 0, 1 or 2");
+            e->opt_tma = value;
+            return configure(e);
         default: return e->fail(FK_ERR_ARG, "unknown option %d", option);
     }
 }
@@ -978,7 +982,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_CTAS_PER_SM: *value = e->opt_ctas_per_sm; return FK_OK;
         case FK_OPT_STAGE_H: *value = e->opt_stage; return FK_OK;
         case FK_OPT_GRAPHS: *value = e->opt_graphs; return FK_OK;
-        case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? 1 : 0) : e->opt_tma; return FK_OK;
+        case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }
 }

@@ -11,15 +11,19 @@ cudaError_t step_one(const StepArgs& a, const Launch& l) {
     k_cheb_step<S, B, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     return cudaGetLastError();
 }
-template <class S, int B, int NP>
-cudaError_t staged_one(const StepArgs& a, const StageTables& t, const Launch& l) {
+template <class S, int B, int NP, bool TMA>
+cudaError_t staged_launch(const StepArgs& a, const StageTables& t, const Launch& l) {
     if (l.smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute((const void*)k_cheb_step_staged<S, B, NP>,
+        cudaError_t e = cudaFuncSetAttribute((const void*)k_cheb_step_staged<S, B, NP, TMA>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem);
         if (e != cudaSuccess) return e;
     }
-    k_cheb_step_staged<S, B, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a, t);
+    k_cheb_step_staged<S, B, NP, TMA><<<l.grid, kThreads, l.smem, l.stream>>>(a, t);
     return cudaGetLastError();
+}
+template <class S, int B, int NP>
+cudaError_t staged_one(const StepArgs& a, const StageTables& t, const Launch& l, int tma) {
+    return tma ? staged_launch<S, B, NP, true>(a, t, l) : staged_launch<S, B, NP, false>(a, t, l);
 }
 template <class S, int B, int NP>
 cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
@@ -35,7 +39,8 @@ template <class S, int B, int NP>
 cudaError_t occ_one(int kind, size_t smem, int* n) {
     const void* f = kind == kStep ? (const void*)k_cheb_step<S, B, NP>
                   : kind == kAdjoint ? (const void*)k_adjoint_step<S, B, NP>
-                  : kind == kStepStaged ? (const void*)k_cheb_step_staged<S, B, NP>
+                  : kind == kStepStaged ? (const void*)k_cheb_step_staged<S, B, NP, true>
+                  : kind == kStepStagedAsync ? (const void*)k_cheb_step_staged<S, B, NP, false>
                   : (const void*)k_outer<S, B, NP>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -72,9 +77,9 @@ cudaError_t occ_one(int kind, size_t smem, int* n) {
 cudaError_t FK_CAT(launch_step, FK_PREC_NAME)(int cplx, int B, int NP, const StepArgs& a, const Launch& l) {
     FK_DISPATCH(step_one, a, l);
 }
-cudaError_t FK_CAT(launch_step_staged, FK_PREC_NAME)(int cplx, int B, int NP, const StepArgs& a, const StageTables& t,
-                                                   const Launch& l) {
-    FK_DISPATCH(staged_one, a, t, l);
+cudaError_t FK_CAT(launch_step_staged, FK_PREC_NAME)(int cplx, int B, int NP, int tma, const StepArgs& a,
+                                                   const StageTables& t, const Launch& l) {
+    FK_DISPATCH(staged_one, a, t, l, tma);
 }
 cudaError_t FK_CAT(launch_adjoint, FK_PREC_NAME)(int cplx, int B, int NP, const AdjArgs& a, const Launch& l) {
     FK_DISPATCH(adj_one, a, l);

@@ -64,13 +64,24 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 }
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// 16-byte asynchronous global -> shared copy (bypasses L1), grouped and waited by the hardware
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // Shared-memory bytes the staged step kernel needs.
 __host__ __device__ inline size_t staged_smem_bytes(int umax, int B, int W, int stage_cap, int hsize) {
     const size_t buf = (size_t)umax * B * W * 16;
     return 128 + 2 * buf + (size_t)stage_cap * ((size_t)B * B * hsize + 4 + 2) + 16;
 }
 
-template <class S, int B, int NP>
+// TMA = true: warp 0 issues one cp.async.bulk per row chunk, completion on an mbarrier.
+// TMA = false: every thread issues 16-byte cp.async copies of its share of the unit's
+// row chunks (commit/wait groups); no spin loop at all.
+template <class S, int B, int NP, bool TMA>
 __global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, StageTables tb) {
     typedef typename S::E E;
     typedef typename S::H H;
@@ -105,14 +116,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, St
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
-        mbar_fence_init();
+        if constexpr (TMA) {
+            mbar_init(&mbar[0], 1);
+            mbar_init(&mbar[1], 1);
+            mbar_fence_init();
+        }
         s_fail = 0;
     }
     __syncthreads();
 
-    // warp 0: put the row chunks of `unit` in flight into buffer unit & 1
+    // put the row chunks of `unit` in flight into buffer unit & 1
+    // (TMA: warp 0 only; cp.async: every thread, then one commit group per thread)
     auto issue = [&](int unit) {
         const int lt = lc + (unit / nch) * sd.ctas;
         const int c = unit % nch;
@@ -120,30 +134,43 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, St
         const int u0 = tb.uoff[gt];
         const int nu = tb.uoff[gt + 1] - u0;
         const int pk = min(W, P - c * W);
-        const unsigned row_bytes = (unsigned)pk * 16u;
         uint4* dstb = buf0 + (size_t)(unit & 1) * buf_packets;
-        // the generic-proxy reads of this buffer (two units ago, ordered by the CTA barrier)
-        // must precede this lane's async-proxy writes into it
-        fence_proxy_async_smem();
-        if (lane == 0) mbar_expect_tx(&mbar[unit & 1], row_bytes * (unsigned)(nu * B));
-        __syncwarp();
-        for (int q = lane; q < nu * B; q += 32) {
-            const int ui = q / B, bj = q - (q / B) * B;
-            const int col = tb.ucol[u0 + ui];
-            const E* src = x + (size_t)(B * col + bj) * a.ld + (size_t)c * W * EPP;
-            bulk_g2s(dstb + (size_t)(ui * B + bj) * W, src, row_bytes, &mbar[unit & 1]);
+        if constexpr (TMA) {
+            const unsigned row_bytes = (unsigned)pk * 16u;
+            // the generic-proxy reads of this buffer (two units ago, ordered by the CTA barrier)
+            // must precede this lane's async-proxy writes into it
+            fence_proxy_async_smem();
+            if (lane == 0) mbar_expect_tx(&mbar[unit & 1], row_bytes * (unsigned)(nu * B));
+            __syncwarp();
+            for (int q = lane; q < nu * B; q += 32) {
+                const int ui = q / B, bj = q - (q / B) * B;
+                const int col = tb.ucol[u0 + ui];
+                const E* src = x + (size_t)(B * col + bj) * a.ld + (size_t)c * W * EPP;
+                bulk_g2s(dstb + (size_t)(ui * B + bj) * W, src, row_bytes, &mbar[unit & 1]);
+            }
+        } else {
+            const int per_col = B * pk;   // packets of one distinct column in this chunk
+            for (int q = threadIdx.x; q < nu * per_col; q += kThreads) {
+                const int ui = q / per_col;
+                const int rem = q - ui * per_col;
+                const int bj = rem / pk, p = rem - (rem / pk) * pk;
+                const int col = tb.ucol[u0 + ui];
+                const E* src = x + (size_t)(B * col + bj) * a.ld + (size_t)(c * W + p) * EPP;
+                cp_async16(dstb + (size_t)(ui * B + bj) * W + p, src);
+            }
+            cp_async_commit();
         }
     };
 
     typename S::Dot dxx = S::dot_zero(), dyx = S::dot_zero();
-    if (warp == 0 && n_units > 0) issue(0);
+    if ((TMA ? warp == 0 : true) && n_units > 0) issue(0);
     int k_lo = 0;
     for (int unit = 0; unit < n_units; unit++) {
         const int lt = lc + (unit / nch) * sd.ctas;
         const int c = unit % nch;
         const long long t0 = (long long)lt * kThreads;
         const int r_lo = sd.row_base + (int)(t0 / Gp);
-        if (warp == 0 && unit + 1 < n_units) issue(unit + 1);
+        if ((TMA ? warp == 0 : true) && unit + 1 < n_units) issue(unit + 1);
         if (c == 0) {
             // H blocks, their columns and their slots for this tile
             const long long t_last = min(t0 + kThreads, items) - 1;
@@ -156,18 +183,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, St
             }
             for (int q = threadIdx.x; q < nk * B * B; q += blockDim.x) s_h[q] = hval[(size_t)k_lo * B * B + q];
         }
-        // wait for this unit's row chunks: thread 0 with a bound, then everyone acquires
-        if (threadIdx.x == 0 && !mbar_wait_bounded(&mbar[unit & 1], (unsigned)(unit >> 1) & 1u)) s_fail = 1;
-        __syncthreads();
-        if (s_fail) {
-            if (threadIdx.x == 0) {
-                atomicExch(tb.err, 1);
-                // the next unit's copies may be in flight: wait for them (bounded) before leaving
-                if (unit + 1 < n_units) mbar_wait_bounded(&mbar[(unit + 1) & 1], (unsigned)((unit + 1) >> 1) & 1u);
+        if constexpr (TMA) {
+            // wait for this unit's row chunks: thread 0 with a bound, then everyone acquires
+            if (threadIdx.x == 0 && !mbar_wait_bounded(&mbar[unit & 1], (unsigned)(unit >> 1) & 1u)) s_fail = 1;
+            __syncthreads();
+            if (s_fail) {
+                if (threadIdx.x == 0) {
+                    atomicExch(tb.err, 1);
+                    // the next unit's copies may be in flight: wait for them (bounded) before leaving
+                    if (unit + 1 < n_units) mbar_wait_bounded(&mbar[(unit + 1) & 1], (unsigned)((unit + 1) >> 1) & 1u);
+                }
+                return;
             }
-            return;
+            mbar_wait_bounded(&mbar[unit & 1], (unsigned)(unit >> 1) & 1u);   // completed: returns at once
+        } else {
+            // this thread's copies of this unit are done once at most the next unit's group is pending
+            if (unit + 1 < n_units) cp_async_wait<1>();
+            else cp_async_wait<0>();
+            __syncthreads();
         }
-        mbar_wait_bounded(&mbar[unit & 1], (unsigned)(unit >> 1) & 1u);   // completed: returns at once
         const uint4* sb = buf0 + (size_t)(unit & 1) * buf_packets;
         const long long t = t0 + threadIdx.x;
         if (t < items) {

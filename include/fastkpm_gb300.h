@@ -78,8 +78,10 @@ int  fk_engine_synchronize(fk_engine* e);
 #define FK_OPT_NP_STEP     5   /* packets per lane of the step kernel only (0: FK_OPT_NP / default)               */
 #define FK_OPT_NP_ADJOINT  6   /* ... of the adjoint kernel only                                                  */
 #define FK_OPT_NP_OUTER    7   /* ... of the outer-product kernel only                                            */
-#define FK_OPT_TMA         8   /* 1: stage the step kernel's neighbour rows with TMA bulk copies when the per-tile
-                                * gather lists fit shared memory; 0 (default): per-thread gathers                 */
+#define FK_OPT_TMA         8   /* step kernel gathers: 0 (default) per-thread loads; when the per-tile gather lists
+                                * fit shared memory, 1 stages them with TMA bulk copies (mbarrier completion),
+                                * 2 with per-thread 16-byte cp.async copies; reading the option returns the mode
+                                * in use                                                                         */
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 
