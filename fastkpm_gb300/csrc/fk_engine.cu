@@ -17,6 +17,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -71,7 +72,7 @@ struct fk_engine {
     std::string err;
 
     // options
-    int opt_fuse_d = 2, opt_np = 0, opt_ctas_per_sm = 0, opt_stage = 1, opt_graphs = 0;
+    int opt_fuse_d = 2, opt_np = 0, opt_ctas_per_sm = 0, opt_stage = 2, opt_graphs = 0;
     int opt_np_kind[3] = {0, 0, 0};   // per kernel kind (step, adjoint, outer); 0 = opt_np / default
     // Stage the step kernel's gathers with TMA bulk copies when they fit. Off by default: on the
     // cubic L=64 workload the per-copy cost of its 512-byte row chunks made it 2-3x slower than
@@ -110,6 +111,11 @@ struct fk_engine {
 
     // timer
     cudaEvent_t t_start = nullptr, t_stop = nullptr;
+
+    // captured launch sequences (FK_OPT_GRAPHS), keyed by call kind and shape; each keeps the
+    // buffer addresses and launch shapes it was captured with and is recaptured when they change
+    struct GraphEntry { std::vector<long long> sig; cudaGraphExec_t exec = nullptr; };
+    std::map<long long, GraphEntry> graphs;
 
     // profiling
     bool profiling = false;
@@ -205,14 +211,81 @@ struct ProfScope {
         if (e->profiling) { cudaEventRecord(b, e->stream); e->prof_pending.push_back({kind, a, b}); }
     }
 };
-cudaError_t prec_scale(fk_engine* e, const void* x, void* y, double c) {
+// y = (*c_dev) x, the factor read on the device (graph replays see new values)
+cudaError_t prec_scale(fk_engine* e, const void* x, void* y, const double* c_dev) {
     const long long ne = (long long)e->n * e->ld;
     ProfScope ps(e, fk::kHelper);
     switch (e->prec) {
-        case fk::kF64: return fk::launch_scale_f64(e->cplx, x, y, ne, c, e->stream);
-        case fk::kF32: return fk::launch_scale_f32(e->cplx, x, y, ne, c, e->stream);
-        default: return fk::launch_scale_ds(e->cplx, x, y, ne, c, e->stream);
+        case fk::kF64: return fk::launch_scale_f64(e->cplx, x, y, ne, 0.0, c_dev, e->stream);
+        case fk::kF32: return fk::launch_scale_f32(e->cplx, x, y, ne, 0.0, c_dev, e->stream);
+        default: return fk::launch_scale_ds(e->cplx, x, y, ne, 0.0, c_dev, e->stream);
     }
+}
+
+// Graph capture of a fixed launch sequence (FK_OPT_GRAPHS): captured on first use per key,
+// replayed afterwards. Keys encode the call kind and every value baked into the launches.
+long long graph_key(int kind, int M, long long extra) {
+    return ((long long)kind << 56) ^ ((long long)M << 24) ^ extra;
+}
+// Everything a captured sequence bakes in besides its key: buffer addresses, sizes and launch shapes.
+std::vector<long long> graph_signature(const fk_engine* e) {
+    std::vector<long long> s;
+    auto addr = [&](const void* p) { s.push_back((long long)(uintptr_t)p); };
+    addr(e->stream);
+    for (const DevBuf* b : {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2],
+                            &e->d_V[3], &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc,
+                            &e->d_partials, &e->d_raw, &e->d_coef})
+        addr(b->p);
+    for (long long v : {(long long)e->n_b, (long long)e->b, (long long)e->nnzb, (long long)e->n, (long long)e->s, e->ld,
+                        (long long)e->P, (long long)e->d_nnzb})
+        s.push_back(v);
+    long long mag_bits;
+    const double mag = (e->es_hi - e->es_lo) / 2.0;
+    std::memcpy(&mag_bits, &mag, sizeof mag);
+    s.push_back(mag_bits);
+    for (const KCfg& c : e->cfg) {
+        for (long long v : {(long long)c.Gp, (long long)c.NP, (long long)c.slices, (long long)c.W,
+                            (long long)c.stage_cap, (long long)c.smem, (long long)c.ctas, (long long)c.valid})
+            s.push_back(v);
+        addr(c.sys.p);
+        addr(c.cta_sys.p);
+    }
+    return s;
+}
+void drop_graphs(fk_engine* e) {
+    for (auto& g : e->graphs) cudaGraphExecDestroy(g.second.exec);
+    e->graphs.clear();
+}
+// Run a call's launch sequence directly, or (FK_OPT_GRAPHS) replay it as a CUDA graph captured on
+// first use. Not used while profiling (per-launch events) or with the staged step kernel.
+template <class F>
+int run_launches(fk_engine* e, long long key, F&& launches) {
+    if (!e->opt_graphs || e->profiling || e->cfg[fk::kStep].staged) return launches();
+    std::vector<long long> sig = graph_signature(e);
+    auto it = e->graphs.find(key);
+    if (it != e->graphs.end() && it->second.sig != sig) {
+        cudaGraphExecDestroy(it->second.exec);
+        e->graphs.erase(it);
+        it = e->graphs.end();
+    }
+    if (it == e->graphs.end()) {
+        cudaGraph_t g = nullptr;
+        FK_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const int rc = launches();
+        const cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        if (rc != FK_OK) { if (g) cudaGraphDestroy(g); return rc; }
+        if (ce != cudaSuccess) return e->cuda_fail(ce, "end capture");
+        cudaGraphExec_t ge = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return e->cuda_fail(ie, "instantiate graph");
+        fk_engine::GraphEntry ent;
+        ent.sig = std::move(sig);
+        ent.exec = ge;
+        it = e->graphs.emplace(key, std::move(ent)).first;
+    }
+    FK_TRY(cudaGraphLaunch(it->second.exec, e->stream), "graph launch");
+    return FK_OK;
 }
 void prof_flush(fk_engine* e) {
     for (auto& p : e->prof_pending) {
@@ -314,7 +387,11 @@ int configure(fk_engine* e) {
         const long long items = (long long)e->n_b * Gp;
         const long long tiles = (items + fk::kThreads - 1) / fk::kThreads;
         const int nk_max = fk::max_tile_blocks(e->h_row_ptr.data(), e->n_b, Gp);
-        const int stage_cap = (e->opt_stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
+        // FK_OPT_STAGE_H 2 (default): stage except in the FP32 step kernel, where the barrier
+        // around the stage cost more than the re-read H blocks (0.96 vs 1.03 ms per step on
+        // cubic L=64, S=256); the FP64 and DS step kernels run 12-25% faster staged.
+        const bool stage = e->opt_stage == 2 ? !(kind == fk::kStep && e->prec == fk::kF32) : e->opt_stage != 0;
+        const int stage_cap = (stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
         KCfg& c = e->cfg[kind];
         c.Gp = Gp; c.NP = NP; c.slices = slices; c.W = W;
         c.stage_cap = kind == fk::kOuter ? 0 : stage_cap;
@@ -557,26 +634,35 @@ int moments_enqueue(fk_engine* e, int M) {
     const KCfg& c = e->cfg[fk::kStep];
     const size_t per_step = (size_t)c.slices * c.ctas * 2;
     double* part = e->d_partials.as<double>();
-    // step 0: alpha_1 = Hs R; dots <R,R>, Re<alpha_1,R>
-    rc = run_step(e, e->d_R.p, nullptr, e->d_V[0].p, false, true, 0, nullptr, nullptr, part);
-    if (rc != FK_OK) return rc;
-    int x = 0, z = -1;   // x = alpha_m, z = alpha_{m-1}  (-1 = R)
-    for (int m = 1; m < nsteps; m++) {
-        const int y = (z == -1) ? 1 : z;   // never overwrite R
-        rc = run_step(e, e->V(x), e->V(z), e->V(y), true, true, 0, nullptr, nullptr, part + per_step * m);
-        if (rc != FK_OK) return rc;
-        z = x;
-        x = y;
-    }
-    // after the loop: alpha_{M/2-1} in z, alpha_{M/2} in x
-    e->mom_M = M;
-    e->mom_a0 = z;
-    e->mom_a1 = x;
-    {
+    auto launches = [&]() -> int {
+        // step 0: alpha_1 = Hs R; dots <R,R>, Re<alpha_1,R>
+        int r = run_step(e, e->d_R.p, nullptr, e->d_V[0].p, false, true, 0, nullptr, nullptr, part);
+        if (r != FK_OK) return r;
+        int x = 0, z = -1;   // x = alpha_m, z = alpha_{m-1}  (-1 = R)
+        for (int m = 1; m < nsteps; m++) {
+            const int y = (z == -1) ? 1 : z;   // never overwrite R
+            r = run_step(e, e->V(x), e->V(z), e->V(y), true, true, 0, nullptr, nullptr, part + per_step * m);
+            if (r != FK_OK) return r;
+            z = x;
+            x = y;
+        }
         ProfScope ps(e, fk::kHelper);
         k_reduce_steps<<<(nsteps * 32 + 255) / 256, 256, 0, e->stream>>>(part, (int)(per_step / 2), e->d_raw.as<double>(), nsteps);
         FK_TRY(cudaGetLastError(), "moment reduction launch");
+        return FK_OK;
+    };
+    rc = run_launches(e, graph_key(0, M, 0), launches);
+    if (rc != FK_OK) return rc;
+    // buffer roles after the loop: alpha_{M/2-1} in z, alpha_{M/2} in x
+    int x = 0, z = -1;
+    for (int m = 1; m < nsteps; m++) {
+        const int y = (z == -1) ? 1 : z;
+        z = x;
+        x = y;
     }
+    e->mom_M = M;
+    e->mom_a0 = z;
+    e->mom_a1 = x;
     e->pending_M = M;
     return FK_OK;
 }
@@ -617,26 +703,31 @@ int stoch_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, c
            "upload coefficients");
     const double* cd = e->d_coef.as<double>();
     void* xi = e->d_V[2].p;
-    // m = 1: alpha_1 = Hs R, xi = c0 R + c1 alpha_1
-    rc = run_step(e, e->d_R.p, nullptr, e->d_V[0].p, false, false, 1, xi, cd, nullptr);
-    if (rc != FK_OK) return rc;
-    int x = 0, z = -1;
-    for (int m = 2; m < M; m++) {
-        const int y = (z == -1) ? 1 : z;
-        rc = run_step(e, e->V(x), e->V(z), e->V(y), true, false, 2, xi, cd + 2 * m, nullptr);
-        if (rc != FK_OK) return rc;
-        z = x;
-        x = y;
-    }
-    // D = (R xi^dag + xi R^dag)/2 on D's pattern
     const size_t dn = (size_t)d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
-    FK_TRY(cudaMemsetAsync(e->dd_acc.p, 0, sizeof(double) * std::max<size_t>(dn, 1), e->stream), "clear D");
-    if (d_nnzb > 0) {
-        rc = run_outer(e, e->d_R.p, xi, 0.5, true);
-        if (rc != FK_OK) return rc;
-        rc = finish_D_accumulator(e, dn);
-        if (rc != FK_OK) return rc;
-    }
+    auto launches = [&]() -> int {
+        // m = 1: alpha_1 = Hs R, xi = c0 R + c1 alpha_1
+        int r = run_step(e, e->d_R.p, nullptr, e->d_V[0].p, false, false, 1, xi, cd, nullptr);
+        if (r != FK_OK) return r;
+        int x = 0, z = -1;
+        for (int m = 2; m < M; m++) {
+            const int y = (z == -1) ? 1 : z;
+            r = run_step(e, e->V(x), e->V(z), e->V(y), true, false, 2, xi, cd + 2 * m, nullptr);
+            if (r != FK_OK) return r;
+            z = x;
+            x = y;
+        }
+        // D = (R xi^dag + xi R^dag)/2 on D's pattern
+        FK_TRY(cudaMemsetAsync(e->dd_acc.p, 0, sizeof(double) * std::max<size_t>(dn, 1), e->stream), "clear D");
+        if (d_nnzb > 0) {
+            r = run_outer(e, e->d_R.p, xi, 0.5, true);
+            if (r != FK_OK) return r;
+            r = finish_D_accumulator(e, dn);
+            if (r != FK_OK) return r;
+        }
+        return FK_OK;
+    };
+    rc = run_launches(e, graph_key(1, M, 0), launches);
+    if (rc != FK_OK) return rc;
     e->mom_M = 0;   // the recursion state is no longer the one autodiff needs (reference clears a0, a1)
     e->mom_a0 = e->mom_a1 = -2;
     return FK_OK;
@@ -651,18 +742,21 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
     rc = set_D_pattern(e, d_n_b, d_nnzb, rp, ci, true);
     if (rc != FK_OK) return rc;
     const size_t dn = (size_t)d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
-    FK_TRY(cudaMemsetAsync(e->dd_acc.p, 0, sizeof(double) * std::max<size_t>(dn, 1), e->stream), "clear D");
     double diag = c[1];
     for (int m = 1; m < M / 2; m++) diag -= c[2 * m + 1];
     const int nsteps = M / 2 - 1;
-    rc = ensure_coef(e, 3 * (size_t)std::max(nsteps, 1));
+    const size_t nadj = 3 * (size_t)std::max(nsteps, 1);
+    rc = ensure_coef(e, nadj + 2);
     if (rc != FK_OK) return rc;
-    std::vector<double> coef(3 * (size_t)std::max(nsteps, 1), 0.0);
+    // per adjoint step q: {4 c_2m, 2 c_2m+1, 2 c_2m-1 or diag}; then the scale factors 2 c_{M-1}, diag
+    std::vector<double> coef(nadj + 2, 0.0);
     for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
         coef[3 * q + 0] = 4 * c[2 * m];
         coef[3 * q + 1] = 2 * c[2 * m + 1];
         coef[3 * q + 2] = (m > 1) ? 2 * c[2 * m - 1] : diag;   // m = 1 folds diag * R R^dag into beta_1
     }
+    coef[nadj] = 2 * c[M - 1];
+    coef[nadj + 1] = diag;
     FK_TRY(cudaMemcpyAsync(e->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, e->stream),
            "upload coefficients");
     // FK_OPT_FUSE_D: 1 always fuse (when D's pattern is H's), 0 never, 2 (default) by precision:
@@ -671,44 +765,52 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
     const bool fuse_pref = e->opt_fuse_d == 2 ? e->prec == fk::kF32 : e->opt_fuse_d != 0;
     const bool fuse = fuse_pref && e->d_same_as_H;
     // buffers: alpha_m in A, alpha_{m+1} in Ap (moments left alpha_{M/2-1}, alpha_{M/2})
-    int A = e->mom_a0, Ap = e->mom_a1;
-    int freeb[4], nf = 0;
-    for (int q = 0; q < 4; q++) if (q != A && q != Ap) freeb[nf++] = q;
-    int Bv = freeb[0], Bp = freeb[1];
-    if (M > 2) {
-        // beta_{M/2} = 2 c_{M-1} alpha_{M/2-1}, beta_{M/2+1} = 0
-        FK_TRY(prec_scale(e, e->V(A), e->V(Bv), 2 * c[M - 1]), "scale kernel");
-        FK_TRY(cudaMemsetAsync(e->V(Bp), 0, e->vec_bytes(), e->stream), "clear beta");
-        for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
-            if (!fuse && d_nnzb > 0) {
-                rc = run_outer(e, e->V(A), e->V(Bv), 2.0, false);   // D += 2 alpha_m beta_{m+1}^dag
-                if (rc != FK_OK) return rc;
+    const double* scales = e->d_coef.as<double>() + nadj;   // [2 c_{M-1}, diag]
+    auto launches = [&]() -> int {
+        int A = e->mom_a0, Ap = e->mom_a1;
+        int freeb[4], nf = 0;
+        for (int q = 0; q < 4; q++) if (q != A && q != Ap) freeb[nf++] = q;
+        int Bv = freeb[0], Bp = freeb[1];
+        FK_TRY(cudaMemsetAsync(e->dd_acc.p, 0, sizeof(double) * std::max<size_t>(dn, 1), e->stream), "clear D");
+        if (M > 2) {
+            // beta_{M/2} = 2 c_{M-1} alpha_{M/2-1}, beta_{M/2+1} = 0
+            FK_TRY(prec_scale(e, e->V(A), e->V(Bv), scales), "scale kernel");
+            FK_TRY(cudaMemsetAsync(e->V(Bp), 0, e->vec_bytes(), e->stream), "clear beta");
+            for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
+                if (!fuse && d_nnzb > 0) {
+                    const int r = run_outer(e, e->V(A), e->V(Bv), 2.0, false);   // D += 2 alpha_m beta_{m+1}^dag
+                    if (r != FK_OK) return r;
+                }
+                const int r = run_adjoint(e, e->V(A), e->V(Ap), e->V(Bv), e->V(Bp), e->d_coef.as<double>() + 3 * q,
+                                          fuse ? e->dd_acc.as<double>() : nullptr);
+                if (r != FK_OK) return r;
+                std::swap(A, Ap);    // A = alpha_{m-1}, Ap = alpha_m
+                std::swap(Bv, Bp);   // Bv = beta_m,   Bp = beta_{m+1}
             }
-            rc = run_adjoint(e, e->V(A), e->V(Ap), e->V(Bv), e->V(Bp), e->d_coef.as<double>() + 3 * q,
-                             fuse ? e->dd_acc.as<double>() : nullptr);
-            if (rc != FK_OK) return rc;
-            std::swap(A, Ap);    // A = alpha_{m-1}, Ap = alpha_m
-            std::swap(Bv, Bp);   // Bv = beta_m,   Bp = beta_{m+1}
+        } else {
+            // M = 2: D = diag R R^dag = R (diag R)^dag
+            FK_TRY(prec_scale(e, e->V(A), e->V(Bv), scales + 1), "scale kernel");
         }
-    } else {
-        // M = 2: D = diag R R^dag = R (diag R)^dag
-        FK_TRY(prec_scale(e, e->V(A), e->V(Bv), diag), "scale kernel");
-    }
-    // D += alpha_0 (beta_1 + diag alpha_0)^dag, then symmetrize and divide by mag
-    if (d_nnzb > 0) {
-        rc = run_outer(e, e->V(A), e->V(Bv), 1.0, false);
-        if (rc != FK_OK) return rc;
-        rc = finish_D_accumulator(e, dn);
-        if (rc != FK_OK) return rc;
-        const double mag = (e->es_hi - e->es_lo) / 2.0;
-        const long long work = (long long)d_nnzb * e->b * e->b;
-        int grid = (int)std::min<long long>((work + 255) / 256, 152LL * 16);
-        ProfScope ps(e, fk::kHelper);
-        fk::k_symmetrize_scale<<<std::max(grid, 1), 256, 0, e->stream>>>(
-            e->dd_acc.as<double>(), e->dd_rows.as<int>(), e->dd_colc.as<int>(), e->dd_pair.as<int>(), d_nnzb, e->b,
-            e->cplx, 1.0 / mag);
-        FK_TRY(cudaGetLastError(), "symmetrize launch");
-    }
+        // D += alpha_0 (beta_1 + diag alpha_0)^dag, then symmetrize and divide by mag
+        if (d_nnzb > 0) {
+            int r = run_outer(e, e->V(A), e->V(Bv), 1.0, false);
+            if (r != FK_OK) return r;
+            r = finish_D_accumulator(e, dn);
+            if (r != FK_OK) return r;
+            const double mag = (e->es_hi - e->es_lo) / 2.0;
+            const long long work = (long long)d_nnzb * e->b * e->b;
+            const int grid = (int)std::min<long long>((work + 255) / 256, 152LL * 16);
+            ProfScope ps(e, fk::kHelper);
+            fk::k_symmetrize_scale<<<std::max(grid, 1), 256, 0, e->stream>>>(
+                e->dd_acc.as<double>(), e->dd_rows.as<int>(), e->dd_colc.as<int>(), e->dd_pair.as<int>(), d_nnzb, e->b,
+                e->cplx, 1.0 / mag);
+            FK_TRY(cudaGetLastError(), "symmetrize launch");
+        }
+        return FK_OK;
+    };
+    rc = run_launches(e, graph_key(2, M, ((long long)fuse << 40) ^ ((long long)e->mom_a0 + 2) ^ ((long long)d_nnzb << 4)),
+                      launches);
+    if (rc != FK_OK) return rc;
     e->mom_M = 0;   // alpha state consumed (reference zeroes a_d[0..1])
     e->mom_a0 = e->mom_a1 = -2;
     return FK_OK;
@@ -904,6 +1006,7 @@ int fk_engine_destroy(fk_engine* e) {
     for (auto ev : e->prof_pool) cudaEventDestroy(ev);
     if (e->t_start) cudaEventDestroy(e->t_start);
     if (e->t_stop) cudaEventDestroy(e->t_stop);
+    drop_graphs(e);
     DevBuf* bufs[] = {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2], &e->d_V[3],
                       &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc, &e->d_partials, &e->d_raw,
                       &e->d_coef, &e->d_stage, &e->d_t_uoff, &e->d_t_ucol, &e->d_t_own, &e->d_t_kslot,
@@ -957,8 +1060,14 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
         case FK_OPT_CTAS_PER_SM:
             if (value < 0) return e->fail(FK_ERR_ARG, "negative CTA cap");
             e->opt_ctas_per_sm = value; return configure(e);
-        case FK_OPT_STAGE_H: e->opt_stage = value ? 1 : 0; return configure(e);
-        case FK_OPT_GRAPHS: e->opt_graphs = value ? 1 : 0; return FK_OK;
+        case FK_OPT_STAGE_H:
+            if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "STAGE_H must be 0, 1 or 2");
+            e->opt_stage = value;
+            return configure(e);
+        case FK_OPT_GRAPHS:
+            e->opt_graphs = value ? 1 : 0;
+            if (!e->opt_graphs) drop_graphs(e);
+            return FK_OK;
         case FK_OPT_TMA:
             if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "TMA must be 0, 1 or 2");
             e->opt_tma = value;
@@ -1180,7 +1289,8 @@ int fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* ro
         beta[j] = std::sqrt(ww);
         if (!(beta[j] > 0)) { iters = j; break; }   // invariant subspace found
         // v0 <- v1, v1 <- w / beta
-        FK_TRY(fk::launch_scale_f64(e->cplx, t->V(w), t->V(vz), (long long)t->n * t->ld, 1.0 / beta[j], t->stream), "lanczos scale");
+        FK_TRY(fk::launch_scale_f64(e->cplx, t->V(w), t->V(vz), (long long)t->n * t->ld, 1.0 / beta[j], nullptr, t->stream),
+               "lanczos scale");
         std::swap(v1, vz);   // new v1 = scaled w (in old vz), new v0 = old v1
     }
     double emin, emax;

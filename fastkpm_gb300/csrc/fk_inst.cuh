@@ -113,10 +113,10 @@ cudaError_t FK_CAT(launch_store_colmajor, FK_PREC_NAME)(int cplx, const void* sr
     return cudaGetLastError();
 }
 cudaError_t FK_CAT(launch_scale, FK_PREC_NAME)(int cplx, const void* x, void* y, long long n_elems, double c,
-                                             cudaStream_t st) {
+                                             const double* c_dev, cudaStream_t st) {
     const int g = helper_grid(n_elems);
-    if (cplx) k_scale<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(x), reinterpret_cast<FK_SYS_C::E*>(y), n_elems, c);
-    else k_scale<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(x), reinterpret_cast<FK_SYS_R::E*>(y), n_elems, c);
+    if (cplx) k_scale<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(x), reinterpret_cast<FK_SYS_C::E*>(y), n_elems, c, c_dev);
+    else k_scale<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(x), reinterpret_cast<FK_SYS_R::E*>(y), n_elems, c, c_dev);
     return cudaGetLastError();
 }
 

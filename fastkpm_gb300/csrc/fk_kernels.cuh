@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step(StepArgs a) {
             for (int bi = 0; bi < B; bi++)
 #pragma unroll
                 for (int e = 0; e < EPT; e++) acc[bi][e] = S::zero();
-#pragma unroll 2
+#pragma unroll 1   // measured: unrolling the block loop adds registers and no gather parallelism
             for (int k = kb; k < ke; k++) {
                 const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
                 const H* hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
@@ -662,10 +662,11 @@ __global__ void k_store_colmajor(const typename S::E* src, long long n, int ncol
     }
 }
 
-// y = c * x over the whole vector (n_elems elements)
+// y = c * x over the whole vector (n_elems elements); the factor is *c_dev when given
+// (so a replayed CUDA graph picks up new values), else c.
 template <class S>
-__global__ void k_scale(const typename S::E* x, typename S::E* y, long long n_elems, double c) {
-    const typename S::Coef cc = S::coef(c);
+__global__ void k_scale(const typename S::E* x, typename S::E* y, long long n_elems, double c, const double* c_dev) {
+    const typename S::Coef cc = S::coef(c_dev ? *c_dev : c);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_elems; q += (long long)gridDim.x * blockDim.x)
         y[q] = S::scale(cc, x[q]);
 }

@@ -202,6 +202,45 @@ def test_device_expansion_coefficients(gpu):
             assert np.max(np.abs(c - ref)) <= 1e-13
 
 
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+def test_graph_replay_matches_direct_launches(gpu, prec):
+    """FK_OPT_GRAPHS: captured sequences give bit-identical results to direct launches, replays
+    see new coefficients and new R values, and a reallocated R (more columns) is recaptured."""
+    H, es, _ = small_complex_case(4, 16, 6)
+    M = 24
+    probes = [W.phase_probes(W.cubic_colour_groups(4, 2), realisations=r, seed=s) for r, s in [(1, 1), (1, 2), (3, 3)]]
+    coefs = [W.fermi_coefficients(M, es, "fermi_energy", 0.0, mu) for mu in (0.0, 0.4)]
+
+    def run(graphs):
+        eng = fk.Engine(True, prec)
+        eng.set_option(L.FK_OPT_GRAPHS, graphs)
+        eng.set_H(H, es)
+        out = []
+        for R in probes:
+            eng.set_R(R)
+            for c in coefs:
+                D = H.pattern_like(True)
+                out.append(eng.moments(M))
+                eng.autodiff_matrix(c, D)
+                out.append(D.val.copy())
+                eng.stoch_matrix(c, D)
+                out.append(D.val.copy())
+        eng.close()
+        return out
+
+    direct, replayed = run(0), run(1)
+    for a, b in zip(direct, replayed):
+        assert np.array_equal(a, b)
+    # the replayed results are the right ones, not only repeatable
+    orc = O.OracleEngine(True)
+    orc.set_H(H, es)
+    orc.set_R(probes[2])
+    mu_ref = orc.moments(M)
+    D_ref = orc.autodiff_matrix(coefs[1], H.pattern_like(True))
+    assert mu_err(replayed[-3], mu_ref) <= TOL_MU[prec]
+    assert rel_err(replayed[-2], D_ref) <= TOL_D[prec]
+
+
 def test_results_are_deterministic(gpu):
     H, es, R = small_complex_case(6, 32, 2)
     eng = fk.Engine(True, "ds")
