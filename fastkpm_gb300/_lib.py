@@ -51,6 +51,8 @@ SIGNATURES = {
     "fk_engine_fetch_D": (_i, [_p, _dp]),
     "fk_engine_energy_scale": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _d, _i, _dp, _dp, _dp]),
     "fk_engine_expansion_coefficients": (_i, [_p, _i, _i, _i, _d, _d, _d, _d, _dp]),
+    "fk_engine_kpm_filling": (_i, [_p, _i, _d, _d, _d, _dp, _dp]),
+    "fk_engine_solve_filling": (_i, [_p, _i, _i, _d, _d, _d, _i, _i, _ip, _ip, _dp, _dp, _dp]),
     "fk_engine_set_profiling": (_i, [_p, _i]),
     "fk_engine_profile_read": (_i, [_p, _i, C.POINTER(C.c_longlong), _dp]),
     "fk_engine_profile_reset": (_i, [_p]),

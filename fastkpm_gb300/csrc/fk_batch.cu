@@ -49,7 +49,8 @@ struct PendingSystem {
 };
 
 struct Mapping {
-    int Gp = 0, NP = 0, cap_per_sm = 0, stage = 1;   // 0 = automatic
+    int Gp = 0, NP = 0, cap_per_sm = 0;   // 0 = automatic
+    int stage = -1;                       // -1 = automatic (off for FP32, as in the single engine)
 };
 
 // Process-wide memory of autotuned mappings, keyed by batch shape.
@@ -166,8 +167,9 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
         Gp = m.Gp;
         NP = m.NP > 0 ? m.NP : 1;
     } else if (P <= 32) {
-        Gp = next_pow2(P);
-        NP = 1;
+        // narrow rows: two packets per lane (measured faster than one on b=1, S=32 lattices)
+        NP = P >= 2 ? 2 : 1;
+        Gp = next_pow2((P + NP - 1) / NP);
     } else {
         Gp = 32;
         NP = (P + 31) / 32;
@@ -189,7 +191,8 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
         nk_max = std::max(nk_max, fk::max_tile_blocks(local.data(), bt->n_b[k], Gp));
     }
     const size_t per_blk = (size_t)bt->b * bt->b * bt->esize() + sizeof(unsigned);
-    bt->stage_cap = (m.stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
+    const int stage = m.stage >= 0 ? m.stage : (bt->prec == fk::kF32 ? 0 : 1);
+    bt->stage_cap = (stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
     bt->smem = bt->stage_cap ? ((size_t)bt->stage_cap * per_blk + 15) / 16 * 16 : 0;
     int occ = 0;
     BT_TRY(batch_occupancy(bt, NP, bt->smem, &occ), "occupancy query");
@@ -211,7 +214,7 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     BT_TRY(bt->d_cta_sys.ensure(sizeof(int) * base), "alloc CTA table");
     BT_TRY(cudaMemcpy(bt->d_sys.p, bt->sysd.data(), sizeof(SysDesc) * bt->n_sys, cudaMemcpyHostToDevice), "upload system table");
     BT_TRY(cudaMemcpy(bt->d_cta_sys.p, cta_sys.data(), sizeof(int) * base, cudaMemcpyHostToDevice), "upload CTA table");
-    bt->cur = Mapping{Gp, NP, m.cap_per_sm, m.stage};
+    bt->cur = Mapping{Gp, NP, m.cap_per_sm, stage};
     bt->configured = true;
     return FK_OK;
 }
@@ -462,7 +465,7 @@ int fk_batch_set_option(fk_batch* bt, int option, int value) {
             bt->opt.Gp = 0;
             break;
         case FK_OPT_CTAS_PER_SM: bt->opt.cap_per_sm = std::max(0, value); break;
-        case FK_OPT_STAGE_H: bt->opt.stage = value ? 1 : 0; break;
+        case FK_OPT_STAGE_H: bt->opt.stage = value == 2 ? -1 : (value ? 1 : 0); break;
         case FK_OPT_FUSE_D: return FK_OK;
         default: return bt->fail(FK_ERR_ARG, "unknown option %d", option);
     }

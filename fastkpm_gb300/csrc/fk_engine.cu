@@ -23,6 +23,7 @@
 
 #include "../../include/fastkpm_gb300.h"
 #include "fk_dispatch.h"
+#include "fk_post.cuh"
 #include "fk_prep.h"
 
 using fk::SysDesc;
@@ -105,6 +106,8 @@ struct fk_engine {
 
     // scratch
     DevBuf d_partials, d_raw, d_coef, d_stage;
+    DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
+    int post_M = 0, post_Mq = 0;
     std::vector<double> h_raw;
 
     KCfg cfg[fk::kNumKinds];
@@ -367,8 +370,8 @@ int configure(fk_engine* e) {
     // on the cubic L=64, S=256 workload are 4 for the step and outer kernels and 2 for the
     // adjoint kernel, whose fused epilogue holds the most live values.
     const int slices = 1, W = P;
-    // {step, adjoint, outer}; the FP64 adjoint (FP64-pipe bound) prefers the lightest threads
-    const int kDefaultNP[fk::kHelper] = {4, e->prec == fk::kF64 ? 1 : 2, 4};
+    // {step, adjoint, outer} on rows wider than 32 packets
+    const int kDefaultNP[fk::kHelper] = {4, e->prec == fk::kF64 ? 4 : 2, 4};
     const size_t per_blk = (size_t)e->b * e->b * e->hsize() + sizeof(unsigned);
     for (int kind = 0; kind < fk::kHelper; kind++) {
         int NP, Gp;
@@ -377,8 +380,10 @@ int configure(fk_engine* e) {
             NP = want;
             Gp = std::min(32, next_pow2((P + NP - 1) / NP));
         } else if (P <= 32) {
-            NP = 1;
-            Gp = next_pow2(P);
+            // narrow rows: two packets per lane (b=1 real FP32, S=32 on a 1024^2 square lattice:
+            // 0.12 ms per step with 4 lanes x 2 packets vs 0.20 ms with 8 lanes x 1)
+            NP = P >= 2 ? 2 : 1;
+            Gp = next_pow2((P + NP - 1) / NP);
         } else {
             NP = kDefaultNP[kind];
             Gp = 32;
@@ -733,8 +738,10 @@ int stoch_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, c
     return FK_OK;
 }
 
-int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp, const int* ci) {
-    if (!c) return e->fail(FK_ERR_ARG, "autodiff_matrix: null coefficients");
+// c: host coefficients, or (c == null) c_dev: device coefficients (the fixed-filling solve)
+int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb, const int* rp, const int* ci,
+                     const double* c_dev = nullptr) {
+    if (!c && !c_dev) return e->fail(FK_ERR_ARG, "autodiff_matrix: null coefficients");
     int rc = require_ready(e);
     if (rc != FK_OK) return rc;
     if (e->mom_M == 0 || e->mom_M != M)
@@ -742,27 +749,35 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
     rc = set_D_pattern(e, d_n_b, d_nnzb, rp, ci, true);
     if (rc != FK_OK) return rc;
     const size_t dn = (size_t)d_nnzb * e->b * e->b * (e->cplx ? 2 : 1);
-    double diag = c[1];
-    for (int m = 1; m < M / 2; m++) diag -= c[2 * m + 1];
     const int nsteps = M / 2 - 1;
     const size_t nadj = 3 * (size_t)std::max(nsteps, 1);
     rc = ensure_coef(e, nadj + 2);
     if (rc != FK_OK) return rc;
-    // per adjoint step q: {4 c_2m, 2 c_2m+1, 2 c_2m-1 or diag}; then the scale factors 2 c_{M-1}, diag
-    std::vector<double> coef(nadj + 2, 0.0);
-    for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
-        coef[3 * q + 0] = 4 * c[2 * m];
-        coef[3 * q + 1] = 2 * c[2 * m + 1];
-        coef[3 * q + 2] = (m > 1) ? 2 * c[2 * m - 1] : diag;   // m = 1 folds diag * R R^dag into beta_1
+    if (c) {
+        double diag = c[1];
+        for (int m = 1; m < M / 2; m++) diag -= c[2 * m + 1];
+        // per adjoint step q: {4 c_2m, 2 c_2m+1, 2 c_2m-1 or diag}; then the scale factors 2 c_{M-1}, diag
+        std::vector<double> coef(nadj + 2, 0.0);
+        for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
+            coef[3 * q + 0] = 4 * c[2 * m];
+            coef[3 * q + 1] = 2 * c[2 * m + 1];
+            coef[3 * q + 2] = (m > 1) ? 2 * c[2 * m - 1] : diag;   // m = 1 folds diag * R R^dag into beta_1
+        }
+        coef[nadj] = 2 * c[M - 1];
+        coef[nadj + 1] = diag;
+        FK_TRY(cudaMemcpyAsync(e->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice,
+                               e->stream),
+               "upload coefficients");
+    } else {
+        ProfScope ps(e, fk::kHelper);
+        fk::k_adjoint_coefs<<<1, fk::kPostThreads, 0, e->stream>>>(c_dev, M, e->d_coef.as<double>());
+        FK_TRY(cudaGetLastError(), "coefficient table launch");
     }
-    coef[nadj] = 2 * c[M - 1];
-    coef[nadj + 1] = diag;
-    FK_TRY(cudaMemcpyAsync(e->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, e->stream),
-           "upload coefficients");
-    // FK_OPT_FUSE_D: 1 always fuse (when D's pattern is H's), 0 never, 2 (default) by precision:
-    // fusing saves two gathered vector reads per step, which pays when the step is memory-bound
-    // (FP32); the FP64-class systems are arithmetic-bound and run the two kernels faster apart.
-    const bool fuse_pref = e->opt_fuse_d == 2 ? e->prec == fk::kF32 : e->opt_fuse_d != 0;
+    // FK_OPT_FUSE_D: 1 always fuse (when D's pattern is H's), 0 never, 2 (default) by precision.
+    // Measured per reverse step on cubic L=64, S=256: FP32 fused 3.24 ms vs 3.52 apart (the fused
+    // kernel saves two gathered vector reads), FP64 29.2 vs 30.4 (the outer product is FP64-pipe
+    // bound either way), DS 11.7 vs 11.4 (float-float epilogue registers cost the adjoint more).
+    const bool fuse_pref = e->opt_fuse_d == 2 ? e->prec != fk::kDS : e->opt_fuse_d != 0;
     const bool fuse = fuse_pref && e->d_same_as_H;
     // buffers: alpha_m in A, alpha_{m+1} in Ap (moments left alpha_{M/2-1}, alpha_{M/2})
     const double* scales = e->d_coef.as<double>() + nadj;   // [2 c_{M-1}, diag]
@@ -826,46 +841,45 @@ int fetch_D(fk_engine* e, double* D) {
     return FK_OK;
 }
 
-}  // namespace
-
-// ===================================================================================
-// Jackson-damped expansion coefficients in FP64 on the device
-// (expansion_coefficients, reference src/fastkpm.cpp:41-78; jackson_kernel :13-20;
-//  fermi_density / fermi_energy :375-393)
-// ===================================================================================
-namespace {
-
-__device__ double dev_fermi(int kind, double x, double kT, double mu) {
-    const double a = (x - mu) / fabs(kT);
-    if (kT < 1e-15 || fabs(a) > 20) return kind == 0 ? (x < mu ? 1.0 : 0.0) : (x < mu ? (x - mu) : 0.0);
-    return kind == 0 ? 1.0 / (exp(a) + 1.0) : -kT * log(1.0 + exp(-a));
+// Post-processing of the last moments(M) on the device, enqueued behind it: moments from the
+// per-step sums, gamma = moment_transform(mu, Mq), {mu_F, energy, n_tot} for the filling and,
+// with want_coef, the fermi_energy expansion coefficients at mu_F (kT as given).
+int post_enqueue(fk_engine* e, int Mq, double kT, double filling, double delta, bool want_coef) {
+    const int M = e->pending_M;
+    if (M == 0) return e->fail(FK_ERR_STATE, "kpm post-processing needs moments(M) first");
+    if (Mq < M) return e->fail(FK_ERR_ARG, "kpm post-processing: Mq (%d) must be >= M (%d)", Mq, M);
+    if (!(filling > 0.0 && filling < 1.0)) return e->fail(FK_ERR_ARG, "kpm post-processing: filling must be in (0, 1)");
+    if (!(delta >= 0.0) || filling - delta <= 0.0 || filling + delta >= 1.0)
+        return e->fail(FK_ERR_ARG, "kpm post-processing: need 0 <= delta_filling < min(filling, 1 - filling)");
+    FK_TRY(e->d_post.ensure(sizeof(double) * (2 * (size_t)M + 2 * (size_t)Mq + 4)), "alloc post-processing");
+    double* mu = e->d_post.as<double>();
+    double* gamma = mu + M;
+    double* en = gamma + Mq;
+    double* res = en + Mq;
+    double* c = res + 4;
+    const double avg = (e->es_hi + e->es_lo) / 2.0, mag = (e->es_hi - e->es_lo) / 2.0;
+    ProfScope ps(e, fk::kHelper);
+    fk::k_moments_from_raw<<<(M + 255) / 256, 256, 0, e->stream>>>(e->d_raw.as<double>(), M, mu);
+    fk::k_moment_transform<<<(Mq + 255) / 256, 256, 0, e->stream>>>(mu, M, Mq, avg, mag, gamma, en);
+    fk::k_filling_solve<<<1, fk::kPostThreads, 0, e->stream>>>(gamma, en, Mq, e->es_lo, e->es_hi, kT, filling, delta, res);
+    if (want_coef)
+        fk::k_expansion_coefficients<<<M, fk::kPostThreads, 0, e->stream>>>(M, Mq, 1, kT, 0.0, res, avg, mag, c);
+    FK_TRY(cudaGetLastError(), "post-processing launch");
+    e->post_M = M;
+    e->post_Mq = Mq;
+    return FK_OK;
 }
 
-// One CTA per order m: c_m = (m == 0 ? 1 : 2) g_m (1/Mq) sum_i f(E_i) T_m(x_i), x_i = cos(pi (i + 1/2) / Mq),
-// T_m(x_i) = cos(m pi (i + 1/2) / Mq); the node sum is reduced in a fixed order.
-__global__ void k_expansion_coefficients(int M, int Mq, int kind, double kT, double mu, double avg, double mag,
-                                         double* out) {
-    const int m = blockIdx.x;
-    if (m >= M) return;
-    const double pi = 3.141592653589793238463;
-    double acc = 0.0;
-    for (int i = threadIdx.x; i < Mq; i += blockDim.x) {
-        const double th = pi * (i + 0.5) / Mq;
-        const double f = dev_fermi(kind, cos(th) * mag + avg, kT, mu);
-        acc += f * cos(m * th);
-    }
-    __shared__ double red[256];
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const double Mp = M + 1.0;
-        const double g = ((Mp - m) * cos(pi * m / Mp) + sin(pi * m / Mp) / tan(pi / Mp)) / Mp;
-        out[m] = (m == 0 ? 1.0 : 2.0) * g * red[0] / Mq;
-    }
+// result[0..3) = {mu_F, energy, n_tot}; gamma (optional) = Mq doubles
+int post_fetch(fk_engine* e, double* result, double* gamma) {
+    const double* res = e->d_post.as<double>() + e->post_M + 2 * (size_t)e->post_Mq;
+    FK_TRY(cudaMemcpyAsync(result, res, sizeof(double) * 3, cudaMemcpyDeviceToHost, e->stream), "copy results");
+    if (gamma)
+        FK_TRY(cudaMemcpyAsync(gamma, e->d_post.as<double>() + e->post_M, sizeof(double) * e->post_Mq,
+                               cudaMemcpyDeviceToHost, e->stream),
+               "copy gamma");
+    FK_TRY(cudaStreamSynchronize(e->stream), "post-processing");
+    return FK_OK;
 }
 
 }  // namespace
@@ -875,10 +889,28 @@ __global__ void k_expansion_coefficients(int M, int Mq, int kind, double kT, dou
 // ===================================================================================
 namespace {
 
-// w <- w - alpha v1 - beta v0 (real or complex doubles), partial |w|^2 per CTA
-__global__ void k_lanczos_update(double* w, const double* v1, const double* v0, long long n_dbl, const double* ab,
-                                 double* part) {
-    const double al = ab[0], be = ab[1];
+// alpha_j = sum of the step kernel's per-CTA Re<Hv, v> partials (odd entries), in CTA order
+__global__ void k_lanczos_alpha(const double* step_part, int ctas, double* alpha) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a = 0.0;
+    for (int q = 0; q < ctas; q++) a += step_part[2 * q + 1];
+    *alpha = a;
+}
+
+// beta_j = sqrt(sum of |w|^2 partials) in CTA order, and 1/beta_j (0 once the Krylov space is exhausted)
+__global__ void k_lanczos_beta(const double* part, int n, double* beta, double* inv_beta) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    for (int q = 0; q < n; q++) s += part[q];
+    const double b = sqrt(s);
+    *beta = b;
+    *inv_beta = b > 0.0 ? 1.0 / b : 0.0;
+}
+
+// w <- w - alpha_j v1 - beta_{j-1} v0 (real or complex doubles), partial |w|^2 per CTA
+__global__ void k_lanczos_update(double* w, const double* v1, const double* v0, long long n_dbl, const double* alpha,
+                                 const double* beta, double* part) {
+    const double al = *alpha, be = *beta;
     double acc = 0.0;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_dbl; q += (long long)gridDim.x * blockDim.x) {
         const double v = w[q] - al * v1[q] - be * v0[q];
@@ -1009,7 +1041,7 @@ int fk_engine_destroy(fk_engine* e) {
     drop_graphs(e);
     DevBuf* bufs[] = {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2], &e->d_V[3],
                       &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc, &e->d_partials, &e->d_raw,
-                      &e->d_coef, &e->d_stage, &e->d_t_uoff, &e->d_t_ucol, &e->d_t_own, &e->d_t_kslot,
+                      &e->d_coef, &e->d_stage, &e->d_post, &e->d_t_uoff, &e->d_t_ucol, &e->d_t_own, &e->d_t_kslot,
                       &e->d_t_base, &e->d_err};
     for (auto* b : bufs) b->release();
     for (auto& c : e->cfg) { c.sys.release(); c.cta_sys.release(); }
@@ -1225,6 +1257,33 @@ int fk_engine_fetch_D(fk_engine* e, double* D) {
     return fetch_D(e, D);
 }
 
+int fk_engine_kpm_filling(fk_engine* e, int Mq, double kT, double filling, double delta_filling, double* result,
+                          double* gamma) {
+    if (!e || !result) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    int rc = post_enqueue(e, Mq, kT, filling, delta_filling, false);
+    if (rc != FK_OK) return rc;
+    return post_fetch(e, result, gamma);
+}
+
+int fk_engine_solve_filling(fk_engine* e, int M, int Mq, double kT, double filling, double delta_filling, int d_n_b,
+                            int d_nnzb, const int* d_row_ptr, const int* d_col_idx, double* D, double* result,
+                            double* gamma) {
+    if (!e || !D || !result || !d_row_ptr || (d_nnzb > 0 && !d_col_idx)) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    if (Mq < M) return e->fail(FK_ERR_ARG, "solve_filling: Mq (%d) must be >= M (%d)", Mq, M);
+    int rc = moments_enqueue(e, M);
+    if (rc != FK_OK) return rc;
+    rc = post_enqueue(e, Mq, kT, filling, delta_filling, true);
+    if (rc != FK_OK) return rc;
+    const double* c_dev = e->d_post.as<double>() + 2 * (size_t)M + 2 * (size_t)Mq + 4;
+    rc = autodiff_enqueue(e, M, nullptr, d_n_b, d_nnzb, d_row_ptr, d_col_idx, c_dev);
+    if (rc != FK_OK) return rc;
+    rc = fetch_D(e, D);
+    if (rc != FK_OK) return rc;
+    return post_fetch(e, result, gamma);
+}
+
 int fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
                            const double* val, double extend, int iters, const double* v0, double* lo, double* hi) {
     if (!e || !lo || !hi) return FK_ERR_ARG;
@@ -1259,47 +1318,53 @@ int fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* ro
     FK_TRY(cudaMemcpyAsync(t->d_V[0].p, t->d_R.p, vb, cudaMemcpyDeviceToDevice, t->stream), "lanczos init");
     FK_TRY(cudaMemsetAsync(t->d_V[1].p, 0, vb, t->stream), "lanczos init");
     const long long n_dbl = (long long)vb / sizeof(double);
-    DevBuf ab, part;
+    // The whole recursion stays on the device: the scalars alpha_j, beta_j, 1/beta_j are
+    // reduced into device arrays that the next launches read, so the host waits once, at the
+    // end, and then solves the iters x iters tridiagonal problem.
+    DevBuf scal, spart, upart;
     const int ugrid = 152 * 4;
-    FK_TRY(ab.ensure(2 * sizeof(double)), "lanczos scalars");
-    FK_TRY(part.ensure(sizeof(double) * std::max(ugrid, 2 * t->cfg[fk::kStep].ctas * t->cfg[fk::kStep].slices)), "lanczos partials");
-    std::vector<double> alpha(iters), beta(iters), hp(std::max(ugrid, 2 * t->cfg[fk::kStep].ctas * t->cfg[fk::kStep].slices));
-    beta[0] = 0;
+    const int ctas = t->cfg[fk::kStep].ctas;   // one column slice
+    FK_TRY(scal.ensure(sizeof(double) * 3 * (size_t)(iters + 1)), "lanczos scalars");
+    FK_TRY(spart.ensure(sizeof(double) * 2 * (size_t)ctas), "lanczos partials");
+    FK_TRY(upart.ensure(sizeof(double) * ugrid), "lanczos partials");
+    double* d_alpha = scal.as<double>();
+    double* d_beta = d_alpha + (iters + 1);
+    double* d_inv = d_beta + (iters + 1);
+    FK_TRY(cudaMemsetAsync(scal.p, 0, scal.bytes, t->stream), "lanczos init");
     int v1 = 0, vz = 1, w = 2;
-    const int pcount = 2 * t->cfg[fk::kStep].ctas * t->cfg[fk::kStep].slices;
     for (int j = 1; j <= iters; j++) {
-        // w = H v1 with the step kernel (alpha = <w, v1> from its dots)
-        rc = run_step(t, t->V(v1), nullptr, t->V(w), false, true, 0, nullptr, nullptr, part.as<double>());
+        // w = H v1 with the step kernel; alpha_j = <w, v1> from its dots
+        rc = run_step(t, t->V(v1), nullptr, t->V(w), false, true, 0, nullptr, nullptr, spart.as<double>());
         if (rc != FK_OK) return e->fail(rc, "energy_scale: %s", t->err.c_str());
-        FK_TRY(cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * pcount, cudaMemcpyDeviceToHost, t->stream), "lanczos");
-        FK_TRY(cudaStreamSynchronize(t->stream), "lanczos");
-        double a = 0;
-        for (int q = 1; q < pcount; q += 2) a += hp[q];
-        alpha[j - 1] = a;
+        k_lanczos_alpha<<<1, 32, 0, t->stream>>>(spart.as<double>(), ctas, d_alpha + (j - 1));
+        FK_TRY(cudaGetLastError(), "lanczos alpha");
         if (j == iters) break;
-        const double abh[2] = {alpha[j - 1], beta[j - 1]};
-        FK_TRY(cudaMemcpyAsync(ab.p, abh, sizeof abh, cudaMemcpyHostToDevice, t->stream), "lanczos");
         k_lanczos_update<<<ugrid, 256, 0, t->stream>>>(t->d_V[w].as<double>(), t->d_V[v1].as<double>(),
-                                                       t->d_V[vz].as<double>(), n_dbl, ab.as<double>(), part.as<double>());
+                                                       t->d_V[vz].as<double>(), n_dbl, d_alpha + (j - 1), d_beta + (j - 1),
+                                                       upart.as<double>());
         FK_TRY(cudaGetLastError(), "lanczos update");
-        FK_TRY(cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * ugrid, cudaMemcpyDeviceToHost, t->stream), "lanczos");
-        FK_TRY(cudaStreamSynchronize(t->stream), "lanczos");
-        double ww = 0;
-        for (int q = 0; q < ugrid; q++) ww += hp[q];
-        beta[j] = std::sqrt(ww);
-        if (!(beta[j] > 0)) { iters = j; break; }   // invariant subspace found
-        // v0 <- v1, v1 <- w / beta
-        FK_TRY(fk::launch_scale_f64(e->cplx, t->V(w), t->V(vz), (long long)t->n * t->ld, 1.0 / beta[j], nullptr, t->stream),
+        k_lanczos_beta<<<1, 32, 0, t->stream>>>(upart.as<double>(), ugrid, d_beta + j, d_inv + j);
+        FK_TRY(cudaGetLastError(), "lanczos beta");
+        // v0 <- v1, v1 <- w / beta_j (w / 0 -> 0 once the Krylov space is exhausted)
+        FK_TRY(fk::launch_scale_f64(e->cplx, t->V(w), t->V(vz), (long long)t->n * t->ld, 0.0, d_inv + j, t->stream),
                "lanczos scale");
         std::swap(v1, vz);   // new v1 = scaled w (in old vz), new v0 = old v1
     }
+    std::vector<double> alpha(iters + 1), beta(iters + 1);
+    FK_TRY(cudaMemcpyAsync(alpha.data(), d_alpha, sizeof(double) * (iters + 1), cudaMemcpyDeviceToHost, t->stream),
+           "lanczos");
+    FK_TRY(cudaMemcpyAsync(beta.data(), d_beta, sizeof(double) * (iters + 1), cudaMemcpyDeviceToHost, t->stream), "lanczos");
+    FK_TRY(cudaStreamSynchronize(t->stream), "lanczos");
+    for (int j = 1; j < iters; j++)
+        if (!(beta[j] > 0)) { iters = j; break; }   // invariant subspace found at step j
     double emin, emax;
     tridiag_extremes(iters, alpha.data(), beta.data(), &emin, &emax);
     const double slack = extend * (emax - emin);
     *lo = emin - slack;
     *hi = emax + slack;
-    ab.release();
-    part.release();
+    scal.release();
+    spart.release();
+    upart.release();
     return FK_OK;
 }
 
@@ -1311,7 +1376,7 @@ int fk_engine_expansion_coefficients(fk_engine* e, int M, int Mq, int f_kind, do
     cudaSetDevice(e->device);
     DevBuf d;
     FK_TRY(d.ensure(sizeof(double) * M), "alloc coefficients");
-    k_expansion_coefficients<<<M, 256, 0, e->stream>>>(M, Mq, f_kind, kT, mu, (es_hi + es_lo) / 2.0,
+    fk::k_expansion_coefficients<<<M, fk::kPostThreads, 0, e->stream>>>(M, Mq, f_kind, kT, mu, nullptr, (es_hi + es_lo) / 2.0,
                                                        (es_hi - es_lo) / 2.0, d.as<double>());
     cudaError_t ce = cudaGetLastError();
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(out, d.p, sizeof(double) * M, cudaMemcpyDeviceToHost, e->stream);

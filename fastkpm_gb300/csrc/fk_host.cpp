@@ -213,19 +213,28 @@ double mu_to_filling(Vec<double> const& gamma, EnergyScale const& es, double kT,
     const double tot = density_product(gamma, [](double) { return 1.0; }, es);
     return occ / tot;
 }
-// Chemical potential for a filling: bracketed bisection on the monotone
-// mu_to_filling (the reference uses Boost's toms748 on the same bracket
-// [es.lo, es.hi], stopping when the bracket filling is within delta_filling).
+// Chemical potential for a filling (src/fastkpm.cpp:413-427): thermal smearing
+// kT' = max(kT, 0.1 mag / Mq), bracket [lo - max(c, 0), hi + max(-c, 0)] with
+// c = kT' log(1/filling - 1), root of mu_to_filling(gamma, es, kT', mu) = filling
+// (two roots at filling +- delta_filling, averaged, when delta_filling != 0). The
+// reference solves with Boost's toms748 to 30 bits; this bisects to 1e-14, so the
+// two agree to the reference's tolerance.
 double filling_to_mu(Vec<double> const& gamma, EnergyScale const& es, double kT, double filling, double delta_filling) {
-    double lo = es.lo, hi = es.hi;
-    for (int it = 0; it < 200; it++) {
-        const double mid = 0.5 * (lo + hi);
-        const double f = mu_to_filling(gamma, es, kT, mid);
-        if (std::fabs(f - filling) <= delta_filling && hi - lo < 1e-12 * std::max(1.0, std::fabs(mid))) return mid;
-        if (f < filling) lo = mid; else hi = mid;
-        if (hi - lo <= 1e-14 * std::max(1.0, std::fabs(mid))) break;
-    }
-    return 0.5 * (lo + hi);
+    const double kTs = std::max(kT, 0.1 * es.mag() / (double)gamma.size());
+    const double c = kTs * std::log(1.0 / filling - 1.0);
+    const double a0 = es.lo - std::max(c, 0.0), b0 = es.hi + std::max(-c, 0.0);
+    auto root = [&](double target) {
+        double a = a0, b = b0;
+        for (int it = 0; it < 200; it++) {
+            const double mid = 0.5 * (a + b);
+            if (mu_to_filling(gamma, es, kTs, mid) - target < 0) a = mid;
+            else b = mid;
+            if (b - a <= 1e-14 * std::max(1.0, std::fabs(mid))) break;
+        }
+        return 0.5 * (a + b);
+    };
+    if (delta_filling == 0) return root(filling);
+    return 0.5 * (root(filling + delta_filling) + root(filling - delta_filling));
 }
 double electronic_grand_energy(Vec<double> const& gamma, EnergyScale const& es, double kT, double mu) {
     return density_product(gamma, [&](double x) { return fermi_energy(x, kT, mu); }, es);

@@ -264,7 +264,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step(StepArgs a) {
             for (int bi = 0; bi < B; bi++)
 #pragma unroll
                 for (int e = 0; e < EPT; e++) acc[bi][e] = S::zero();
-#pragma unroll 1   // measured: unrolling the block loop adds registers and no gather parallelism
+            // Not unrolled: every unroll factor measured slower (more registers, fewer warps),
+            // for light (b=1, S=32 FP32) and heavy (b=2, S=256 complex) threads alike.
+#pragma unroll 1
             for (int k = kb; k < ke; k++) {
                 const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
                 const H* hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
@@ -339,10 +341,27 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step(StepArgs a) {
 // sums of values [first, first + count), and `writer` marks the one lane (of those
 // holding the same values) that stores them. The lane that stores a value depends
 // only on g, so successive chunks update each D entry from the same thread.
-template <class S, int V>
-__device__ __forceinline__ void group_sum_transposed(typename S::OAcc (&v)[V], int Gp, int g, int& first, int& count,
-                                                     bool& writer) {
+struct Owner {
+    int first, count;   // values [first, first + count) of the V end up in this lane
+    bool writer;        // the lane that stores them
+};
+template <int V>
+__device__ __forceinline__ Owner transposed_owner(int Gp, int g) {
     int off = Gp >> 1, sel = 0, cur = V;
+#pragma unroll
+    for (int h = V >> 1; h >= 1; h >>= 1) {
+        if (off > 0) {
+            sel = (sel << 1) | ((g & off) != 0 ? 1 : 0);
+            cur = h;
+            off >>= 1;
+        }
+    }
+    const int span = Gp / (V / cur);   // lanes holding the same values
+    return Owner{sel * cur, cur, (g & (span - 1)) == 0};
+}
+template <class S, int V>
+__device__ __forceinline__ void group_sum_transposed(typename S::OAcc (&v)[V], int Gp, int g) {
+    int off = Gp >> 1, cur = V;
 #pragma unroll
     for (int h = V >> 1; h >= 1; h >>= 1) {
         if (off > 0) {
@@ -353,7 +372,6 @@ __device__ __forceinline__ void group_sum_transposed(typename S::OAcc (&v)[V], i
                 const typename S::OAcc keep = up ? v[i + h] : v[i];
                 v[i] = S::oa_add(keep, S::oa_shfl(send, off));
             }
-            sel = (sel << 1) | (up ? 1 : 0);
             cur = h;
             off >>= 1;
         }
@@ -363,39 +381,55 @@ __device__ __forceinline__ void group_sum_transposed(typename S::OAcc (&v)[V], i
         for (int i = 0; i < V; i++)
             if (i < cur) v[i] = S::oa_add(v[i], S::oa_shfl(v[i], off));
     }
-    count = cur;
-    first = sel * cur;
-    const int span = Gp / (V / cur);   // lanes holding the same values
-    writer = (g & (span - 1)) == 0;
 }
 
-// Reduce a block's per-lane D partials over the row group and add them to Dacc[k].
-// FP64 systems accumulate in double; FP32 and DS systems keep the accumulator as
-// float-float pairs (same 8 bytes per real) on the FP32 pipe and convert it to
-// double once at the end (k_ds_to_double).
+// Early read of the first D entry a writer lane updates for block k (8 bytes per real:
+// a double, or a float-float pair for FP32/DS systems), issued before the block's
+// gathers so that the read-modify-write does not wait a memory round trip at the end.
+template <class S, int B>
+__device__ __forceinline__ double2 d_prefetch(const double* Dacc, size_t k, const Owner& o, bool on) {
+    double2 v = make_double2(0.0, 0.0);
+    if (on) {
+        const size_t q = (k * B * B + o.first) * (S::CPLX ? 2 : 1);
+        if (S::CPLX) v = *reinterpret_cast<const double2*>(Dacc + q);
+        else v.x = Dacc[q];
+    }
+    return v;
+}
+__device__ __forceinline__ float2 bits_float2(double d) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    return make_float2(__int_as_float((int)(unsigned)(u & 0xffffffffull)), __int_as_float((int)(unsigned)(u >> 32)));
+}
+
+// Reduce a block's per-lane D partials over the row group and add them to Dacc[k];
+// `pre` is the d_prefetch of the lane's first entry. FP64 systems accumulate in
+// double; FP32 and DS systems keep the accumulator as float-float pairs (same 8 bytes
+// per real) on the FP32 pipe and convert it to double once at the end (k_ds_to_double).
 template <class S, int B>
 __device__ __forceinline__ void flush_block(typename S::OAcc (&of)[B * B], int Gp, int g, bool has, size_t k,
-                                            double scale, float2 scale_ds, double* Dacc) {
-    int first, count;
-    bool writer;
-    group_sum_transposed<S, B * B>(of, Gp, g, first, count, writer);
-    if (has && writer) {
+                                            double scale, float2 scale_ds, double* Dacc, const Owner& o, double2 pre) {
+    group_sum_transposed<S, B * B>(of, Gp, g);
+    if (has && o.writer) {
 #pragma unroll
         for (int t = 0; t < B * B; t++) {
-            if (t < count) {
-                const size_t q = (k * B * B + first + t) * (S::CPLX ? 2 : 1);
+            if (t < o.count) {
+                const size_t q = (k * B * B + o.first + t) * (S::CPLX ? 2 : 1);
                 if constexpr (S::DACC_DS) {
                     float2* D2 = reinterpret_cast<float2*>(Dacc);
 #pragma unroll
                     for (int comp = 0; comp < (S::CPLX ? 2 : 1); comp++) {
-                        float2 cur = D2[q + comp];
+                        float2 cur = t == 0 ? bits_float2(comp ? pre.y : pre.x) : D2[q + comp];
                         ds_mac(cur, scale_ds, S::oa_ds(of[t], comp));
                         D2[q + comp] = ds_norm(cur);
                     }
                 } else {
                     const double2 v = S::oa_get(of[t]);
-                    Dacc[q] += scale * v.x;
-                    if (S::CPLX) Dacc[q + 1] += scale * v.y;
+                    const double re = t == 0 ? pre.x : Dacc[q];
+                    Dacc[q] = re + scale * v.x;
+                    if (S::CPLX) {
+                        const double im = t == 0 ? pre.y : Dacc[q + 1];
+                        Dacc[q + 1] = im + scale * v.y;
+                    }
                 }
             }
         }
@@ -443,6 +477,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_step(AdjArgs a) {
     const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
     const bool fuse = a.Dacc != nullptr;
     const float2 dscale_ds = ds_from_double(a.dscale);
+    const Owner own = transposed_owner<B * B>(Gp, (int)(threadIdx.x % Gp));   // Gp divides kThreads
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
         const Tile tl = tile_range(a.row_ptr, sd, t0, items, Gp, a.stage_cap);
@@ -494,6 +529,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_step(AdjArgs a) {
                     hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
                 }
                 const int j = (int)(cc & kColMask);
+                const double2 dpre = d_prefetch<S, B>(a.Dacc, (size_t)k, own, fuse && has && own.writer);
                 typename S::OAcc of[B * B];
 #pragma unroll
                 for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
@@ -516,7 +552,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_step(AdjArgs a) {
                             for (int e = 0; e < EPT; e++) S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
                     }
                 }
-                if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, dscale_ds, a.Dacc);
+                if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, dscale_ds, a.Dacc, own, dpre);
             }
             if (active) {
 #pragma unroll
@@ -565,6 +601,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
     const E* Bv = reinterpret_cast<const E*>(a.Bv);
     const bool two_terms = a.two_terms != 0;
     const float2 alpha_ds = ds_from_double(a.alpha);
+    const Owner own = transposed_owner<B * B>(Gp, (int)(threadIdx.x % Gp));   // Gp divides kThreads
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
         const long long t = t0 + threadIdx.x;
@@ -594,10 +631,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
                     for (int e = 0; e < EPT; e++) { Ai[bi][e] = S::to(S::zero()); Bi[bi][e] = Ai[bi][e]; }
                 }
             }
+            unsigned cc_next = ke > kb ? __ldg(a.colc + kb) : 0u;   // column index one block ahead
             for (int kk = 0; kk < nmax; kk++) {
                 const int k = kb + kk;
                 const bool has = kk < ke - kb;
-                const int j = has ? (int)(__ldg(a.colc + k) & kColMask) : 0;
+                const int j = has ? (int)(cc_next & kColMask) : 0;
+                cc_next = kk + 1 < ke - kb ? __ldg(a.colc + k + 1) : 0u;
+                const double2 dpre = d_prefetch<S, B>(a.Dacc, (size_t)k, own, has && own.writer);
                 typename S::OAcc of[B * B];
 #pragma unroll
                 for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
@@ -623,7 +663,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
                             if (two_terms) S::oa_mac(of[bj * B + bi], Bi[bi][e], av[e]);
                         }
                 }
-                flush_block<S, B>(of, Gp, g, has, (size_t)k, a.alpha, alpha_ds, a.Dacc);
+                flush_block<S, B>(of, Gp, g, has, (size_t)k, a.alpha, alpha_ds, a.Dacc, own, dpre);
             }
         }
     }

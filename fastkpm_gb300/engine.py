@@ -405,6 +405,29 @@ class Engine:
                     "expansion_coefficients")
         return out
 
+    def kpm_filling(self, Mq, kT, filling, delta_filling=0.0):
+        """Post-process the last moments(M) on the device: returns (mu_F, energy, n_tot, gamma) with
+        gamma = moment_transform(mu, Mq), mu_F = filling_to_mu(gamma, es, kT, filling, delta_filling),
+        energy = electronic_energy(gamma, es, kT, filling, mu_F) (src/fastkpm.cpp:236-476)."""
+        res = np.zeros(3)
+        gamma = np.zeros(Mq)
+        self._check(self.lib.fk_engine_kpm_filling(self.h, Mq, kT, filling, delta_filling, _dp(res), _dp(gamma)),
+                    "kpm_filling")
+        return res[0], res[1], res[2], gamma
+
+    def solve_filling(self, M, Mq, kT, filling, D, delta_filling=0.0):
+        """moments(M) -> mu_F, energy at the filling -> fermi_energy coefficients at mu_F ->
+        autodiff_matrix(c, D), every stage on the device. Fills D.val; returns (mu_F, energy, gamma)."""
+        res = np.zeros(3)
+        gamma = np.zeros(Mq)
+        dt = np.complex128 if self.complex_values else np.float64
+        out = np.zeros(D.n_blocks() * D.b_len ** 2, dt)
+        self._check(self.lib.fk_engine_solve_filling(self.h, M, Mq, kT, filling, delta_filling, D.n_rows, D.n_blocks(),
+                                                     _ip(D.row_ptr), _ip(D.col_idx), _dp(out.view(np.float64)),
+                                                     _dp(res), _dp(gamma)), "solve_filling")
+        D.val = out
+        return res[0], res[1], gamma
+
     def moments2_v1(self, *a, **k):
         raise NotImplementedError("moments2_v1 (conductivity) is not part of the GB300 build")
 

@@ -70,7 +70,7 @@ const char* fk_engine_last_error(const fk_engine* e);
 int  fk_engine_set_stream(fk_engine* e, void* cuda_stream);
 int  fk_engine_synchronize(fk_engine* e);
 /* Engine options: FK_OPT_* below. */
-#define FK_OPT_FUSE_D      0   /* fuse the outer product into the adjoint step when D's pattern is H's: 1 always, 0 never, 2 (default) for FP32 only */
+#define FK_OPT_FUSE_D      0   /* fuse the outer product into the adjoint step when D's pattern is H's: 1 always, 0 never, 2 (default): FP32, FP64 */
 #define FK_OPT_NP          1   /* packets per lane: 0 auto, or 1, 2, 4                                           */
 #define FK_OPT_CTAS_PER_SM 2   /* 0 auto (occupancy), else a cap on CTAs per SM                                   */
 #define FK_OPT_STAGE_H     3   /* 1: stage H blocks in shared memory, 0: never, 2 (default): not in the FP32 step */
@@ -136,6 +136,24 @@ int  fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* r
  * cos(m theta_i), node sums reduced in a fixed order. out[M] on the host. */
 int  fk_engine_expansion_coefficients(fk_engine* e, int M, int Mq, int f_kind, double kT, double mu,
                                       double es_lo, double es_hi, double* out);
+
+/* KPM post-processing of the last moments(M) on the device, with no host round trip after
+ * the moments: gamma = moment_transform(mu, Mq) (reference src/fastkpm.cpp:236-256), the
+ * chemical potential mu_F = filling_to_mu(gamma, es, kT, filling, delta_filling) (:413-427:
+ * thermal smearing kT' = max(kT, 0.1 mag / Mq), the same bracket, root by bisection where
+ * the reference uses toms748 to 30 bits, so the two agree to that tolerance), and
+ * E = electronic_energy(gamma, es, kT, filling, mu_F) (:463-467). result[3] = {mu_F, E, n_tot}
+ * with n_tot = density_product(gamma, 1) (:314-322); gamma[Mq] out when not NULL.
+ * Needs 0 < filling - delta_filling, filling + delta_filling < 1, Mq >= M. No reference C entry
+ * point: it replaces the caller's host calls between moments() and autodiff_matrix(). */
+int  fk_engine_kpm_filling(fk_engine* e, int Mq, double kT, double filling, double delta_filling,
+                           double* result, double* gamma);
+/* The fixed-filling solve of a Kondo-lattice caller in one call, every stage on the device:
+ * moments(M); mu_F, E as fk_engine_kpm_filling; c = expansion_coefficients(M, Mq,
+ * fermi_energy(., kT, mu_F), es); autodiff_matrix(c, D). D_val, result[3], gamma (optional). */
+int  fk_engine_solve_filling(fk_engine* e, int M, int Mq, double kT, double filling, double delta_filling,
+                             int d_n_b, int d_nnzb, const int* d_row_ptr, const int* d_col_idx,
+                             double* D_val, double* result, double* gamma);
 
 /* Profiling: when on, each kernel launch is bracketed by CUDA events on the engine's stream. */
 int  fk_engine_set_profiling(fk_engine* e, int on);

@@ -608,4 +608,62 @@ double orc_moment_product(int M, const double* c, const double* mu) {
     return r;
 }
 
+// moment_transform (src/fastkpm.cpp:236-256): Jackson-damped density on the Mq Chebyshev nodes
+void orc_moment_transform(int M, const double* mu, int Mq, double* gamma) {
+    std::vector<double> kernel(M), T(M), mup(M);
+    orc_jackson_kernel(M, kernel.data());
+    for (int m = 0; m < M; m++) mup[m] = mu[m] * kernel[m];
+    for (int i = 0; i < Mq; i++) {
+        gamma[i] = 0.0;
+        orc_chebyshev_fill_array(std::cos(kPi * (i + 0.5) / Mq), M, 1, T.data());
+        for (int m = 0; m < M; m++) gamma[i] += (m == 0 ? 1 : 2) * mup[m] * T[m];
+    }
+}
+
+// density_product (src/fastkpm.cpp:314-322) with f = 1 (kind -1), fermi_density (0), fermi_energy (1)
+static double density_product(int Mq, const double* gamma, int kind, double kT, double mu, double lo, double hi) {
+    const double avg = (hi + lo) / 2.0, mag = (hi - lo) / 2.0;
+    double r = 0.0;
+    for (int i = 0; i < Mq; i++) {
+        const double E = std::cos(kPi * (i + 0.5) / Mq) * mag + avg;
+        const double f = kind < 0 ? 1.0 : (kind == 0 ? orc_fermi_density(E, kT, mu) : orc_fermi_energy(E, kT, mu));
+        r += gamma[i] * f;
+    }
+    return r / Mq;
+}
+
+// mu_to_filling (src/fastkpm.cpp:395-400)
+double orc_mu_to_filling(int Mq, const double* gamma, double lo, double hi, double kT, double mu) {
+    return density_product(Mq, gamma, 0, kT, mu, lo, hi) / density_product(Mq, gamma, -1, kT, mu, lo, hi);
+}
+
+// filling_to_mu (src/fastkpm.cpp:413-427): smearing kT' = max(kT, 0.1 mag / Mq), bracket
+// [lo - max(c, 0), hi + max(-c, 0)] with c = kT' log(1/filling - 1); the reference's toms748
+// root (30-bit tolerance, src/fastkpm.cpp:405-411) is replaced by bisection to 1e-14, so the
+// two agree to the reference's tolerance; two roots at filling +- delta are averaged.
+double orc_filling_to_mu(int Mq, const double* gamma, double lo, double hi, double kT, double filling,
+                         double delta_filling) {
+    const double kTs = std::max(kT, 0.1 * ((hi - lo) / 2.0) / Mq);
+    const double c = kTs * std::log(1.0 / filling - 1.0);
+    const double a0 = lo - std::max(c, 0.0), b0 = hi + std::max(-c, 0.0);
+    auto root = [&](double target) {
+        double a = a0, b = b0;
+        for (int it = 0; it < 200; it++) {
+            const double mid = 0.5 * (a + b);
+            if (orc_mu_to_filling(Mq, gamma, lo, hi, kTs, mid) - target < 0) a = mid;
+            else b = mid;
+            if (b - a <= 1e-14 * std::max(1.0, std::fabs(mid))) break;
+        }
+        return 0.5 * (a + b);
+    };
+    if (delta_filling == 0) return root(filling);
+    return 0.5 * (root(filling + delta_filling) + root(filling - delta_filling));
+}
+
+// electronic_energy (src/fastkpm.cpp:463-467) = electronic_grand_energy (:448-451) + mu n_occ
+double orc_electronic_energy(int Mq, const double* gamma, double lo, double hi, double kT, double filling, double mu) {
+    const double n_tot = density_product(Mq, gamma, -1, kT, mu, lo, hi);
+    return density_product(Mq, gamma, 1, kT, mu, lo, hi) + mu * filling * n_tot;
+}
+
 }  // extern "C"

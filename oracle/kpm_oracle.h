@@ -80,6 +80,14 @@ double orc_fermi_energy(double x, double kT, double mu);
 void   orc_expansion_coefficients(int M, int Mq, int kind, double kT, double mu,
                                   double es_lo, double es_hi, double* out);
 double orc_moment_product(int M, const double* c, const double* mu);
+/* moment_transform, mu_to_filling, filling_to_mu, electronic_energy (src/fastkpm.cpp:236-256,
+ * :395-400, :413-427, :463-467); es = [lo, hi] */
+void   orc_moment_transform(int M, const double* mu, int Mq, double* gamma);
+double orc_mu_to_filling(int Mq, const double* gamma, double lo, double hi, double kT, double mu);
+double orc_filling_to_mu(int Mq, const double* gamma, double lo, double hi, double kT, double filling,
+                         double delta_filling);
+double orc_electronic_energy(int Mq, const double* gamma, double lo, double hi, double kT, double filling,
+                             double mu);
 
 #ifdef __cplusplus
 }

@@ -41,6 +41,10 @@ _SIG = {
     "orc_fermi_energy": (_d, [_d, _d, _d]),
     "orc_expansion_coefficients": (None, [_i, _i, _i, _d, _d, _d, _d, _dp]),
     "orc_moment_product": (_d, [_i, _dp, _dp]),
+    "orc_moment_transform": (None, [_i, _dp, _i, _dp]),
+    "orc_mu_to_filling": (_d, [_i, _dp, _d, _d, _d, _d]),
+    "orc_filling_to_mu": (_d, [_i, _dp, _d, _d, _d, _d, _d]),
+    "orc_electronic_energy": (_d, [_i, _dp, _d, _d, _d, _d, _d]),
 }
 
 _lib = None
@@ -198,3 +202,25 @@ def tridiag_extremes(alpha, beta):
     lo, hi = C.c_double(), C.c_double()
     lib().orc_tridiag_extremes(len(a), _dp_(a), _dp_(b), C.byref(lo), C.byref(hi))
     return lo.value, hi.value
+
+
+def moment_transform(mu, Mq):
+    mu = np.ascontiguousarray(mu, np.float64)
+    gamma = np.zeros(Mq)
+    lib().orc_moment_transform(len(mu), _dp_(mu), Mq, _dp_(gamma))
+    return gamma
+
+
+def mu_to_filling(gamma, lo, hi, kT, mu):
+    g = np.ascontiguousarray(gamma, np.float64)
+    return lib().orc_mu_to_filling(len(g), _dp_(g), lo, hi, kT, mu)
+
+
+def filling_to_mu(gamma, lo, hi, kT, filling, delta_filling=0.0):
+    g = np.ascontiguousarray(gamma, np.float64)
+    return lib().orc_filling_to_mu(len(g), _dp_(g), lo, hi, kT, filling, delta_filling)
+
+
+def electronic_energy(gamma, lo, hi, kT, filling, mu):
+    g = np.ascontiguousarray(gamma, np.float64)
+    return lib().orc_electronic_energy(len(g), _dp_(g), lo, hi, kT, filling, mu)

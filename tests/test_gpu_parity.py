@@ -302,6 +302,13 @@ def test_energy_scale_lanczos(gpu):
     assert abs(es2.lo - lo) < 1e-9 and abs(es2.hi - hi) < 1e-9
     es3 = eng.energy_scale(H, 0.01)   # seeded start vector
     assert es3.lo <= lam.min() + 1e-6 and es3.hi >= lam.max() - 1e-6
+    # a start vector that is an eigenvector ends the recursion at beta_1 = 0 (exactly)
+    d = np.arange(1.0, 9.0)
+    Hd = fk.SpMatBsr.build(8, 1, np.arange(8), np.arange(8), d[:, None])
+    e0 = np.zeros(8)
+    e0[2] = 1.0
+    es4 = eng.energy_scale(Hd, 0.0, 6, v0=e0)
+    assert es4.lo == 3.0 and es4.hi == 3.0
 
 
 def test_complex_energy_scale(gpu):

@@ -217,3 +217,53 @@ def test_bsr_build_sorts_and_merges():
     assert np.all(np.diff(r) >= 0)
     for i in range(n):
         assert np.all(np.diff(c[rp[i]:rp[i + 1]]) > 0)
+
+
+def _exact_moments(lam, M):
+    """mu_m = sum_k T_m(lam_k): the moments of identity probes on a matrix with spectrum lam."""
+    return np.array([cheb_T(m, lam).sum() for m in range(M)])
+
+
+def test_moment_transform_total_weight_is_mu0():
+    # sum_i gamma_i / Mq = g_0 mu_0 = mu_0: the nodes' sum of T_m vanishes for 0 < m < 2 Mq
+    rng = np.random.default_rng(0)
+    lam = rng.uniform(-0.9, 0.9, 200)
+    mu = _exact_moments(lam, 100)
+    gamma = O.moment_transform(mu, 300)
+    assert abs(gamma.sum() / 300 - 200) < 1e-10
+    assert O.jackson_kernel(100)[0] == pytest.approx(1.0, abs=1e-15)
+
+
+def test_filling_of_particle_hole_symmetric_spectrum():
+    # a bipartite lattice has a symmetric spectrum: half filling puts mu at the band centre,
+    # and the smeared filling of the returned mu is the requested one
+    H, _ = W.square_lattice(16, -1.0, 0.0, seed=0)
+    lam = np.linalg.eigvalsh(H.to_dense())
+    es = EnergyScale(-4.5, 4.5)
+    mu = _exact_moments(lam / es.mag(), 200)
+    gamma = O.moment_transform(mu, 400)
+    mu_f = O.filling_to_mu(gamma, es.lo, es.hi, 0.0, 0.5)
+    assert abs(mu_f) < 1e-10
+    kTs = 0.1 * es.mag() / 400
+    for f in (0.2, 0.37, 0.8):
+        m = O.filling_to_mu(gamma, es.lo, es.hi, 0.0, f)
+        assert O.mu_to_filling(gamma, es.lo, es.hi, kTs, m) == pytest.approx(f, abs=1e-12)
+    # delta_filling averages the roots at f +- delta
+    a = O.filling_to_mu(gamma, es.lo, es.hi, 0.0, 0.3, 0.01)
+    b = 0.5 * (O.filling_to_mu(gamma, es.lo, es.hi, 0.0, 0.31) + O.filling_to_mu(gamma, es.lo, es.hi, 0.0, 0.29))
+    assert a == pytest.approx(b, abs=1e-13)
+
+
+def test_electronic_energy_approaches_sum_of_occupied_levels():
+    # at kT = 0 the KPM energy tends to the sum of the lowest filling*N eigenvalues as M grows
+    rng = np.random.default_rng(1)
+    H, _ = W.square_lattice(16, -1.0, 1.0, seed=2)
+    lam = np.linalg.eigvalsh(H.to_dense())
+    es = EnergyScale(-5.0, 5.0)
+    exact = np.sort(lam)[:128].sum()
+    errs = []
+    for M in (100, 400):
+        gamma = O.moment_transform(_exact_moments(lam / es.mag(), M), 2 * M)
+        mu_f = O.filling_to_mu(gamma, es.lo, es.hi, 0.0, 0.5)
+        errs.append(abs(O.electronic_energy(gamma, es.lo, es.hi, 0.0, 0.5, mu_f) - exact) / abs(exact))
+    assert errs[1] < 5e-3 and errs[1] < errs[0]
