@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-M", type=int, default=8)
-    p.add_argument("--workload", default="solve", choices=["solve", "precision", "batch", "serve", "cfg1"])
+    p.add_argument("--workload", default="solve", choices=["solve", "precision", "batch", "serve", "cfg1", "square"])
     p.add_argument("--serve-requests", type=int, default=24)
     p.add_argument("--serve-max-sites", type=float, default=1e6)
     return p.parse_args()
@@ -555,6 +555,60 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_square(args):
+    """One large square lattice (L = --L, default 1448: 2.1 M sites), b=1 real, S = --S (default 32)
+    +-1 probes, moments(M) in --precision (default fp32): the narrow-row step kernel of the batched
+    workload at a size above L2, with its roofline; error vs the FP64 engine on the first 40 moments."""
+    import fastkpm_gb300 as fk
+    from fastkpm_gb300 import _lib as Lb
+    from fastkpm_gb300 import workloads as W
+    L = args.L if args.L != 64 else 1448
+    S = args.S if args.S != 256 else 32
+    prec = args.precision if args.precision != "ds" else "fp32"
+    M = args.M
+    H, es = W.square_lattice(L, -1.0, 1.0, 7)
+    R = fk.probe_uncorrelated(H.n_rows, S, fk.RNG(7))
+    eng = fk.Engine(False, prec)
+    eng.set_H(H, es)
+    eng.set_R(R)
+    eng.set_option(Lb.FK_OPT_GRAPHS, 1)
+    for _ in range(max(args.warmup, 1)):
+        mu = eng.moments(M)
+    eng.set_profiling(1)
+    eng.profile_reset()
+    eng.moments(M)
+    n_step, t_step = eng.profile(0)
+    eng.set_profiling(0)
+    with ClockSampler(0) as clk:
+        eng.timer_start()
+        for _ in range(args.steps):
+            eng.moments_async(M)
+        ms = eng.timer_stop() / args.steps
+    mu = eng.fetch_moments(M)
+    Mv = min(40, M)
+    ref = fk.Engine(False, "fp64")
+    ref.set_H(H, es)
+    ref.set_R(R)
+    err = _mu_err(mu[:Mv], ref.moments(Mv))
+    ref.close()
+    sv = {"fp32": 4, "ds": 8, "fp64": 8}[prec]
+    bytes_step = 3 * H.n_rows * S * sv + H.n_blocks() * (sv + 4) + 4 * (H.n_rows + 1)
+    achieved = bytes_step / (t_step / n_step * 1e-3) / 1e9
+    peak, kind = peaks()
+    per = float(H.n_rows) * M * S
+    line = {"metric": METRIC, "value": per / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": prec, "data": "synthetic",
+            "config": {"workload": "square lattice L=%d (N=%d), b=1 real, S=%d, M=%d: moments, CUDA graph" % (L, H.n_rows, S, M),
+                       "l2": "inputs larger than L2" if 3 * H.n_rows * S * sv > 129e6 else "L2-resident"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "kernel": "k_cheb_step", "peak_source": kind, "bytes_per_launch": bytes_step,
+                         "avg_launch_ms": t_step / n_step},
+            "moments_max_rel_mu0_vs_fp64": err, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
 def run_cfg1(args):
     """32x32 square lattice, M=200, S=64, FP64: moments + stoch_matrix; oracle timed beside it."""
     import fastkpm_gb300 as fk
@@ -604,7 +658,8 @@ def main():
         return
     if args.workload != "solve":
         if rank == 0:
-            {"precision": run_precision, "batch": run_batch, "serve": run_serve, "cfg1": run_cfg1}[args.workload](args)
+            {"precision": run_precision, "batch": run_batch, "serve": run_serve, "cfg1": run_cfg1,
+             "square": run_square}[args.workload](args)
         return
     r = run_gb300(args, rank, ws, dist)
     cpu = None

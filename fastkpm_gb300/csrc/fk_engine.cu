@@ -9,6 +9,7 @@
 //   vectors rotate. stoch_matrix: two rotating vectors plus xi. autodiff: the
 //   two moment vectors (alpha) plus two beta vectors, all updated in place by
 //   the fused adjoint kernel. No allocation happens inside any recursion.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -108,6 +109,13 @@ struct fk_engine {
     DevBuf d_partials, d_raw, d_coef, d_stage;
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
+
+    // second-order moments (moments2_v1): operators j1, j2 in the engine's format, the two
+    // double panels of Chebyshev vectors, a scratch vector, the M x M result; cuBLAS reduces
+    struct Op { DevBuf row_ptr, colc, hval; };
+    Op d_j[2];
+    DevBuf d_panel[2], d_tmp, d_mu2;
+    cublasHandle_t blas = nullptr;
     std::vector<double> h_raw;
 
     KCfg cfg[fk::kNumKinds];
@@ -841,6 +849,21 @@ int fetch_D(fk_engine* e, double* D) {
     return FK_OK;
 }
 
+// Layout of the post-processing buffer for (M, Mq): [mu M][gamma Mq][energies Mq][result 4][c M]
+struct PostLayout {
+    double *mu, *gamma, *en, *res, *c;
+    static size_t doubles(int M, int Mq) { return 2 * (size_t)M + 2 * (size_t)Mq + 4; }
+};
+PostLayout post_layout(const fk_engine* e, int M, int Mq) {
+    PostLayout l;
+    l.mu = e->d_post.as<double>();
+    l.gamma = l.mu + M;
+    l.en = l.gamma + Mq;
+    l.res = l.en + Mq;
+    l.c = l.res + 4;
+    return l;
+}
+
 // Post-processing of the last moments(M) on the device, enqueued behind it: moments from the
 // per-step sums, gamma = moment_transform(mu, Mq), {mu_F, energy, n_tot} for the filling and,
 // with want_coef, the fermi_energy expansion coefficients at mu_F (kT as given).
@@ -851,12 +874,9 @@ int post_enqueue(fk_engine* e, int Mq, double kT, double filling, double delta, 
     if (!(filling > 0.0 && filling < 1.0)) return e->fail(FK_ERR_ARG, "kpm post-processing: filling must be in (0, 1)");
     if (!(delta >= 0.0) || filling - delta <= 0.0 || filling + delta >= 1.0)
         return e->fail(FK_ERR_ARG, "kpm post-processing: need 0 <= delta_filling < min(filling, 1 - filling)");
-    FK_TRY(e->d_post.ensure(sizeof(double) * (2 * (size_t)M + 2 * (size_t)Mq + 4)), "alloc post-processing");
-    double* mu = e->d_post.as<double>();
-    double* gamma = mu + M;
-    double* en = gamma + Mq;
-    double* res = en + Mq;
-    double* c = res + 4;
+    FK_TRY(e->d_post.ensure(sizeof(double) * PostLayout::doubles(M, Mq)), "alloc post-processing");
+    const PostLayout pl = post_layout(e, M, Mq);
+    double *mu = pl.mu, *gamma = pl.gamma, *en = pl.en, *res = pl.res, *c = pl.c;
     const double avg = (e->es_hi + e->es_lo) / 2.0, mag = (e->es_hi - e->es_lo) / 2.0;
     ProfScope ps(e, fk::kHelper);
     fk::k_moments_from_raw<<<(M + 255) / 256, 256, 0, e->stream>>>(e->d_raw.as<double>(), M, mu);
@@ -872,13 +892,216 @@ int post_enqueue(fk_engine* e, int Mq, double kT, double filling, double delta, 
 
 // result[0..3) = {mu_F, energy, n_tot}; gamma (optional) = Mq doubles
 int post_fetch(fk_engine* e, double* result, double* gamma) {
-    const double* res = e->d_post.as<double>() + e->post_M + 2 * (size_t)e->post_Mq;
-    FK_TRY(cudaMemcpyAsync(result, res, sizeof(double) * 3, cudaMemcpyDeviceToHost, e->stream), "copy results");
+    const PostLayout pl = post_layout(e, e->post_M, e->post_Mq);
+    FK_TRY(cudaMemcpyAsync(result, pl.res, sizeof(double) * 3, cudaMemcpyDeviceToHost, e->stream), "copy results");
     if (gamma)
-        FK_TRY(cudaMemcpyAsync(gamma, e->d_post.as<double>() + e->post_M, sizeof(double) * e->post_Mq,
+        FK_TRY(cudaMemcpyAsync(gamma, pl.gamma, sizeof(double) * e->post_Mq,
                                cudaMemcpyDeviceToHost, e->stream),
                "copy gamma");
     FK_TRY(cudaStreamSynchronize(e->stream), "post-processing");
+    return FK_OK;
+}
+
+// ---- second-order moments (moments2_v1) ----
+
+cudaError_t prec_export(fk_engine* e, const void* src, long long c0, int w, double* dst) {
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_export_panel_f64(e->cplx, src, e->n, e->ld, c0, w, dst, e->stream);
+        case fk::kF32: return fk::launch_export_panel_f32(e->cplx, src, e->n, e->ld, c0, w, dst, e->stream);
+        default: return fk::launch_export_panel_ds(e->cplx, src, e->n, e->ld, c0, w, dst, e->stream);
+    }
+}
+
+struct M2Mat {
+    const int* row_ptr;
+    const unsigned* colc;
+    const void* hval;
+};
+
+// y = (two ? 2 : 1) A x (- z) on the packet columns [c0_el / EPP, + P_sl) of the row-major
+// vectors, with the step kernel's launch shape (any BSR A with H's block rows fits it: the H
+// stage holds stage_cap blocks and tiles with more blocks read A from global memory).
+int m2_step(fk_engine* e, const M2Mat& A, const void* x, const void* z, void* y, bool two, long long c0_el, int P_sl) {
+    const KCfg& c = e->cfg[fk::kStep];
+    const size_t es = e->esize();
+    fk::StepArgs a;
+    a.sys = c.sys.as<SysDesc>();
+    a.cta_sys = c.cta_sys.as<int>();
+    a.Gp = c.Gp;
+    a.P = P_sl;
+    a.ld = e->ld;
+    a.row_ptr = A.row_ptr;
+    a.colc = A.colc;
+    a.hval = A.hval;
+    a.x = (const char*)x + c0_el * es;
+    a.z = z ? (const char*)z + c0_el * es : nullptr;
+    a.y = (char*)y + c0_el * es;
+    a.xi = nullptr;
+    a.coef = nullptr;
+    a.cstride = 0;
+    a.two = two;
+    a.has_z = z != nullptr;
+    a.want_dots = 0;
+    a.xi_mode = 0;
+    a.partials = nullptr;
+    // the staged (TMA) configuration sizes its shared memory differently: run unstaged then
+    a.stage_cap = c.staged ? 0 : c.stage_cap;
+    ProfScope ps(e, fk::kStep);
+    FK_TRY(prec_launch_step(e, c.NP, a, fk::Launch{c.ctas, c.staged ? 0 : c.smem, e->stream}), "moments2 step");
+    return FK_OK;
+}
+
+int blas_fail(fk_engine* e, cublasStatus_t st, const char* what) {
+    return e->fail(st == CUBLAS_STATUS_ALLOC_FAILED ? FK_ERR_OOM : FK_ERR_CUDA, "%s: cuBLAS status %d", what, (int)st);
+}
+
+// Upload operator q (j1 or j2) in the engine's format: H's block rows, unscaled (energy scale
+// [-1, 1]), a zero diagonal block inserted where a row has none.
+int m2_upload_op(fk_engine* e, int q, int nnzb, const int* rp, const int* ci, const double* val) {
+    fk::PreparedH ph;
+    std::string why;
+    const int rc = fk::prepare_H(e->prec, e->cplx, e->n_b, e->b, nnzb, rp, ci, val, -1.0, 1.0, 0, ph, why);
+    if (rc != FK_OK) return e->fail(rc, "moments2_v1: j%d: %s", q + 1, why.c_str());
+    fk_engine::Op& op = e->d_j[q];
+    FK_TRY(op.row_ptr.ensure(sizeof(int) * ph.row_ptr.size()), "alloc operator");
+    FK_TRY(op.colc.ensure(sizeof(unsigned) * std::max<size_t>(ph.colc.size(), 1)), "alloc operator");
+    FK_TRY(op.hval.ensure(std::max<size_t>(ph.hval.size(), 16)), "alloc operator");
+    FK_TRY(cudaMemcpy(op.row_ptr.p, ph.row_ptr.data(), sizeof(int) * ph.row_ptr.size(), cudaMemcpyHostToDevice),
+           "upload operator");
+    if (!ph.colc.empty()) {
+        FK_TRY(cudaMemcpy(op.colc.p, ph.colc.data(), sizeof(unsigned) * ph.colc.size(), cudaMemcpyHostToDevice),
+               "upload operator");
+        FK_TRY(cudaMemcpy(op.hval.p, ph.hval.data(), ph.hval.size(), cudaMemcpyHostToDevice), "upload operator");
+    }
+    return FK_OK;
+}
+
+// moments2_v1 (reference src/engine_cpu.cpp:86-160, src/engine_cusparse.cpp:793-902):
+//   mu[m1][m2] = sum_k <T_m1(Hs) r_k, j2 T_m2(Hs) j1 r_k>.
+// The probe columns run in slices of r_chunk columns (all at once by default); per slice the
+// Chebyshev vectors alpha_m = T_m r and j2 atild_m (atild_m = T_m j1 r) are written, K orders
+// at a time, as double panels, and mu's K x K blocks are one GEMM each (A^H B over the panel
+// rows) instead of the reference's M^2 separate dot products. K = a_chunk when >= 3, else the
+// largest that fits 60% of free device memory (K = M: every recursion runs once per slice).
+// Each panel of atild restarts its recursion from j1 r, as the reference does.
+int moments2_v1(fk_engine* e, int M, const int* nnzb, const int* const* rp, const int* const* ci,
+                const double* const* val, int a_chunk, int r_chunk, double* mu_out) {
+    if (M < 2 || M % 2 != 0) return e->fail(FK_ERR_ARG, "moments2_v1: M must be even and >= 2 (got %d)", M);
+    int rc = require_ready(e);
+    if (rc != FK_OK) return rc;
+    for (int q = 0; q < 2; q++) {
+        rc = m2_upload_op(e, q, nnzb[q], rp[q], ci[q], val[q]);
+        if (rc != FK_OK) return rc;
+    }
+    const int epp = e->epp();
+    const int w_el = r_chunk > 0 ? std::min(r_chunk, e->s) : e->s;
+    int wp = (w_el + epp - 1) / epp;                                  // packets per column slice
+    while (wp > 1 && (long long)e->n * wp * epp >= (1LL << 31)) wp = (wp + 1) / 2;   // GEMM sizes are int
+    if ((long long)e->n * wp * epp >= (1LL << 31)) return e->fail(FK_ERR_UNSUPPORTED, "moments2_v1: too many rows");
+    const int nsl = (e->P + wp - 1) / wp;
+    const long long Lmax = (long long)e->n * wp * epp;
+    const size_t elt = e->cplx ? 16 : 8;
+    int K;
+    if (a_chunk >= 3) {
+        K = std::min(a_chunk, M);
+    } else {
+        size_t fr = 0, tot = 0;
+        FK_TRY(cudaMemGetInfo(&fr, &tot), "memory query");
+        const size_t per = 2 * (size_t)Lmax * elt;
+        K = (int)std::min<size_t>(M, std::max<size_t>(2, fr / 10 * 6 / per));
+    }
+    FK_TRY(e->d_panel[0].ensure((size_t)K * Lmax * elt), "alloc panel");
+    FK_TRY(e->d_panel[1].ensure((size_t)K * Lmax * elt), "alloc panel");
+    FK_TRY(e->d_tmp.ensure(e->vec_bytes()), "alloc scratch vector");
+    FK_TRY(e->d_mu2.ensure((size_t)M * M * elt), "alloc moments");
+    FK_TRY(cudaMemsetAsync(e->d_mu2.p, 0, (size_t)M * M * elt, e->stream), "clear moments");
+    if (!e->blas) {
+        const cublasStatus_t st = cublasCreate(&e->blas);
+        if (st != CUBLAS_STATUS_SUCCESS) { e->blas = nullptr; return blas_fail(e, st, "cublasCreate"); }
+    }
+    cublasStatus_t bst = cublasSetStream(e->blas, e->stream);
+    if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "cublasSetStream");
+    const M2Mat hs{e->d_row_ptr.as<int>(), e->d_colc.as<unsigned>(), e->d_hval.p};
+    const M2Mat j1{e->d_j[0].row_ptr.as<int>(), e->d_j[0].colc.as<unsigned>(), e->d_j[0].hval.p};
+    const M2Mat j2{e->d_j[1].row_ptr.as<int>(), e->d_j[1].colc.as<unsigned>(), e->d_j[1].hval.p};
+    void* R = e->d_R.p;
+    void* V[4] = {e->d_V[0].p, e->d_V[1].p, e->d_V[2].p, e->d_V[3].p};
+    char* PA = e->d_panel[0].as<char>();
+    char* PB = e->d_panel[1].as<char>();
+    for (int sl = 0; sl < nsl; sl++) {
+        const long long c0 = (long long)sl * wp * epp;
+        const int P_sl = std::min(wp, e->P - sl * wp);
+        const int w = P_sl * epp;
+        const long long L = (long long)e->n * w;
+        // alpha_m = T_m(Hs) r: alpha_0 = R, then two rotating vectors (never overwriting R)
+        const void* aP = nullptr;
+        void* aC = nullptr;
+        int am = -1;
+        auto alpha_next = [&]() -> int {
+            const int m = ++am;
+            if (m == 0) { aC = R; return FK_OK; }
+            void* y = m == 1 ? V[0] : (aP == R ? V[1] : const_cast<void*>(aP));
+            const int r = m2_step(e, hs, aC, m == 1 ? nullptr : aP, y, m > 1, c0, P_sl);
+            aP = aC;
+            aC = y;
+            return r;
+        };
+        for (int a0 = 0; a0 < M; a0 += K) {
+            const int Ka = std::min(K, M - a0);
+            for (int q = 0; q < Ka; q++) {
+                rc = alpha_next();
+                if (rc != FK_OK) return rc;
+                FK_TRY(prec_export(e, aC, c0, w, reinterpret_cast<double*>(PA + (size_t)q * L * elt)), "export panel");
+            }
+            // atild_m = T_m(Hs) j1 r, restarted for every alpha panel; panel B holds j2 atild_m
+            void* tP = nullptr;
+            void* tC = nullptr;
+            for (int b0 = 0, tm = -1; b0 < M; b0 += K) {
+                const int Kb = std::min(K, M - b0);
+                for (int q = 0; q < Kb; q++) {
+                    const int m = ++tm;
+                    void* y = m == 0 ? V[2] : (m == 1 ? V[3] : tP);
+                    rc = m == 0 ? m2_step(e, j1, R, nullptr, y, false, c0, P_sl)
+                                : m2_step(e, hs, tC, m == 1 ? nullptr : tP, y, m > 1, c0, P_sl);
+                    if (rc != FK_OK) return rc;
+                    tP = tC;
+                    tC = y;
+                    rc = m2_step(e, j2, tC, nullptr, e->d_tmp.p, false, c0, P_sl);
+                    if (rc != FK_OK) return rc;
+                    FK_TRY(prec_export(e, e->d_tmp.p, c0, w, reinterpret_cast<double*>(PB + (size_t)q * L * elt)),
+                           "export panel");
+                }
+                // mu[a0 .. a0+Ka, b0 .. b0+Kb] += A^H B   (mu column-major M x M on the device)
+                if (e->cplx) {
+                    const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0);
+                    bst = cublasZgemm(e->blas, CUBLAS_OP_C, CUBLAS_OP_N, Ka, Kb, (int)L, &one,
+                                      reinterpret_cast<const cuDoubleComplex*>(PA), (int)L,
+                                      reinterpret_cast<const cuDoubleComplex*>(PB), (int)L, &one,
+                                      e->d_mu2.as<cuDoubleComplex>() + a0 + (size_t)b0 * M, M);
+                } else {
+                    const double one = 1.0;
+                    bst = cublasDgemm(e->blas, CUBLAS_OP_T, CUBLAS_OP_N, Ka, Kb, (int)L, &one, reinterpret_cast<const double*>(PA),
+                                      (int)L, reinterpret_cast<const double*>(PB), (int)L, &one,
+                                      e->d_mu2.as<double>() + a0 + (size_t)b0 * M, M);
+                }
+                if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "moments2 GEMM");
+            }
+        }
+    }
+    std::vector<double> h((size_t)M * M * (e->cplx ? 2 : 1));
+    FK_TRY(cudaMemcpyAsync(h.data(), e->d_mu2.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
+           "copy moments");
+    FK_TRY(cudaStreamSynchronize(e->stream), "moments2_v1");
+    for (int m1 = 0; m1 < M; m1++)
+        for (int m2 = 0; m2 < M; m2++) {
+            const size_t src = (size_t)m1 + (size_t)m2 * M, dst = (size_t)m1 * M + m2;
+            mu_out[2 * dst] = e->cplx ? h[2 * src] : h[src];
+            mu_out[2 * dst + 1] = e->cplx ? h[2 * src + 1] : 0.0;
+        }
+    // the work vectors no longer hold the moments' recursion state
+    e->mom_M = 0;
+    e->mom_a0 = e->mom_a1 = -2;
+    if (e->profiling) prof_flush(e);
     return FK_OK;
 }
 
@@ -1039,6 +1262,11 @@ int fk_engine_destroy(fk_engine* e) {
     if (e->t_start) cudaEventDestroy(e->t_start);
     if (e->t_stop) cudaEventDestroy(e->t_stop);
     drop_graphs(e);
+    if (e->blas) cublasDestroy(e->blas);
+    for (auto& op : e->d_j) { op.row_ptr.release(); op.colc.release(); op.hval.release(); }
+    for (auto& pb : e->d_panel) pb.release();
+    e->d_tmp.release();
+    e->d_mu2.release();
     DevBuf* bufs[] = {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2], &e->d_V[3],
                       &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc, &e->d_partials, &e->d_raw,
                       &e->d_coef, &e->d_stage, &e->d_post, &e->d_t_uoff, &e->d_t_ucol, &e->d_t_own, &e->d_t_kslot,
@@ -1257,6 +1485,18 @@ int fk_engine_fetch_D(fk_engine* e, double* D) {
     return fetch_D(e, D);
 }
 
+int fk_engine_moments2_v1(fk_engine* e, int M, int j1_nnzb, const int* j1_row_ptr, const int* j1_col_idx,
+                          const double* j1_val, int j2_nnzb, const int* j2_row_ptr, const int* j2_col_idx,
+                          const double* j2_val, int a_chunk_ncols, int R_chunk_ncols, double* mu) {
+    if (!e || !mu || !j1_row_ptr || !j2_row_ptr) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    const int nnzb[2] = {j1_nnzb, j2_nnzb};
+    const int* rp[2] = {j1_row_ptr, j2_row_ptr};
+    const int* ci[2] = {j1_col_idx, j2_col_idx};
+    const double* val[2] = {j1_val, j2_val};
+    return moments2_v1(e, M, nnzb, rp, ci, val, a_chunk_ncols, R_chunk_ncols, mu);
+}
+
 int fk_engine_kpm_filling(fk_engine* e, int Mq, double kT, double filling, double delta_filling, double* result,
                           double* gamma) {
     if (!e || !result) return FK_ERR_ARG;
@@ -1276,7 +1516,7 @@ int fk_engine_solve_filling(fk_engine* e, int M, int Mq, double kT, double filli
     if (rc != FK_OK) return rc;
     rc = post_enqueue(e, Mq, kT, filling, delta_filling, true);
     if (rc != FK_OK) return rc;
-    const double* c_dev = e->d_post.as<double>() + 2 * (size_t)M + 2 * (size_t)Mq + 4;
+    const double* c_dev = post_layout(e, M, Mq).c;
     rc = autodiff_enqueue(e, M, nullptr, d_n_b, d_nnzb, d_row_ptr, d_col_idx, c_dev);
     if (rc != FK_OK) return rc;
     rc = fetch_D(e, D);

@@ -161,6 +161,105 @@ cx_double moment_product(Vec<Vec<cx_double>> const& c, Vec<Vec<cx_double>> const
         for (size_t b = 0; b < c[a].size(); b++) r += c[a][b] * mu[a][b];
     return r;
 }
+// Kubo-Bastin coefficients of the conductivity, src/fastkpm.cpp:80-233 (the direct-sum branch
+// without FFTW): static (omega = 0) and optical (0 < omega < 2 mag) forms on the Chebyshev
+// nodes, points within `cutoff` of the band edges skipped, scaled by the kernel and 2 pi.
+Vec<Vec<cx_double>> electrical_conductivity_coefficients(int M, int Mq, double kT, double mu, double omega,
+                                                         EnergyScale es, Vec<double> const& kernel) {
+    if ((int)kernel.size() != M) throw std::invalid_argument("electrical_conductivity_coefficients: kernel size != M");
+    if (Mq < 2 * M) throw std::invalid_argument("electrical_conductivity_coefficients: need Mq >= 2 M");
+    if (omega < 0.0) throw std::invalid_argument("electrical_conductivity_coefficients: omega must be >= 0");
+    const double cutoff = 1e-4;
+    const double ws = omega / es.mag();
+    Vec<Vec<cx_double>> ret(M, Vec<cx_double>(M, cx_double(0.0, 0.0)));
+    if (ws >= 2.0) return ret;
+    Vec<double> Ta(M), Tb(M);
+    if (ws < 1.0e-10) {
+        for (int i = 0; i < Mq; i++) {
+            const double x = std::cos(Pi * (i + 0.5) / Mq);
+            const double one_m = 1.0 - x * x;
+            if (one_m < cutoff) continue;
+            chebyshev_fill_array(x, Ta);            // T_m(x) = cos(m theta)
+            chebyshev_fill_array(x, Tb, 2);         // U_m(x); sin(m theta) = sqrt(1-x^2) U_{m-1}(x)
+            const double sq = std::sqrt(one_m);
+            for (int m = M - 1; m > 0; m--) Tb[m] = Tb[m - 1] * sq;
+            Tb[0] = 0.0;
+            const double f = fermi_density(es.unscale(x), kT, mu) / std::pow(one_m, 1.5);
+            for (int m1 = 0; m1 < M; m1++)
+                for (int m2 = 0; m2 < M; m2++)
+                    ret[m1][m2] += (Ta[m1] * cx_double(Ta[m2], -Tb[m2]) * cx_double(x, m2 * sq) +
+                                    Ta[m2] * cx_double(Ta[m1], Tb[m1]) * cx_double(x, -m1 * sq)) * f;
+        }
+    } else {
+        const int i_start = (int)std::ceil(std::acos(1.0 - ws) / Pi * Mq - 0.5);
+        if (Mq - i_start < 20) throw std::invalid_argument("electrical_conductivity_coefficients: omega too large for Mq");
+        for (int i = i_start; i < Mq; i++) {
+            const double x = std::cos(Pi * (i + 0.5) / Mq);
+            const double xw = x + ws;
+            if (x < -1.0 + cutoff || xw > 1.0 - cutoff) continue;
+            chebyshev_fill_array(xw, Ta);
+            chebyshev_fill_array(x, Tb);
+            const double E = es.unscale(x);
+            const double f = (fermi_density(E, kT, mu) - fermi_density(E + omega, kT, mu)) / (ws * std::sqrt(1.0 - xw * xw));
+            for (int m1 = 0; m1 < M; m1++)
+                for (int m2 = 0; m2 < M; m2++) ret[m1][m2] += Ta[m1] * Tb[m2] * f;
+        }
+    }
+    for (int m1 = 0; m1 < M; m1++) {
+        const double p1 = 2.0 * Pi * (m1 == 0 ? 1.0 : 2.0) * kernel[m1] / (Mq * es.mag() * es.mag());
+        for (int m2 = 0; m2 < M; m2++) ret[m1][m2] *= p1 * (m2 == 0 ? 1.0 : 2.0) * kernel[m2];
+    }
+    return ret;
+}
+
+// Two-dimensional moment_transform (src/fastkpm.cpp:258-289): gamma[i][j] =
+// sum_{m1,m2} T_m1(x_i) T_m2(x_j) mup[m1][m2], mup = (m1?2:1)(m2?2:1) g_m1 g_m2 mu[m1][m2],
+// evaluated as two matrix products (T^T mup, then by T) instead of the reference's fourfold loop.
+Vec<Vec<cx_double>> moment_transform(Vec<Vec<cx_double>> const& moments, int Mq, Vec<double> const& kernel) {
+    const int M = (int)moments.size();
+    Vec<double> T((size_t)Mq * M), row(M);
+    for (int i = 0; i < Mq; i++) {
+        chebyshev_fill_array(std::cos(Pi * (i + 0.5) / Mq), row);
+        std::copy(row.begin(), row.end(), T.begin() + (size_t)i * M);
+    }
+    std::vector<cx_double> mup((size_t)M * M), half((size_t)Mq * M, cx_double(0.0, 0.0));
+    for (int a = 0; a < M; a++)
+        for (int b = 0; b < M; b++)
+            mup[(size_t)a * M + b] = ((a == 0 ? 1.0 : 2.0) * (b == 0 ? 1.0 : 2.0) * kernel[a] * kernel[b]) * moments[a][b];
+    for (int i = 0; i < Mq; i++)        // half[i][m2] = sum_m1 T_m1(x_i) mup[m1][m2]
+        for (int a = 0; a < M; a++) {
+            const double t = T[(size_t)i * M + a];
+            for (int b = 0; b < M; b++) half[(size_t)i * M + b] += t * mup[(size_t)a * M + b];
+        }
+    Vec<Vec<cx_double>> gamma(Mq, Vec<cx_double>(Mq, cx_double(0.0, 0.0)));
+    for (int i = 0; i < Mq; i++)
+        for (int j = 0; j < Mq; j++) {
+            cx_double acc(0.0, 0.0);
+            for (int b = 0; b < M; b++) acc += T[(size_t)j * M + b] * half[(size_t)i * M + b];
+            gamma[i][j] = acc;
+        }
+    return gamma;
+}
+
+// Two-dimensional density_function (src/fastkpm.cpp:335-361)
+void density_function(Vec<Vec<cx_double>> const& gamma, EnergyScale es, Vec<double>& x, Vec<double>& y,
+                      Vec<Vec<cx_double>>& rho) {
+    const int Mq1 = (int)gamma.size(), Mq2 = Mq1 ? (int)gamma[0].size() : 0;
+    x.assign(Mq1, 0.0);
+    y.assign(Mq2, 0.0);
+    rho.assign(Mq1, Vec<cx_double>(Mq2, cx_double(0.0, 0.0)));
+    for (int i2 = 0; i2 < Mq2; i2++) y[Mq2 - 1 - i2] = es.unscale(std::cos(Pi * (i2 + 0.5) / Mq2));
+    for (int i1 = 0; i1 < Mq1; i1++) {
+        const double x1 = std::cos(Pi * (i1 + 0.5) / Mq1);
+        x[Mq1 - 1 - i1] = es.unscale(x1);
+        for (int i2 = 0; i2 < Mq2; i2++) {
+            const double x2 = std::cos(Pi * (i2 + 0.5) / Mq2);
+            rho[Mq1 - 1 - i1][Mq2 - 1 - i2] =
+                gamma[i1][i2] / (Pi * std::sqrt(1.0 - x1 * x1) * Pi * std::sqrt(1.0 - x2 * x2) * es.mag() * es.mag());
+        }
+    }
+}
+
 Vec<double> moment_transform(Vec<double> const& moments, int Mq) {
     const int M = (int)moments.size();
     const Vec<double> g = jackson_kernel(M);
@@ -416,11 +515,29 @@ public:
         return mu;
     }
 
-    Vec<Vec<cx_double>> moments2_v1(int, SpMatBsr<T> const&, SpMatBsr<T> const&, int, int) override {
-        throw std::runtime_error("fkpm: moments2_v1 (conductivity) is not part of the GB300 build");
+    Vec<Vec<cx_double>> moments2_v1(int M, SpMatBsr<T> const& j1op, SpMatBsr<T> const& j2op, int a_chunk_ncols,
+                                    int R_chunk_ncols) override {
+        for (auto* j : {&j1op, &j2op})
+            if (j->n_rows != n_rows_ || j->n_cols != n_rows_ || j->b_len != b_len_)
+                throw std::invalid_argument("moments2_v1: j1 and j2 must have H's shape and block size");
+        std::vector<double> v1, v2, out(2 * (size_t)M * M);
+        to_doubles(j1op.val.data(), j1op.val.size(), v1);
+        to_doubles(j2op.val.data(), j2op.val.size(), v2);
+        check(fk_engine_moments2_v1(e_, M, j1op.n_blocks(), j1op.row_ptr.data(), j1op.col_idx.data(), v1.data(),
+                                    j2op.n_blocks(), j2op.row_ptr.data(), j2op.col_idx.data(), v2.data(),
+                                    a_chunk_ncols, R_chunk_ncols, out.data()),
+              "moments2_v1");
+        Vec<Vec<cx_double>> mu(M, Vec<cx_double>(M));
+        for (int m1 = 0; m1 < M; m1++)
+            for (int m2 = 0; m2 < M; m2++) {
+                const size_t q = (size_t)m1 * M + m2;
+                mu[m1][m2] = cx_double(out[2 * q], out[2 * q + 1]);
+            }
+        return mu;
     }
     Vec<Vec<cx_double>> moments2_v2(int, SpMatBsr<T> const&, SpMatBsr<T> const&, int, int) override {
-        throw std::runtime_error("fkpm: moments2_v2 (conductivity) is not part of the GB300 build");
+        // the reference's GPU engine exits here too (src/engine_cusparse.cpp:904-908)
+        throw std::runtime_error("fkpm: moments2_v2 is not implemented on the GPU");
     }
 
     void stoch_matrix(Vec<double> const& c, SpMatBsr<T>& D) override {

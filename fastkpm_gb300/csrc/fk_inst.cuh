@@ -119,5 +119,12 @@ cudaError_t FK_CAT(launch_scale, FK_PREC_NAME)(int cplx, const void* x, void* y,
     else k_scale<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(x), reinterpret_cast<FK_SYS_R::E*>(y), n_elems, c, c_dev);
     return cudaGetLastError();
 }
+cudaError_t FK_CAT(launch_export_panel, FK_PREC_NAME)(int cplx, const void* src, long long n, long long ld, long long c0,
+                                                    int w, double* dst, cudaStream_t st) {
+    const int g = helper_grid(n * w);
+    if (cplx) k_export_panel<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(src), n, ld, c0, w, dst);
+    else k_export_panel<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(src), n, ld, c0, w, dst);
+    return cudaGetLastError();
+}
 
 }  // namespace fk

@@ -688,6 +688,21 @@ __global__ void k_load_colmajor(const double* src, long long n, int ncols, int c
     }
 }
 
+// Columns [c0, c0 + w) of a row-major vector -> a dense row-major n x w panel of doubles (real) or
+// (re, im) double pairs (complex), converted from system S: one column of the GEMM that forms
+// the second-order moments.
+template <class S>
+__global__ void k_export_panel(const typename S::E* src, long long n, long long ld, long long c0, int w, double* dst) {
+    const long long total = n * (long long)w;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const long long r = q / w;
+        const int c = (int)(q - r * w);
+        const double2 v = S::to_double2(src[r * ld + c0 + c]);
+        if (S::CPLX) reinterpret_cast<double2*>(dst)[q] = v;
+        else dst[q] = v.x;
+    }
+}
+
 // Row-major device vector -> column-major double host layout (for reading back R / state).
 template <class S>
 __global__ void k_store_colmajor(const typename S::E* src, long long n, int ncols, long long ld, double* dst) {

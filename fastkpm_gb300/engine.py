@@ -428,10 +428,22 @@ class Engine:
         D.val = out
         return res[0], res[1], gamma
 
-    def moments2_v1(self, *a, **k):
-        raise NotImplementedError("moments2_v1 (conductivity) is not part of the GB300 build")
+    def moments2_v1(self, M, j1, j2, a_chunk_ncols=0, R_chunk_ncols=0):
+        """Second-order moments mu[m1, m2] = sum_k <T_m1 r_k, j2 T_m2 j1 r_k> ((M, M) complex;
+        src/engine_cusparse.cpp:793-902). j1, j2: SpMatBsr with H's block rows, unscaled."""
+        dt = np.complex128 if self.complex_values else np.float64
+        v1 = np.ascontiguousarray(j1.val, dtype=dt)
+        v2 = np.ascontiguousarray(j2.val, dtype=dt)
+        out = np.zeros(2 * M * M)
+        self._check(self.lib.fk_engine_moments2_v1(self.h, M, j1.n_blocks(), _ip(j1.row_ptr), _ip(j1.col_idx),
+                                                   _dp(v1.view(np.float64)), j2.n_blocks(), _ip(j2.row_ptr),
+                                                   _ip(j2.col_idx), _dp(v2.view(np.float64)), a_chunk_ncols,
+                                                   R_chunk_ncols, _dp(out)), "moments2_v1")
+        return out.view(np.complex128).reshape(M, M)
 
-    moments2_v2 = moments2_v1
+    def moments2_v2(self, *a, **k):
+        raise NotImplementedError("moments2_v2 is not implemented on the GPU (the reference's GPU engine exits "
+                                  "there too, src/engine_cusparse.cpp:904-908)")
 
 
 class Batch:

@@ -14,7 +14,8 @@
 //     mk_engine_cpu<T>() and mk_engine_mpi<T>() throw: neither is part of this
 //     build. mk_engine_cuSPARSE<T>(devices) returns the GB300 engine on
 //     devices[0] (device 0 when empty).
-//   * moments2_v1 / moments2_v2 (conductivity) throw std::runtime_error.
+//   * moments2_v1 runs on the GPU; moments2_v2 throws std::runtime_error (the
+//     reference's GPU engine does not implement it either).
 //   * Errors throw std::runtime_error instead of assert/abort/exit.
 //   * set_H(H) (one argument) is added; it takes the energy scale from
 //     energy_scale(H, 0.01).
@@ -154,6 +155,12 @@ namespace fkpm {
     double moment_product(Vec<double> const& c, Vec<double> const& mu);
     cx_double moment_product(Vec<Vec<cx_double>> const& c, Vec<Vec<cx_double>> const& mu);
     Vec<double> moment_transform(Vec<double> const& moments, int Mq);
+    // conductivity: Kubo-Bastin coefficients (direct-sum form) and the 2D transforms
+    Vec<Vec<cx_double>> electrical_conductivity_coefficients(int M, int Mq, double kT, double mu, double omega,
+                                                             EnergyScale es, Vec<double> const& kernel);
+    Vec<Vec<cx_double>> moment_transform(Vec<Vec<cx_double>> const& moments, int Mq, Vec<double> const& kernel);
+    void density_function(Vec<Vec<cx_double>> const& gamma, EnergyScale es, Vec<double>& x, Vec<double>& y,
+                          Vec<Vec<cx_double>>& rho);
     double density_product(Vec<double> const& gamma, std::function<double(double)> f, EnergyScale es);
     void density_function(Vec<double> const& gamma, EnergyScale es, Vec<double>& x, Vec<double>& rho);
     void integrated_density_function(Vec<double> const& gamma, EnergyScale es, Vec<double>& x, Vec<double>& irho);

@@ -137,6 +137,19 @@ int  fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* r
 int  fk_engine_expansion_coefficients(fk_engine* e, int M, int Mq, int f_kind, double kT, double mu,
                                       double es_lo, double es_hi, double* out);
 
+/* Engine<T>::moments2_v1(M, j1, j2, a_chunk_ncols, R_chunk_ncols) (reference
+ * src/engine_cusparse.cpp:793-902, src/engine_cpu.cpp:86-160): second-order moments
+ * mu[m1][m2] = sum_k <T_m1(Hs) r_k, j2 T_m2(Hs) j1 r_k> ~ tr(j1 T_m1(Hs) j2 T_m2(Hs)) over the
+ * probe columns r_k of R. j1, j2: BSR operators with H's block rows and block size (values as
+ * for set_H, not scaled). mu[2*(m1*M + m2) + {0,1}] = (re, im), M even. Chebyshev vectors in
+ * the engine's precision, reduction in FP64 (cuBLAS GEMMs over double panels).
+ * R_chunk_ncols > 0: probe columns per pass (default all); a_chunk_ncols >= 3: Chebyshev orders
+ * per panel (default: as many as fit 60% of free device memory). Overwrites the recursion state
+ * that moments() leaves for autodiff_matrix(). */
+int  fk_engine_moments2_v1(fk_engine* e, int M, int j1_nnzb, const int* j1_row_ptr, const int* j1_col_idx,
+                           const double* j1_val, int j2_nnzb, const int* j2_row_ptr, const int* j2_col_idx,
+                           const double* j2_val, int a_chunk_ncols, int R_chunk_ncols, double* mu);
+
 /* KPM post-processing of the last moments(M) on the device, with no host round trip after
  * the moments: gamma = moment_transform(mu, Mq) (reference src/fastkpm.cpp:236-256), the
  * chemical potential mu_F = filling_to_mu(gamma, es, kT, filling, delta_filling) (:413-427:

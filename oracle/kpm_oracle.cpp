@@ -410,6 +410,69 @@ void fill_R_identity(int n, int j0, int j1, T* R) {
     for (int j = j0; j < j1; j++) R[size_t(j - j0) * n + j] = T(1.0);
 }
 
+// y = A x for one vector (BSR A, no scaling)
+template <typename T>
+void bsr_spmv(const int n_b, const int b, const int* row_ptr, const int* col_idx, const T* val, const T* x, T* y) {
+    for (int i = 0; i < n_b; i++) {
+        for (int bi = 0; bi < b; bi++) y[b * i + bi] = T(0);
+        for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+            const T* blk = val + size_t(b) * b * k;
+            for (int bj = 0; bj < b; bj++)
+                for (int bi = 0; bi < b; bi++) y[b * i + bi] += blk[b * bj + bi] * x[b * col_idx[k] + bj];
+        }
+    }
+}
+
+// moments2_v1 (src/engine_cpu.cpp:86-160): mu[m1][m2] = sum_k cdot(alpha_m1, j2 atild_m2) with
+// alpha_m = T_m(Hs) r_k, atild_m = T_m(Hs) j1 r_k over the probe columns r_k. The reference walks
+// the orders in chunks of a_chunk_ncols, recomputing the recursions; the chunking changes no sum,
+// so this keeps every order of one column at once. Columns run in parallel; the per-column
+// contributions are added in column order.
+template <typename T>
+int moments2_v1(Engine<T>& e, int M, int n_b, int b, const int* rp1, const int* ci1, const T* v1, const int* rp2,
+                const int* ci2, const T* v2, cx* mu) {
+    const int n = e.n, s = e.s;
+    if (M < 2 || M % 2 != 0 || n == 0 || n_b * b != n || e.Hs.n_b != n_b || e.Hs.b != b) return 1;
+    std::vector<std::vector<cx>> part(s, std::vector<cx>(size_t(M) * M, cx(0)));
+    const Bsr<T>& H = e.Hs;
+    auto hs = [&](const T* x, T* y) {
+        bsr_spmv(n_b, b, H.row_ptr.data(), H.col_idx.data(), H.val.data(), x, y);
+    };
+    parallel_ranges(e.nthreads, s, [&](int, long k0, long k1) {
+        std::vector<T> A(size_t(M) * n), Bt(size_t(M) * n), t(n), r(n);
+        for (long k = k0; k < k1; k++) {
+            for (int i = 0; i < n; i++) r[i] = e.R[size_t(i) * s + k];
+            auto recurse = [&](const T* v0, T* out) {   // out[m] = T_m(Hs) v0
+                std::copy_n(v0, n, out);
+                if (M > 1) hs(out, out + n);
+                for (int m = 2; m < M; m++) {
+                    hs(out + size_t(m - 1) * n, out + size_t(m) * n);
+                    for (int i = 0; i < n; i++)
+                        out[size_t(m) * n + i] = T(2) * out[size_t(m) * n + i] - out[size_t(m - 2) * n + i];
+                }
+            };
+            recurse(r.data(), A.data());
+            bsr_spmv(n_b, b, rp1, ci1, v1, r.data(), t.data());   // j1 r_k
+            recurse(t.data(), Bt.data());
+            for (int m2 = 0; m2 < M; m2++) {
+                bsr_spmv(n_b, b, rp2, ci2, v2, Bt.data() + size_t(m2) * n, t.data());   // j2 atild_m2
+                for (int m1 = 0; m1 < M; m1++) {
+                    cx acc = 0;
+                    const T* a = A.data() + size_t(m1) * n;
+                    for (int i = 0; i < n; i++) acc += cx(conj_(a[i]) * t[i]);
+                    part[k][size_t(m1) * M + m2] = acc;
+                }
+            }
+        }
+    });
+    for (size_t q = 0; q < size_t(M) * M; q++) {
+        cx acc = 0;
+        for (int k = 0; k < s; k++) acc += part[k][q];
+        mu[q] = acc;
+    }
+    return 0;
+}
+
 }  // namespace
 
 struct orc_engine {
@@ -466,6 +529,15 @@ int orc_autodiff_matrix(orc_engine* e, int M, const double* c, int n_b, int nnzb
     (void)n_b;
     if (e->cplx) return autodiff_matrix(e->ec, M, c, nnzb, row_ptr, rows, cols, reinterpret_cast<cx*>(D));
     return autodiff_matrix(e->er, M, c, nnzb, row_ptr, rows, cols, D);
+}
+
+int orc_moments2_v1(orc_engine* e, int M, int n_b, int b, const int* rp1, const int* ci1, const double* v1,
+                    const int* rp2, const int* ci2, const double* v2, double* mu) {
+    cx* out = reinterpret_cast<cx*>(mu);
+    if (e->cplx)
+        return moments2_v1(e->ec, M, n_b, b, rp1, ci1, reinterpret_cast<const cx*>(v1), rp2, ci2,
+                           reinterpret_cast<const cx*>(v2), out);
+    return moments2_v1(e->er, M, n_b, b, rp1, ci1, v1, rp2, ci2, v2, out);
 }
 
 int orc_energy_scale(orc_engine* e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
@@ -606,6 +678,55 @@ double orc_moment_product(int M, const double* c, const double* mu) {
     double r = 0;
     for (int i = 0; i < M; i++) r += c[i] * mu[i];
     return r;
+}
+
+// electrical_conductivity_coefficients, direct-sum branch (src/fastkpm.cpp:80-233 without FFTW):
+// out[2*(m1*M + m2) + {0,1}]; returns 1 on the reference's assertion failures
+int orc_electrical_conductivity_coefficients(int M, int Mq, double kT, double mu, double omega, double lo, double hi,
+                                             const double* kernel, double* out) {
+    if (Mq < 2 * M || omega < 0.0) return 1;
+    const double mag = (hi - lo) / 2.0, avg = (hi + lo) / 2.0, cutoff = 1e-4, ws = omega / mag;
+    std::vector<cx> ret(size_t(M) * M, cx(0.0, 0.0));
+    std::vector<double> Ti(M), Tj(M);
+    if (ws < 2.0 && ws < 1.0e-10) {
+        for (int i = 0; i < Mq; i++) {
+            const double x = std::cos(kPi * (i + 0.5) / Mq);
+            if (1.0 - x * x < cutoff) continue;
+            orc_chebyshev_fill_array(x, M, 1, Ti.data());
+            orc_chebyshev_fill_array(x, M, 2, Tj.data());
+            const double s1 = std::sqrt(1.0 - x * x);
+            for (int m = M - 1; m > 0; m--) Tj[m] = Tj[m - 1] * s1;
+            Tj[0] = 0.0;
+            const double f = orc_fermi_density(x * mag + avg, kT, mu) / std::pow(1.0 - x * x, 1.5);
+            for (int a = 0; a < M; a++)
+                for (int b = 0; b < M; b++)
+                    ret[size_t(a) * M + b] += (Ti[a] * cx(Ti[b], -Tj[b]) * cx(x, b * s1) +
+                                               Ti[b] * cx(Ti[a], Tj[a]) * cx(x, -a * s1)) * f;
+        }
+    } else if (ws < 2.0) {
+        const int i_start = int(std::ceil(std::acos(1.0 - ws) / kPi * Mq - 0.5));
+        if (Mq - i_start < 20) return 1;
+        for (int i = i_start; i < Mq; i++) {
+            const double x = std::cos(kPi * (i + 0.5) / Mq), xw = x + ws;
+            if (x < -1.0 + cutoff || xw > 1.0 - cutoff) continue;
+            orc_chebyshev_fill_array(xw, M, 1, Ti.data());
+            orc_chebyshev_fill_array(x, M, 1, Tj.data());
+            const double E = x * mag + avg;
+            const double f = (orc_fermi_density(E, kT, mu) - orc_fermi_density(E + omega, kT, mu)) /
+                             (ws * std::sqrt(1.0 - xw * xw));
+            for (int a = 0; a < M; a++)
+                for (int b = 0; b < M; b++) ret[size_t(a) * M + b] += Ti[a] * Tj[b] * f;
+        }
+    }
+    for (int a = 0; a < M; a++)
+        for (int b = 0; b < M; b++) {
+            const double pref = 2.0 * kPi * (a == 0 ? 1.0 : 2.0) * kernel[a] / (Mq * mag * mag) * (b == 0 ? 1.0 : 2.0) *
+                                kernel[b];
+            const cx v = ret[size_t(a) * M + b] * pref;
+            out[2 * (size_t(a) * M + b)] = v.real();
+            out[2 * (size_t(a) * M + b) + 1] = v.imag();
+        }
+    return 0;
 }
 
 // moment_transform (src/fastkpm.cpp:236-256): Jackson-damped density on the Mq Chebyshev nodes

@@ -80,6 +80,14 @@ double orc_fermi_energy(double x, double kT, double mu);
 void   orc_expansion_coefficients(int M, int Mq, int kind, double kT, double mu,
                                   double es_lo, double es_hi, double* out);
 double orc_moment_product(int M, const double* c, const double* mu);
+/* moments2_v1 (src/engine_cpu.cpp:86-160): mu[m1*M + m2] (complex, interleaved) =
+ * sum_k cdot(T_m1(Hs) r_k, j2 T_m2(Hs) j1 r_k); j1, j2 BSR with H's block structure, unscaled */
+int    orc_moments2_v1(orc_engine* e, int M, int n_b, int b, const int* rp1, const int* ci1, const double* v1,
+                       const int* rp2, const int* ci2, const double* v2, double* mu);
+/* electrical_conductivity_coefficients, direct-sum branch (src/fastkpm.cpp:80-233):
+ * out[2*(m1*M + m2) + {0,1}]; 1 on the reference's assertion failures */
+int    orc_electrical_conductivity_coefficients(int M, int Mq, double kT, double mu, double omega, double lo,
+                                                double hi, const double* kernel, double* out);
 /* moment_transform, mu_to_filling, filling_to_mu, electronic_energy (src/fastkpm.cpp:236-256,
  * :395-400, :413-427, :463-467); es = [lo, hi] */
 void   orc_moment_transform(int M, const double* mu, int Mq, double* gamma);

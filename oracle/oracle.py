@@ -42,6 +42,8 @@ _SIG = {
     "orc_expansion_coefficients": (None, [_i, _i, _i, _d, _d, _d, _d, _dp]),
     "orc_moment_product": (_d, [_i, _dp, _dp]),
     "orc_moment_transform": (None, [_i, _dp, _i, _dp]),
+    "orc_moments2_v1": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _ip, _ip, _dp, _dp]),
+    "orc_electrical_conductivity_coefficients": (_i, [_i, _i, _d, _d, _d, _d, _d, _dp, _dp]),
     "orc_mu_to_filling": (_d, [_i, _dp, _d, _d, _d, _d]),
     "orc_filling_to_mu": (_d, [_i, _dp, _d, _d, _d, _d, _d]),
     "orc_electronic_energy": (_d, [_i, _dp, _d, _d, _d, _d, _d]),
@@ -132,6 +134,17 @@ class OracleEngine:
                                         _ip_(D.row_idx), _ip_(D.col_idx), _dp_(_dbl(out)))
         assert st == 0, st
         return out
+
+    def moments2_v1(self, M, j1, j2):
+        """mu[m1, m2] = sum_k <T_m1 r_k, j2 T_m2 j1 r_k> (src/engine_cpu.cpp:86-160), (M, M) complex."""
+        out = np.zeros(2 * M * M)
+        v1 = _dbl(j1.val)
+        v2 = _dbl(j2.val)
+        st = lib().orc_moments2_v1(self.h, M, j1.n_rows, j1.b_len, _ip_(j1.row_ptr), _ip_(j1.col_idx), _dp_(v1),
+                                   _ip_(j2.row_ptr), _ip_(j2.col_idx), _dp_(v2), _dp_(out))
+        if st:
+            raise RuntimeError("orc_moments2_v1: status %d" % st)
+        return out.view(np.complex128).reshape(M, M)
 
     def energy_scale(self, H, extend, iters, v0):
         lo, hi = C.c_double(), C.c_double()
@@ -224,3 +237,12 @@ def filling_to_mu(gamma, lo, hi, kT, filling, delta_filling=0.0):
 def electronic_energy(gamma, lo, hi, kT, filling, mu):
     g = np.ascontiguousarray(gamma, np.float64)
     return lib().orc_electronic_energy(len(g), _dp_(g), lo, hi, kT, filling, mu)
+
+
+def electrical_conductivity_coefficients(M, Mq, kT, mu, omega, lo, hi, kernel):
+    k = np.ascontiguousarray(kernel, np.float64)
+    out = np.zeros(2 * M * M)
+    st = lib().orc_electrical_conductivity_coefficients(M, Mq, kT, mu, omega, lo, hi, _dp_(k), _dp_(out))
+    if st:
+        raise ValueError("electrical_conductivity_coefficients: reference assertion")
+    return out.view(np.complex128).reshape(M, M)

@@ -175,8 +175,10 @@ def test_missing_diagonal_blocks_are_inserted(gpu):
 
 @pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
 def test_staged_and_plain_step_agree(gpu, prec):
-    """The TMA-staged step kernel (default when its gather lists fit) and the per-thread-gather
-    kernel compute the same rows in the same order: moments agree to rounding of the CTA sums."""
+    """The staged step kernels (TMA bulk copies, cp.async) and the per-thread-gather kernel compute
+    the same rows in the same order: FP64/DS moments agree to rounding of the CTA sums (1e-13).
+    FP32 complex products may be contracted into FMAs differently in the two compiled kernels,
+    so FP32 moments agree to FP32 rounding (1e-6, measured 9e-9)."""
     H, es, R = small_complex_case(6, 32, 4)
     M = 30
     mus = []
@@ -189,7 +191,7 @@ def test_staged_and_plain_step_agree(gpu, prec):
         mus.append(eng.moments(M))
         eng.close()
     for mu in mus[:2]:
-        assert np.max(np.abs(mu - mus[2])) / abs(mus[2][0]) <= 1e-13
+        assert np.max(np.abs(mu - mus[2])) / abs(mus[2][0]) <= (1e-6 if prec == "fp32" else 1e-13)
 
 
 def test_device_expansion_coefficients(gpu):

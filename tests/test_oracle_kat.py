@@ -267,3 +267,33 @@ def test_electronic_energy_approaches_sum_of_occupied_levels():
         mu_f = O.filling_to_mu(gamma, es.lo, es.hi, 0.0, 0.5)
         errs.append(abs(O.electronic_energy(gamma, es.lo, es.hi, 0.0, 0.5, mu_f) - exact) / abs(exact))
     assert errs[1] < 5e-3 and errs[1] < errs[0]
+
+
+def _dense_cheb(A, M):
+    T = [np.eye(A.shape[0], dtype=A.dtype), A.copy()]
+    for m in range(2, M):
+        T.append(2 * A @ T[-1] - T[-2])
+    return T[:M]
+
+
+def test_moments2_v1_identity_probes_is_trace():
+    # identity probes: mu[m1, m2] = tr(j1 T_m1(Hs) j2 T_m2(Hs)) exactly
+    H, es, _ = W.cubic_spin_lattice(3, -1.0, 1.0, seed=4)
+    n = H.n_rows * H.b_len                      # scalar rows (n_rows counts block rows)
+    A = dense_Hs(H, es)
+    rng = np.random.default_rng(5)
+    rows, cols = H.row_idx, H.col_idx
+
+    def rand_op():
+        return SpMatBsr.build(H.n_rows, 2, rows, cols,
+                              rng.standard_normal((len(rows), 4)) + 1j * rng.standard_normal((len(rows), 4)))
+    j1, j2 = rand_op(), rand_op()
+    e = O.OracleEngine(True, nthreads=2)
+    e.set_H(H, es)
+    e.set_R(O.R_identity(n, complex_values=True))
+    M = 8
+    mu = e.moments2_v1(M, j1, j2)
+    T = _dense_cheb(A, M)
+    J1, J2 = j1.to_dense(), j2.to_dense()
+    ref = np.array([[np.trace(J1 @ T[a] @ J2 @ T[b]) for b in range(M)] for a in range(M)])
+    assert np.max(np.abs(mu - ref)) <= 1e-11 * np.max(np.abs(ref))
