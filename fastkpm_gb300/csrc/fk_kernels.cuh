@@ -220,8 +220,14 @@ __device__ __forceinline__ Tile tile_range(const int* row_ptr, const SysDesc& sd
 // Chebyshev step: y = (two ? 2 : 1) * Hs x  (- z), fused with the moment partials
 // <x,x>, Re<y,x> over own rows and with the stochastic sum xi.
 // ---------------------------------------------------------------------------------
+// "Light" step threads hold at most 32 bytes of x per block (b=1 and narrow rows, e.g. S=32
+// FP32): they are held to <= 40 registers so that 6 CTAs (48 warps) fit an SM (measured on
+// 64 square lattices, b=1, S=32: 47 ms vs 53 ms per M=500 batch, a few spilled bytes included).
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads, 2) k_cheb_step(StepArgs a) {
+constexpr bool kLightStep = B * NP * S::EPP * (int)sizeof(typename S::E) <= 32;
+
+template <class S, int B, int NP>
+__global__ void __launch_bounds__(kThreads, kLightStep<S, B, NP> ? 6 : 2) k_cheb_step(StepArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
     constexpr int EPT = NP * S::EPP;
@@ -264,8 +270,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step(StepArgs a) {
             for (int bi = 0; bi < B; bi++)
 #pragma unroll
                 for (int e = 0; e < EPT; e++) acc[bi][e] = S::zero();
-            // Not unrolled: every unroll factor measured slower (more registers, fewer warps),
-            // for light (b=1, S=32 FP32) and heavy (b=2, S=256 complex) threads alike.
+            // Not unrolled, and not pipelined by hand: unroll factors and a one-block-ahead
+            // gather both measured slower (registers, fewer warps), for light (b=1, S=32
+            // FP32) and heavy (b=2, S=256 complex) threads alike.
 #pragma unroll 1
             for (int k = kb; k < ke; k++) {
                 const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
