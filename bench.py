@@ -223,8 +223,8 @@ def run_gb300(args, rank, ws, dist):
         lib = Lb.load()
         Rf = np.asfortranarray(R)
         hv = np.ascontiguousarray(H.val)
-        lib.fk_host_register(Rf.ctypes.data, Rf.nbytes)
-        lib.fk_host_register(hv.ctypes.data, hv.nbytes)
+        pinned = lib.fk_host_register(Rf.ctypes.data, Rf.nbytes) == 0
+        pinned = (lib.fk_host_register(hv.ctypes.data, hv.nbytes) == 0) and pinned
         e2 = fk.Engine(True, args.precision, device=dev)
         mu_h = np.zeros(M)
         for _ in range(1):
@@ -234,13 +234,20 @@ def run_gb300(args, rank, ws, dist):
             e2.autodiff_matrix(c, D)
         barrier(dist)
         e2.synchronize()
+        phases = np.zeros(4)   # wall ms per step: set_H, set_R, moments (+ mu read), autodiff (+ D read)
         t0 = time.perf_counter()
         e2.timer_start()
         for _ in range(args.steps):
+            tp = [time.perf_counter()]
             e2.set_H(H, es)
+            tp.append(time.perf_counter())
             e2.set_R(Rf)
+            tp.append(time.perf_counter())
             mu_h = e2.moments(M)
+            tp.append(time.perf_counter())
             e2.autodiff_matrix(c, D)
+            tp.append(time.perf_counter())
+            phases += np.diff(tp) * 1e3
         e2_ms_dev = e2.timer_stop()
         e2_ms_wall = (time.perf_counter() - t0) * 1e3
         barrier(dist)
@@ -248,7 +255,9 @@ def run_gb300(args, rank, ws, dist):
         h2d = int(H.row_ptr.nbytes + H.col_idx.nbytes + hv.nbytes + Rf.nbytes)
         d2h = int(M * 8 + D.val.nbytes)
         e2e = {"value": per_solve * args.steps * ws / (e2_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2_ms / args.steps}
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2_ms / args.steps, "host_buffers_pinned": pinned,
+               "phases_ms_per_step": {k: float(v) / args.steps for k, v in
+                                      zip(["set_H", "set_R", "moments", "autodiff_matrix"], phases)}}
         lib.fk_host_unregister(Rf.ctypes.data)
         lib.fk_host_unregister(hv.ctypes.data)
         e2.close()

@@ -107,6 +107,10 @@ struct fk_engine {
 
     // scratch
     DevBuf d_partials, d_raw, d_coef, d_stage;
+    // R upload: a copy stream and events so the next chunk's host-to-device copy overlaps
+    // the layout kernel of the current one (two halves of d_stage)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
 
@@ -1262,6 +1266,11 @@ int fk_engine_destroy(fk_engine* e) {
     if (e->t_start) cudaEventDestroy(e->t_start);
     if (e->t_stop) cudaEventDestroy(e->t_stop);
     drop_graphs(e);
+    if (e->copy_stream) {
+        cudaStreamSynchronize(e->copy_stream);
+        cudaStreamDestroy(e->copy_stream);
+        for (int q = 0; q < 2; q++) { cudaEventDestroy(e->ev_copied[q]); cudaEventDestroy(e->ev_consumed[q]); }
+    }
     if (e->blas) cublasDestroy(e->blas);
     for (auto& op : e->d_j) { op.row_ptr.release(); op.colc.release(); op.hval.release(); }
     for (auto& pb : e->d_panel) pb.release();
@@ -1401,16 +1410,33 @@ int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
     if (rc != FK_OK) return rc;
     FK_TRY(cudaMemsetAsync(e->d_R.p, 0, e->vec_bytes(), e->stream), "clear R");
     for (auto& v : e->d_V) FK_TRY(cudaMemsetAsync(v.p, 0, e->vec_bytes(), e->stream), "clear work vector");
-    // upload in column chunks of at most ~256 MiB through a staging buffer
+    // upload in column chunks of at most ~128 MiB through two staging halves: the copy of
+    // chunk q+1 (copy stream) overlaps the layout kernel of chunk q (engine stream)
     const size_t col_bytes = sizeof(double) * (size_t)n * (e->cplx ? 2 : 1);
-    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)s, (256u << 20) / col_bytes));
-    FK_TRY(e->d_stage.ensure(col_bytes * chunk), "alloc staging buffer");
-    for (int c0 = 0; c0 < s; c0 += chunk) {
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)s, (128u << 20) / col_bytes));
+    const size_t half = col_bytes * chunk;
+    FK_TRY(e->d_stage.ensure(2 * half), "alloc staging buffer");
+    if (!e->copy_stream) {
+        FK_TRY(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking), "copy stream");
+        for (int q = 0; q < 2; q++) {
+            FK_TRY(cudaEventCreateWithFlags(&e->ev_copied[q], cudaEventDisableTiming), "copy event");
+            FK_TRY(cudaEventCreateWithFlags(&e->ev_consumed[q], cudaEventDisableTiming), "copy event");
+        }
+    }
+    // the staging halves may still be read by an earlier upload's kernels
+    FK_TRY(cudaEventRecord(e->ev_consumed[0], e->stream), "upload order");
+    FK_TRY(cudaEventRecord(e->ev_consumed[1], e->stream), "upload order");
+    for (int c0 = 0, q = 0; c0 < s; c0 += chunk, q ^= 1) {
         const int nc = std::min(chunk, s - c0);
-        FK_TRY(cudaMemcpyAsync(e->d_stage.p, (const char*)R + col_bytes * c0, col_bytes * nc, cudaMemcpyHostToDevice,
-                               e->stream), "upload R");
+        char* buf = e->d_stage.as<char>() + q * half;
+        FK_TRY(cudaStreamWaitEvent(e->copy_stream, e->ev_consumed[q], 0), "upload order");
+        FK_TRY(cudaMemcpyAsync(buf, (const char*)R + col_bytes * c0, col_bytes * nc, cudaMemcpyHostToDevice,
+                               e->copy_stream), "upload R");
+        FK_TRY(cudaEventRecord(e->ev_copied[q], e->copy_stream), "upload order");
+        FK_TRY(cudaStreamWaitEvent(e->stream, e->ev_copied[q], 0), "upload order");
         ProfScope ps(e, fk::kHelper);
-        FK_TRY(prec_load_colmajor(e, e->d_stage.as<double>(), n, nc, c0, e->d_R.p), "R layout kernel");
+        FK_TRY(prec_load_colmajor(e, reinterpret_cast<const double*>(buf), n, nc, c0, e->d_R.p), "R layout kernel");
+        FK_TRY(cudaEventRecord(e->ev_consumed[q], e->stream), "upload order");
     }
     FK_TRY(cudaStreamSynchronize(e->stream), "set_R");
     e->mom_M = 0;

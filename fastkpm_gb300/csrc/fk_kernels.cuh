@@ -206,10 +206,16 @@ struct Tile {
 };
 __device__ __forceinline__ Tile tile_range(const int* row_ptr, const SysDesc& sd, long long t0, long long items, int Gp,
                                            int stage_cap) {
+    Tile t;
+    if (stage_cap <= 0) {   // no stage: skip the two row_ptr reads (a memory round trip per tile)
+        t.k_lo = 0;
+        t.nk = 0;
+        t.staged = false;
+        return t;
+    }
     const int r_lo = sd.row_base + (int)(t0 / Gp);
     const long long t_last = min(t0 + kThreads, items) - 1;
     const int r_hi = sd.row_base + (int)(t_last / Gp);
-    Tile t;
     t.k_lo = row_ptr[r_lo];
     t.nk = row_ptr[r_hi + 1] - t.k_lo;
     t.staged = t.nk <= stage_cap;

@@ -243,6 +243,47 @@ def test_graph_replay_matches_direct_launches(gpu, prec):
     assert rel_err(replayed[-2], D_ref) <= TOL_D[prec]
 
 
+@pytest.mark.parametrize("prec", ["fp64", "ds"])
+def test_permutation_invariance(gpu, prec):
+    """Moments and D do not depend on the order of the probe columns, nor on the labelling of
+    the sites (H, R and D permuted together): equal to rounding (1e-12)."""
+    H, es, R = small_complex_case(4, 16, 13)
+    M = 24
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    eng = fk.Engine(True, prec)
+    eng.set_H(H, es)
+    eng.set_R(R)
+    mu0 = eng.moments(M)
+    D0 = H.pattern_like(True)
+    eng.autodiff_matrix(c, D0)
+    # probe columns reversed
+    eng.set_R(np.asfortranarray(R[:, ::-1]))
+    mu1 = eng.moments(M)
+    D1 = H.pattern_like(True)
+    eng.autodiff_matrix(c, D1)
+    assert mu_err(mu1, mu0) <= 1e-12
+    assert rel_err(D1.val, D0.val) <= 1e-12
+    # sites relabelled by a seeded permutation p: block row i of H' is block row p[i] of H
+    b = H.b_len
+    p = np.random.default_rng(3).permutation(H.n_rows)
+    inv = np.argsort(p)
+    blocks = H.val.reshape(-1, b * b)
+    Hp = fk.SpMatBsr.build(H.n_rows, b, inv[H.row_idx], inv[H.col_idx], blocks)
+    rows = (b * p[:, None] + np.arange(b)).reshape(-1)   # scalar row r' of R' is row rows[r'] of R
+    eng.set_H(Hp, es)
+    eng.set_R(np.asfortranarray(R[rows]))
+    mu2 = eng.moments(M)
+    D2 = Hp.pattern_like(True)
+    eng.autodiff_matrix(c, D2)
+    assert mu_err(mu2, mu0) <= 1e-12
+    for k in range(0, H.n_blocks(), 7):
+        i, j = H.row_idx[k], H.col_idx[k]
+        ref = D0.val[k * b * b:(k + 1) * b * b]
+        kp = Hp.find_index(inv[i], inv[j])
+        assert np.max(np.abs(D2.val[kp * b * b:(kp + 1) * b * b] - ref)) <= 1e-12 * np.max(np.abs(D0.val))
+    eng.close()
+
+
 def test_results_are_deterministic(gpu):
     H, es, R = small_complex_case(6, 32, 2)
     eng = fk.Engine(True, "ds")
