@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, kLightStep<S, B, NP> ? 6 : 2) k_cheb
         const int il = (int)(t / Gp);
         const int g = (int)(t - (long long)il * Gp);
         const int i = sd.row_base + il;
-        const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];
+        const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];   // (reading these a tile ahead measured slower)
         for (int c = 0; c < nch; c++) {
             const int base = c * W;
             typename S::Acc acc[B][EPT];
