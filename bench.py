@@ -145,15 +145,21 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def adjoint_bytes_per_launch(eng_info, N, nnzb, b, sv):
-    """Algorithmic bytes of one fused adjoint launch over one column slice: read alpha_m, alpha_{m+1},
-    beta_{m+1}, beta_{m+2}, write alpha_{m-1}, beta_m (6 vectors of the slice), H once (entries +
-    4-byte column index), row_ptr, and the FP64 complex D accumulator read + write."""
-    cols, entry_bytes = eng_info
-    vec = 6 * N * cols * sv
-    h = nnzb * (b * b * entry_bytes + 4) + 4 * (N // b + 1)
-    d = 2 * nnzb * b * b * 16
+def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
+    """Algorithmic bytes of one adjoint launch (the kernel walks all S columns itself): read alpha_m,
+    alpha_{m+1}, beta_{m+1}, beta_{m+2}, write alpha_{m-1}, beta_m (6 vectors), H once (entries +
+    4-byte column index), row_ptr, and, when the D epilogue is fused, the D accumulator read + write
+    (8 bytes per real: double or float-float)."""
+    vec = 6 * N * S * sv
+    h = nnzb * (b * b * sv + 4) + 4 * (N // b + 1)
+    d = 2 * nnzb * b * b * 16 if fused else 0
     return vec + h + d
+
+
+# DRAM bytes per row of one DS adjoint launch from the ncu capture on the cubic L=32 case
+# (profiles/k_adjoint_step_ds_cubic32.md: 1.253 GB read + 0.508 GB written for 65,536 rows);
+# traffic grows in proportion to the rows, so the L=64 launch's traffic is this times N.
+ADJ_DS_TRAFFIC_PER_ROW = (1.252655e9 + 0.507823e9) / 65536
 
 
 # ---------------------------------------------------------------------------- arms
@@ -193,28 +199,17 @@ def run_gb300(args, rank, ws, dist):
     mu = eng.fetch_moments(M)
     eng.fetch_D(D)
 
-    # roofline of the dominant kernel (fused adjoint step)
+    # roofline of the dominant kernel (the adjoint step)
     n_adj, t_adj = prof[1]
     n_step, t_step = prof[0]
-    P = S   # complex FP64-class: one element per 16-byte packet; DS/FP64 entries 16 B, FP32 8 B
     sv = 8 if args.precision == "fp32" else 16
-    np_opt = eng.get_option(Lb.FK_OPT_NP)
-    epp = 16 // sv
-    packets = (S + epp - 1) // epp
-    slice_packets = min(packets, 32 * np_opt) if packets > 32 else packets
-    slices = (packets + slice_packets - 1) // slice_packets
-    cols = S / slices
-    bytes_adj = adjoint_bytes_per_launch((cols, sv), N, H.n_blocks() + 0, 2, sv)
+    fuse_opt = eng.get_option(Lb.FK_OPT_FUSE_D)
+    fused = fuse_opt == 1 or (fuse_opt == 2 and args.precision != "ds")
+    bytes_adj = adjoint_bytes_per_launch(N, S, H.n_blocks(), 2, sv, fused)
     avg_adj_ms = t_adj / max(n_adj, 1)
     achieved = bytes_adj / (avg_adj_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "adjoint_traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get(args.precision)
-        except Exception:
-            traffic = None
+    traffic = ADJ_DS_TRAFFIC_PER_ROW * N if (args.precision == "ds" and S == 256 and not fused) else None
     launches = sum(v[0] for v in prof.values())
 
     # ---- end to end through the public API with pinned host buffers ----
@@ -284,7 +279,7 @@ def run_gb300(args, rank, ws, dist):
     eng.close()
     return dict(value=value, ms=ms_max, clocks=clk.summary(), prof=prof, achieved=achieved, peak=peak,
                 peak_kind=peak_kind, traffic=traffic, launches=launches, e2e=e2e, err=err, N=N, S=S, M=M,
-                nnzb=H.n_blocks(), mu0=float(mu[0]), bytes_adj=bytes_adj, slices=slices, avg_adj_ms=avg_adj_ms,
+                nnzb=H.n_blocks(), mu0=float(mu[0]), bytes_adj=bytes_adj, fused=fused, avg_adj_ms=avg_adj_ms,
                 avg_step_ms=t_step / max(n_step, 1), n_adj=n_adj, n_step=n_step)
 
 
@@ -692,7 +687,9 @@ def main():
                    "l2": "inputs larger than L2 (2 GiB per vector), no flush"},
         "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
                      "frac": r["achieved"] / r["peak"], "traffic": r["traffic"],
-                     "kernel": "k_adjoint_step (fused reverse-mode step + D epilogue)",
+                     "kernel": "k_adjoint_step (reverse-mode step, both recursions%s)" % (
+                         " + fused D epilogue" if r["fused"] else "; D outer product in k_outer"),
+                     "traffic_source": "ncu capture of the L=32 case scaled by rows (profiles/)" if r["traffic"] else None,
                      "peak_source": r["peak_kind"], "bytes_per_launch": r["bytes_adj"],
                      "avg_launch_ms": r["avg_adj_ms"], "launches": r["n_adj"]},
         "cpu_baseline": cpu,
@@ -702,7 +699,7 @@ def main():
         "err_vs_fp64": r["err"],
         "kernels": {"step_avg_ms": r["avg_step_ms"], "step_launches": r["n_step"],
                     "adjoint_avg_ms": r["avg_adj_ms"], "adjoint_launches": r["n_adj"],
-                    "column_slices": r["slices"]},
+                    "d_epilogue_fused": r["fused"]},
     }
     print(json.dumps(line), flush=True)
 
