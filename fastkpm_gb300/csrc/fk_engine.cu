@@ -110,6 +110,8 @@ struct fk_engine {
     // R upload: a copy stream and events so the next chunk's host-to-device copy overlaps
     // the layout kernel of the current one (two halves of d_stage)
     cudaStream_t copy_stream = nullptr;
+    int pageable_access = 0;   // the GPU reads any host memory (cudaDevAttrPageableMemoryAccess)
+    int opt_upload = 0;        // FK_OPT_UPLOAD: 0 read device-readable host R directly, 1 staging copies
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
@@ -1247,6 +1249,10 @@ int fk_engine_create(int device, int kind, int precision, fk_engine** out) {
     e->cplx = kind;
     e->prec = precision;
     cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaDeviceGetAttribute(&e->pageable_access, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        cudaGetLastError();
+        e->pageable_access = 0;
+    }
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete e;
@@ -1337,6 +1343,10 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             e->opt_graphs = value ? 1 : 0;
             if (!e->opt_graphs) drop_graphs(e);
             return FK_OK;
+        case FK_OPT_UPLOAD:
+            if (value < 0 || value > 1) return e->fail(FK_ERR_ARG, "UPLOAD must be 0 or 1");
+            e->opt_upload = value;
+            return FK_OK;
         case FK_OPT_TMA:
             if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "TMA must be 0, 1 or 2");
             e->opt_tma = value;
@@ -1360,6 +1370,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_CTAS_PER_SM: *value = e->opt_ctas_per_sm; return FK_OK;
         case FK_OPT_STAGE_H: *value = e->opt_stage; return FK_OK;
         case FK_OPT_GRAPHS: *value = e->opt_graphs; return FK_OK;
+        case FK_OPT_UPLOAD: *value = e->opt_upload; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }
@@ -1395,6 +1406,21 @@ int fk_engine_set_H(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, 
     return configure(e);
 }
 
+namespace {
+// Device address through which kernels can read the host buffer [R, R + bytes), or null.
+const double* device_readable(const fk_engine* e, const double* R, size_t bytes) {
+    if (e->pageable_access) return R;
+    cudaPointerAttributes a0, a1;
+    if (cudaPointerGetAttributes(&a0, R) != cudaSuccess || cudaPointerGetAttributes(&a1, (const char*)R + bytes - 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer) return nullptr;
+    if ((const char*)a1.devicePointer - (const char*)a0.devicePointer != (ptrdiff_t)(bytes - 1)) return nullptr;
+    return reinterpret_cast<const double*>(a0.devicePointer);
+}
+}  // namespace
+
 int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
     if (!e) return FK_ERR_ARG;
     cudaSetDevice(e->device);
@@ -1410,9 +1436,20 @@ int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
     if (rc != FK_OK) return rc;
     FK_TRY(cudaMemsetAsync(e->d_R.p, 0, e->vec_bytes(), e->stream), "clear R");
     for (auto& v : e->d_V) FK_TRY(cudaMemsetAsync(v.p, 0, e->vec_bytes(), e->stream), "clear work vector");
-    // upload in column chunks of at most ~128 MiB through two staging halves: the copy of
-    // chunk q+1 (copy stream) overlaps the layout kernel of chunk q (engine stream)
     const size_t col_bytes = sizeof(double) * (size_t)n * (e->cplx ? 2 : 1);
+    // R the GPU can read in place (pinned, or any host memory where the GPU walks the host's
+    // page tables): the layout kernel reads it directly, no staging copy
+    const double* direct = e->opt_upload == 0 ? device_readable(e, R, col_bytes * s) : nullptr;
+    if (direct) {
+        ProfScope ps(e, fk::kHelper);
+        FK_TRY(prec_load_colmajor(e, direct, n, s, 0, e->d_R.p), "R layout kernel");
+        FK_TRY(cudaStreamSynchronize(e->stream), "set_R");
+        e->mom_M = 0;
+        e->mom_a0 = e->mom_a1 = -2;
+        return configure(e);
+    }
+    // otherwise upload in column chunks of at most ~128 MiB through two staging halves: the
+    // copy of chunk q+1 (copy stream) overlaps the layout kernel of chunk q (engine stream)
     const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)s, (128u << 20) / col_bytes));
     const size_t half = col_bytes * chunk;
     FK_TRY(e->d_stage.ensure(2 * half), "alloc staging buffer");

@@ -1,6 +1,8 @@
 // fk_inst.cuh -- instantiates every kernel of one precision (included once per
 // fk_inst_<prec>.cu with FK_PREC_NAME, FK_SYS_R and FK_SYS_C defined).
 #pragma once
+#include <algorithm>
+
 #include "fk_dispatch.h"
 
 namespace fk {
@@ -100,9 +102,11 @@ static int helper_grid(long long work) {
 
 cudaError_t FK_CAT(launch_load_colmajor, FK_PREC_NAME)(int cplx, const double* src, long long n, int ncols, int c0,
                                                      long long ld, void* dst, cudaStream_t st) {
-    const int g = helper_grid(n * ncols);
-    if (cplx) k_load_colmajor<FK_SYS_C><<<g, 256, 0, st>>>(src, n, ncols, c0, ld, reinterpret_cast<FK_SYS_C::E*>(dst));
-    else k_load_colmajor<FK_SYS_R><<<g, 256, 0, st>>>(src, n, ncols, c0, ld, reinterpret_cast<FK_SYS_R::E*>(dst));
+    const long long tiles = ((n + kTransposeTile - 1) / kTransposeTile) * ((ncols + kTransposeTile - 1) / kTransposeTile);
+    const int g = (int)std::max<long long>(1, std::min<long long>(tiles, 152LL * 8));
+    const dim3 blk(kTransposeTile, 8);
+    if (cplx) k_load_colmajor<FK_SYS_C><<<g, blk, 0, st>>>(src, n, ncols, c0, ld, reinterpret_cast<FK_SYS_C::E*>(dst));
+    else k_load_colmajor<FK_SYS_R><<<g, blk, 0, st>>>(src, n, ncols, c0, ld, reinterpret_cast<FK_SYS_R::E*>(dst));
     return cudaGetLastError();
 }
 cudaError_t FK_CAT(launch_store_colmajor, FK_PREC_NAME)(int cplx, const void* src, long long n, int ncols, long long ld,

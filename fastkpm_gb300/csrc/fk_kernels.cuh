@@ -686,18 +686,36 @@ __global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
 // Small helpers
 // ---------------------------------------------------------------------------------
 
-// Column-major double (or interleaved complex double) n x ncols host block, already
-// on the device, -> row-major device vector columns [c0, c0+ncols) in system S.
+// Column-major double (or interleaved complex double) n x ncols block -> row-major vector
+// columns [c0, c0+ncols) in system S. src is device memory or host memory the GPU can read
+// (pinned, or any host memory on systems with pageable-memory access). 32 x 32 tiles are
+// transposed through shared memory so that both the column reads and the row writes are
+// contiguous across a warp (launched with 32 x 8 threads).
+constexpr int kTransposeTile = 32;
 template <class S>
 __global__ void k_load_colmajor(const double* src, long long n, int ncols, int c0, long long ld, typename S::E* dst) {
-    const long long total = n * (long long)ncols;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-        // q walks the destination row-major so that stores are coalesced
-        const long long r = q / ncols;
-        const int c = (int)(q - r * ncols);
-        const long long sidx = (long long)c * n + r;
-        double2 v = S::CPLX ? make_double2(src[2 * sidx], src[2 * sidx + 1]) : make_double2(src[sidx], 0.0);
-        dst[r * ld + c0 + c] = S::from_double2(v);
+    constexpr int T = kTransposeTile;
+    __shared__ double2 tile[T][T + 1];
+    const long long ntr = (n + T - 1) / T;
+    const int ntc = (ncols + T - 1) / T;
+    for (long long tt = blockIdx.x; tt < ntr * ntc; tt += gridDim.x) {
+        const long long r0 = (tt / ntc) * T;
+        const int cc0 = (int)(tt % ntc) * T;
+        for (int j = threadIdx.y; j < T; j += blockDim.y) {
+            const int c = cc0 + j;
+            const long long r = r0 + threadIdx.x;
+            if (c < ncols && r < n) {
+                const long long sidx = (long long)c * n + r;
+                tile[j][threadIdx.x] = S::CPLX ? make_double2(src[2 * sidx], src[2 * sidx + 1]) : make_double2(src[sidx], 0.0);
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.y; j < T; j += blockDim.y) {
+            const long long r = r0 + j;
+            const int c = cc0 + threadIdx.x;
+            if (c < ncols && r < n) dst[r * ld + c0 + c] = S::from_double2(tile[threadIdx.x][j]);
+        }
+        __syncthreads();
     }
 }
 

@@ -82,6 +82,9 @@ int  fk_engine_synchronize(fk_engine* e);
                                 * fit shared memory, 1 stages them with TMA bulk copies (mbarrier completion),
                                 * 2 with per-thread 16-byte cp.async copies; reading the option returns the mode
                                 * in use                                                                         */
+#define FK_OPT_UPLOAD      9   /* set_R: 0 (default) the layout kernel reads R in place when the GPU can (pinned
+                                * memory, or any host memory on systems with pageable-memory access); 1 always
+                                * copy through device staging buffers                                          */
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 

@@ -18,6 +18,7 @@
 #include <functional>
 #include <random>
 #include <thread>
+#include <type_traits>
 #include <vector>
 #include <sched.h>
 
@@ -473,6 +474,57 @@ int moments2_v1(Engine<T>& e, int M, int n_b, int b, const int* rp1, const int* 
     return 0;
 }
 
+// moments2_v2 (src/engine_cpu.cpp:162-209): A_i = R^dag T_i(Hs) j2 R2, B_i = R2^dag T_i(Hs) j1 R
+// (s x s each, arma::trans is the conjugate transpose), mu[m1][m2] = sum_k A_m1.row(k) . B_m2.col(k)
+// (arma::dot, no conjugation) = tr(A_m1 B_m2). R2: n x s row-major like R.
+template <typename T>
+int moments2_v2(Engine<T>& e, int M, int n_b, int b, const int* rp1, const int* ci1, const T* v1, const int* rp2,
+                const int* ci2, const T* v2, const std::vector<T>& R2, cx* mu) {
+    const int n = e.n, s = e.s;
+    if (M < 2 || M % 2 != 0 || n == 0 || n_b * b != n || e.Hs.n_b != n_b || e.Hs.b != b) return 1;
+    const Bsr<T>& H = e.Hs;
+    // projected s x s matrices, row-major [k][l]
+    std::vector<cx> Ap(size_t(M) * s * s), Bp(size_t(M) * s * s);
+    auto run = [&](const std::vector<T>& start, const int* rp, const int* ci, const T* v, const std::vector<T>& proj,
+                   std::vector<cx>& out) {
+        std::vector<T> X0(size_t(n) * s), X1(size_t(n) * s), X2(size_t(n) * s), col(n), y(n);
+        for (int k = 0; k < s; k++) {   // X0 = j start, column by column
+            for (int i = 0; i < n; i++) col[i] = start[size_t(i) * s + k];
+            bsr_spmv(n_b, b, rp, ci, v, col.data(), y.data());
+            for (int i = 0; i < n; i++) X0[size_t(i) * s + k] = y[i];
+        }
+        auto project = [&](const std::vector<T>& X, int m) {   // out[m] = proj^dag X
+            parallel_ranges(e.nthreads, s, [&](int, long k0, long k1) {
+                for (long k = k0; k < k1; k++)
+                    for (int l = 0; l < s; l++) {
+                        cx acc = 0;
+                        for (int i = 0; i < n; i++) acc += cx(conj_(proj[size_t(i) * s + k]) * X[size_t(i) * s + l]);
+                        out[(size_t(m) * s + k) * s + l] = acc;
+                    }
+            });
+        };
+        project(X0, 0);
+        e.spmm(1.0, H, X0, 0.0, nullptr, X1);
+        if (M > 1) project(X1, 1);
+        for (int m = 2; m < M; m++) {
+            e.spmm(2.0, H, X1, -1.0, &X0, X2);
+            project(X2, m);
+            std::swap(X0, X1);
+            std::swap(X1, X2);
+        }
+    };
+    run(R2, rp2, ci2, v2, e.R, Ap);   // A_i = R^dag T_i j2 R2
+    run(e.R, rp1, ci1, v1, R2, Bp);   // B_i = R2^dag T_i j1 R
+    for (int m1 = 0; m1 < M; m1++)
+        for (int m2 = 0; m2 < M; m2++) {
+            cx acc = 0;
+            for (int k = 0; k < s; k++)
+                for (int l = 0; l < s; l++) acc += Ap[(size_t(m1) * s + k) * s + l] * Bp[(size_t(m2) * s + l) * s + k];
+            mu[size_t(m1) * M + m2] = acc;
+        }
+    return 0;
+}
+
 }  // namespace
 
 struct orc_engine {
@@ -538,6 +590,26 @@ int orc_moments2_v1(orc_engine* e, int M, int n_b, int b, const int* rp1, const 
         return moments2_v1(e->ec, M, n_b, b, rp1, ci1, reinterpret_cast<const cx*>(v1), rp2, ci2,
                            reinterpret_cast<const cx*>(v2), out);
     return moments2_v1(e->er, M, n_b, b, rp1, ci1, v1, rp2, ci2, v2, out);
+}
+
+int orc_moments2_v2(orc_engine* e, int M, int n_b, int b, const int* rp1, const int* ci1, const double* v1,
+                    const int* rp2, const int* ci2, const double* v2, const double* R2, double* mu) {
+    cx* out = reinterpret_cast<cx*>(mu);
+    auto load = [&](auto& eng, const auto* src) {   // column-major n x s -> row-major, or R itself
+        using TT = typename std::decay<decltype(eng.R)>::type::value_type;
+        std::vector<TT> r2(eng.R.size());
+        if (!src) return eng.R;
+        for (int j = 0; j < eng.s; j++)
+            for (int i = 0; i < eng.n; i++) r2[size_t(i) * eng.s + j] = src[size_t(j) * eng.n + i];
+        return r2;
+    };
+    if (e->cplx) {
+        const auto r2 = load(e->ec, reinterpret_cast<const cx*>(R2));
+        return moments2_v2(e->ec, M, n_b, b, rp1, ci1, reinterpret_cast<const cx*>(v1), rp2, ci2,
+                           reinterpret_cast<const cx*>(v2), r2, out);
+    }
+    const auto r2 = load(e->er, R2);
+    return moments2_v2(e->er, M, n_b, b, rp1, ci1, v1, rp2, ci2, v2, r2, out);
 }
 
 int orc_energy_scale(orc_engine* e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,

@@ -84,6 +84,10 @@ double orc_moment_product(int M, const double* c, const double* mu);
  * sum_k cdot(T_m1(Hs) r_k, j2 T_m2(Hs) j1 r_k); j1, j2 BSR with H's block structure, unscaled */
 int    orc_moments2_v1(orc_engine* e, int M, int n_b, int b, const int* rp1, const int* ci1, const double* v1,
                        const int* rp2, const int* ci2, const double* v2, double* mu);
+/* moments2_v2 (src/engine_cpu.cpp:162-209): mu[m1*M + m2] = tr(A_m1 B_m2), A_i = R^dag T_i j2 R2,
+ * B_i = R2^dag T_i j1 R; R2 column-major n x s like R, or NULL for R2 = R */
+int    orc_moments2_v2(orc_engine* e, int M, int n_b, int b, const int* rp1, const int* ci1, const double* v1,
+                       const int* rp2, const int* ci2, const double* v2, const double* R2, double* mu);
 /* electrical_conductivity_coefficients, direct-sum branch (src/fastkpm.cpp:80-233):
  * out[2*(m1*M + m2) + {0,1}]; 1 on the reference's assertion failures */
 int    orc_electrical_conductivity_coefficients(int M, int Mq, double kT, double mu, double omega, double lo,

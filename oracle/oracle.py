@@ -43,6 +43,7 @@ _SIG = {
     "orc_moment_product": (_d, [_i, _dp, _dp]),
     "orc_moment_transform": (None, [_i, _dp, _i, _dp]),
     "orc_moments2_v1": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _ip, _ip, _dp, _dp]),
+    "orc_moments2_v2": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _ip, _ip, _dp, _dp, _dp]),
     "orc_electrical_conductivity_coefficients": (_i, [_i, _i, _d, _d, _d, _d, _d, _dp, _dp]),
     "orc_mu_to_filling": (_d, [_i, _dp, _d, _d, _d, _d]),
     "orc_filling_to_mu": (_d, [_i, _dp, _d, _d, _d, _d, _d]),
@@ -144,6 +145,23 @@ class OracleEngine:
                                    _ip_(j2.row_ptr), _ip_(j2.col_idx), _dp_(v2), _dp_(out))
         if st:
             raise RuntimeError("orc_moments2_v1: status %d" % st)
+        return out.view(np.complex128).reshape(M, M)
+
+    def moments2_v2(self, M, j1, j2, R2=None):
+        """mu[m1, m2] = tr(A_m1 B_m2), A_i = R^dag T_i j2 R2, B_i = R2^dag T_i j1 R
+        (src/engine_cpu.cpp:162-209), (M, M) complex; R2 = R when None."""
+        out = np.zeros(2 * M * M)
+        v1 = _dbl(j1.val)
+        v2 = _dbl(j2.val)
+        r2 = None
+        if R2 is not None:
+            dt = np.complex128 if self.cplx else np.float64
+            r2 = _dbl(np.ascontiguousarray(np.asarray(R2, dt).reshape(-1, order="F")))
+        st = lib().orc_moments2_v2(self.h, M, j1.n_rows, j1.b_len, _ip_(j1.row_ptr), _ip_(j1.col_idx), _dp_(v1),
+                                   _ip_(j2.row_ptr), _ip_(j2.col_idx), _dp_(v2),
+                                   _dp_(r2) if r2 is not None else None, _dp_(out))
+        if st:
+            raise RuntimeError("orc_moments2_v2: status %d" % st)
         return out.view(np.complex128).reshape(M, M)
 
     def energy_scale(self, H, extend, iters, v0):

@@ -284,6 +284,31 @@ def test_permutation_invariance(gpu, prec):
     eng.close()
 
 
+@pytest.mark.parametrize("cplx", [False, True])
+def test_upload_paths_agree(gpu, cplx):
+    """set_R through staging copies (FK_OPT_UPLOAD 1) and read in place (0, from ordinary and
+    from page-locked host memory) give the same device R, bit for bit."""
+    H, es, R = small_complex_case(4, 16, 17) if cplx else small_real_case(9, 37, 17)
+    lib = L.load()
+    outs = []
+    for upload, pin in [(1, False), (0, False), (0, True)]:
+        eng = fk.Engine(cplx, "fp64")
+        eng.set_option(L.FK_OPT_UPLOAD, upload)
+        assert eng.get_option(L.FK_OPT_UPLOAD) == upload
+        eng.set_H(H, es)
+        Rh = np.asfortranarray(R.copy())
+        if pin:
+            assert lib.fk_host_register(Rh.ctypes.data, Rh.nbytes) == L.FK_OK
+        eng.set_R(Rh)
+        outs.append((eng.get_R(), eng.moments(20)))
+        if pin:
+            lib.fk_host_unregister(Rh.ctypes.data)
+        eng.close()
+    for Rg, mu in outs:
+        assert np.array_equal(Rg, R)
+        assert np.array_equal(mu, outs[0][1])
+
+
 def test_results_are_deterministic(gpu):
     H, es, R = small_complex_case(6, 32, 2)
     eng = fk.Engine(True, "ds")

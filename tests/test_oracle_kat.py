@@ -297,3 +297,26 @@ def test_moments2_v1_identity_probes_is_trace():
     J1, J2 = j1.to_dense(), j2.to_dense()
     ref = np.array([[np.trace(J1 @ T[a] @ J2 @ T[b]) for b in range(M)] for a in range(M)])
     assert np.max(np.abs(mu - ref)) <= 1e-11 * np.max(np.abs(ref))
+
+
+def test_moments2_v2_identity_probes_is_trace():
+    # R = R2 = identity: A_i = T_i j2, B_i = T_i j1, tr(A_m1 B_m2) = tr(j1 T_m1 j2 T_m2)
+    H, es, _ = W.cubic_spin_lattice(2, -1.0, 1.0, seed=7)
+    n = H.n_rows * H.b_len
+    A = dense_Hs(H, es)
+    rng = np.random.default_rng(8)
+
+    def rand_op():
+        return SpMatBsr.build(H.n_rows, 2, H.row_idx, H.col_idx,
+                              rng.standard_normal((len(H.row_idx), 4)) + 1j * rng.standard_normal((len(H.row_idx), 4)))
+    j1, j2 = rand_op(), rand_op()
+    e = O.OracleEngine(True, nthreads=2)
+    e.set_H(H, es)
+    e.set_R(O.R_identity(n, complex_values=True))
+    M = 6
+    T = _dense_cheb(A, M)
+    J1, J2 = j1.to_dense(), j2.to_dense()
+    ref = np.array([[np.trace(J1 @ T[a] @ J2 @ T[b]) for b in range(M)] for a in range(M)])
+    assert np.max(np.abs(e.moments2_v2(M, j1, j2) - ref)) <= 1e-11 * np.max(np.abs(ref))
+    # an explicit R2 equal to R gives the same
+    assert np.max(np.abs(e.moments2_v2(M, j1, j2, O.R_identity(n, complex_values=True)) - ref)) <= 1e-11 * np.max(np.abs(ref))
