@@ -54,6 +54,7 @@ SIGNATURES = {
     "fk_engine_expansion_coefficients": (_i, [_p, _i, _i, _i, _d, _d, _d, _d, _dp]),
     "fk_engine_kpm_filling": (_i, [_p, _i, _d, _d, _d, _dp, _dp]),
     "fk_engine_moments2_v1": (_i, [_p, _i, _i, _ip, _ip, _dp, _i, _ip, _ip, _dp, _i, _i, _dp]),
+    "fk_engine_moments2_v2": (_i, [_p, _i, _i, _ip, _ip, _dp, _i, _ip, _ip, _dp, _dp, _dp]),
     "fk_engine_solve_filling": (_i, [_p, _i, _i, _d, _d, _d, _i, _i, _ip, _ip, _dp, _dp, _dp]),
     "fk_engine_set_profiling": (_i, [_p, _i]),
     "fk_engine_profile_read": (_i, [_p, _i, C.POINTER(C.c_longlong), _dp]),

@@ -120,7 +120,7 @@ struct fk_engine {
     // double panels of Chebyshev vectors, a scratch vector, the M x M result; cuBLAS reduces
     struct Op { DevBuf row_ptr, colc, hval; };
     Op d_j[2];
-    DevBuf d_panel[2], d_tmp, d_mu2;
+    DevBuf d_panel[2], d_tmp, d_mu2, d_R2;
     cublasHandle_t blas = nullptr;
     std::vector<double> h_raw;
 
@@ -1282,6 +1282,7 @@ int fk_engine_destroy(fk_engine* e) {
     for (auto& pb : e->d_panel) pb.release();
     e->d_tmp.release();
     e->d_mu2.release();
+    e->d_R2.release();
     DevBuf* bufs[] = {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2], &e->d_V[3],
                       &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc, &e->d_partials, &e->d_raw,
                       &e->d_coef, &e->d_stage, &e->d_post, &e->d_t_uoff, &e->d_t_ucol, &e->d_t_own, &e->d_t_kslot,
@@ -1421,35 +1422,20 @@ const double* device_readable(const fk_engine* e, const double* R, size_t bytes)
 }
 }  // namespace
 
-int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
-    if (!e) return FK_ERR_ARG;
-    cudaSetDevice(e->device);
-    if (n <= 0) return e->fail(FK_ERR_ARG, "set_R: n must be positive");
-    if (s <= 0) return e->fail(FK_ERR_ARG, "set_R: cannot handle an empty R (s = %d)", s);
-    if (!R) return e->fail(FK_ERR_ARG, "set_R: null R");
-    const int epp = e->epp();
-    e->n = n;
-    e->s = s;
-    e->ld = ((long long)s + epp - 1) / epp * epp;
-    e->P = (int)(e->ld / epp);
-    int rc = ensure_vectors(e);
-    if (rc != FK_OK) return rc;
-    FK_TRY(cudaMemsetAsync(e->d_R.p, 0, e->vec_bytes(), e->stream), "clear R");
-    for (auto& v : e->d_V) FK_TRY(cudaMemsetAsync(v.p, 0, e->vec_bytes(), e->stream), "clear work vector");
+namespace {
+// Column-major n x s host block -> row-major engine vector dst (n x ld, padding already zero),
+// synchronously. A host buffer the GPU can read is read in place by the layout kernel;
+// otherwise it goes through two staging halves: the copy of chunk q+1 (copy stream)
+// overlaps the layout kernel of chunk q (engine stream).
+int upload_colmajor(fk_engine* e, const double* src, int n, int s, void* dst) {
     const size_t col_bytes = sizeof(double) * (size_t)n * (e->cplx ? 2 : 1);
-    // R the GPU can read in place (pinned, or any host memory where the GPU walks the host's
-    // page tables): the layout kernel reads it directly, no staging copy
-    const double* direct = e->opt_upload == 0 ? device_readable(e, R, col_bytes * s) : nullptr;
+    const double* direct = e->opt_upload == 0 ? device_readable(e, src, col_bytes * s) : nullptr;
     if (direct) {
         ProfScope ps(e, fk::kHelper);
-        FK_TRY(prec_load_colmajor(e, direct, n, s, 0, e->d_R.p), "R layout kernel");
-        FK_TRY(cudaStreamSynchronize(e->stream), "set_R");
-        e->mom_M = 0;
-        e->mom_a0 = e->mom_a1 = -2;
-        return configure(e);
+        FK_TRY(prec_load_colmajor(e, direct, n, s, 0, dst), "layout kernel");
+        FK_TRY(cudaStreamSynchronize(e->stream), "upload");
+        return FK_OK;
     }
-    // otherwise upload in column chunks of at most ~128 MiB through two staging halves: the
-    // copy of chunk q+1 (copy stream) overlaps the layout kernel of chunk q (engine stream)
     const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)s, (128u << 20) / col_bytes));
     const size_t half = col_bytes * chunk;
     FK_TRY(e->d_stage.ensure(2 * half), "alloc staging buffer");
@@ -1467,15 +1453,36 @@ int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
         const int nc = std::min(chunk, s - c0);
         char* buf = e->d_stage.as<char>() + q * half;
         FK_TRY(cudaStreamWaitEvent(e->copy_stream, e->ev_consumed[q], 0), "upload order");
-        FK_TRY(cudaMemcpyAsync(buf, (const char*)R + col_bytes * c0, col_bytes * nc, cudaMemcpyHostToDevice,
-                               e->copy_stream), "upload R");
+        FK_TRY(cudaMemcpyAsync(buf, (const char*)src + col_bytes * c0, col_bytes * nc, cudaMemcpyHostToDevice,
+                               e->copy_stream), "upload");
         FK_TRY(cudaEventRecord(e->ev_copied[q], e->copy_stream), "upload order");
         FK_TRY(cudaStreamWaitEvent(e->stream, e->ev_copied[q], 0), "upload order");
         ProfScope ps(e, fk::kHelper);
-        FK_TRY(prec_load_colmajor(e, reinterpret_cast<const double*>(buf), n, nc, c0, e->d_R.p), "R layout kernel");
+        FK_TRY(prec_load_colmajor(e, reinterpret_cast<const double*>(buf), n, nc, c0, dst), "layout kernel");
         FK_TRY(cudaEventRecord(e->ev_consumed[q], e->stream), "upload order");
     }
-    FK_TRY(cudaStreamSynchronize(e->stream), "set_R");
+    FK_TRY(cudaStreamSynchronize(e->stream), "upload");
+    return FK_OK;
+}
+}  // namespace
+
+int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    if (n <= 0) return e->fail(FK_ERR_ARG, "set_R: n must be positive");
+    if (s <= 0) return e->fail(FK_ERR_ARG, "set_R: cannot handle an empty R (s = %d)", s);
+    if (!R) return e->fail(FK_ERR_ARG, "set_R: null R");
+    const int epp = e->epp();
+    e->n = n;
+    e->s = s;
+    e->ld = ((long long)s + epp - 1) / epp * epp;
+    e->P = (int)(e->ld / epp);
+    int rc = ensure_vectors(e);
+    if (rc != FK_OK) return rc;
+    FK_TRY(cudaMemsetAsync(e->d_R.p, 0, e->vec_bytes(), e->stream), "clear R");
+    for (auto& v : e->d_V) FK_TRY(cudaMemsetAsync(v.p, 0, e->vec_bytes(), e->stream), "clear work vector");
+    rc = upload_colmajor(e, R, n, s, e->d_R.p);
+    if (rc != FK_OK) return rc;
     e->mom_M = 0;
     e->mom_a0 = e->mom_a1 = -2;
     return configure(e);
@@ -1546,6 +1553,123 @@ int fk_engine_fetch_D(fk_engine* e, double* D) {
     if (!e || !D) return FK_ERR_ARG;
     cudaSetDevice(e->device);
     return fetch_D(e, D);
+}
+
+namespace {
+// moments2_v2 (reference src/engine_cpu.cpp:162-209; the reference's GPU engine exits there,
+// src/engine_cusparse.cpp:904-908): with X_i = T_i(Hs) j2 R2 and Y_i = T_i(Hs) j1 R,
+//   A_i = R^dag X_i,  B_i = R2^dag Y_i  (s x s),  mu[m1][m2] = tr(A_m1 B_m2).
+// Per order i the vector is exported as a double panel and projected by one GEMM:
+//   At_i = X_i^T conj(R)  (= A_i transposed),  E_i = R2^T conj(Y_i)  (= conj(B_i)),
+// then mu (row-major) = E^H At over the stacked ld^2-long columns, one more GEMM.
+int moments2_v2(fk_engine* e, int M, const int* nnzb, const int* const* rp, const int* const* ci,
+                const double* const* val, const double* R2_host, double* mu_out) {
+    if (M < 2 || M % 2 != 0) return e->fail(FK_ERR_ARG, "moments2_v2: M must be even and >= 2 (got %d)", M);
+    int rc = require_ready(e);
+    if (rc != FK_OK) return rc;
+    for (int q = 0; q < 2; q++) {
+        rc = m2_upload_op(e, q, nnzb[q], rp[q], ci[q], val[q]);
+        if (rc != FK_OK) return rc;
+    }
+    const long long ld = e->ld, L = (long long)e->n * ld, ld2 = ld * ld;
+    if (L >= (1LL << 31) || (long long)M * ld2 >= (1LL << 31))
+        return e->fail(FK_ERR_UNSUPPORTED, "moments2_v2: too many rows or probe columns for the GEMM sizes");
+    const size_t elt = e->cplx ? 16 : 8;
+    void* R2 = e->d_R.p;
+    if (R2_host) {
+        FK_TRY(e->d_R2.ensure(e->vec_bytes()), "alloc R2");
+        FK_TRY(cudaMemsetAsync(e->d_R2.p, 0, e->vec_bytes(), e->stream), "clear R2");
+        rc = upload_colmajor(e, R2_host, e->n, e->s, e->d_R2.p);
+        if (rc != FK_OK) return rc;
+        R2 = e->d_R2.p;
+    }
+    FK_TRY(e->d_panel[0].ensure(3 * (size_t)L * elt), "alloc panels");
+    FK_TRY(e->d_panel[1].ensure(2 * (size_t)M * ld2 * elt), "alloc projections");
+    FK_TRY(e->d_mu2.ensure((size_t)M * M * elt), "alloc moments");
+    double* Xp = e->d_panel[0].as<double>();
+    double* Rp = Xp + (size_t)L * (elt / 8);
+    double* R2p = Rp + (size_t)L * (elt / 8);
+    char* At = e->d_panel[1].as<char>();
+    char* Ep = At + (size_t)M * ld2 * elt;
+    FK_TRY(prec_export(e, e->d_R.p, 0, (int)ld, Rp), "export R");
+    FK_TRY(prec_export(e, R2, 0, (int)ld, R2p), "export R2");
+    if (!e->blas) {
+        const cublasStatus_t st = cublasCreate(&e->blas);
+        if (st != CUBLAS_STATUS_SUCCESS) { e->blas = nullptr; return blas_fail(e, st, "cublasCreate"); }
+    }
+    cublasStatus_t bst = cublasSetStream(e->blas, e->stream);
+    if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "cublasSetStream");
+    const M2Mat hs{e->d_row_ptr.as<int>(), e->d_colc.as<unsigned>(), e->d_hval.p};
+    const M2Mat j1{e->d_j[0].row_ptr.as<int>(), e->d_j[0].colc.as<unsigned>(), e->d_j[0].hval.p};
+    const M2Mat j2{e->d_j[1].row_ptr.as<int>(), e->d_j[1].colc.as<unsigned>(), e->d_j[1].hval.p};
+    const int n_ld = (int)ld;   // projections: ld x ld GEMMs over the n rows
+    for (int side = 0; side < 2; side++) {
+        // side 0: X_i = T_i j2 R2 in V0/V1 -> At_i;  side 1: Y_i = T_i j1 R in V2/V3 -> E_i
+        void* va = e->d_V[2 * side].p;
+        void* vb = e->d_V[2 * side + 1].p;
+        void* prev = nullptr;
+        void* cur = nullptr;
+        for (int m = 0; m < M; m++) {
+            void* y = m == 0 ? va : (m == 1 ? vb : prev);
+            if (m == 0) rc = m2_step(e, side == 0 ? j2 : j1, side == 0 ? R2 : e->d_R.p, nullptr, y, false, 0, e->P);
+            else rc = m2_step(e, hs, cur, m == 1 ? nullptr : prev, y, m > 1, 0, e->P);
+            if (rc != FK_OK) return rc;
+            prev = cur;
+            cur = y;
+            FK_TRY(prec_export(e, cur, 0, n_ld, Xp), "export panel");
+            char* dst = (side == 0 ? At : Ep) + (size_t)m * ld2 * elt;
+            // panels are column-major ld x n (leading dimension ld)
+            if (e->cplx) {
+                const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+                const cuDoubleComplex* a = reinterpret_cast<const cuDoubleComplex*>(side == 0 ? Xp : R2p);
+                const cuDoubleComplex* b = reinterpret_cast<const cuDoubleComplex*>(side == 0 ? Rp : Xp);
+                bst = cublasZgemm(e->blas, CUBLAS_OP_N, CUBLAS_OP_C, n_ld, n_ld, e->n, &one, a, n_ld, b, n_ld, &zero,
+                                  reinterpret_cast<cuDoubleComplex*>(dst), n_ld);
+            } else {
+                const double one = 1.0, zero = 0.0;
+                bst = cublasDgemm(e->blas, CUBLAS_OP_N, CUBLAS_OP_T, n_ld, n_ld, e->n, &one, side == 0 ? Xp : R2p, n_ld,
+                                  side == 0 ? Rp : Xp, n_ld, &zero, reinterpret_cast<double*>(dst), n_ld);
+            }
+            if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "moments2_v2 projection");
+        }
+    }
+    // mu^T (column-major M x M) = mu row-major: (E^H At)(m2, m1) = sum_q conj(E[q, m2]) At[q, m1]
+    if (e->cplx) {
+        const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+        bst = cublasZgemm(e->blas, CUBLAS_OP_C, CUBLAS_OP_N, M, M, (int)ld2, &one, reinterpret_cast<const cuDoubleComplex*>(Ep),
+                          (int)ld2, reinterpret_cast<const cuDoubleComplex*>(At), (int)ld2, &zero,
+                          e->d_mu2.as<cuDoubleComplex>(), M);
+    } else {
+        const double one = 1.0, zero = 0.0;
+        bst = cublasDgemm(e->blas, CUBLAS_OP_T, CUBLAS_OP_N, M, M, (int)ld2, &one, reinterpret_cast<const double*>(Ep),
+                          (int)ld2, reinterpret_cast<const double*>(At), (int)ld2, &zero, e->d_mu2.as<double>(), M);
+    }
+    if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "moments2_v2 trace GEMM");
+    std::vector<double> h((size_t)M * M * (e->cplx ? 2 : 1));
+    FK_TRY(cudaMemcpyAsync(h.data(), e->d_mu2.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
+           "copy moments");
+    FK_TRY(cudaStreamSynchronize(e->stream), "moments2_v2");
+    for (size_t q = 0; q < (size_t)M * M; q++) {   // column-major (m2 + m1 M) of mu^T = row-major mu
+        mu_out[2 * q] = e->cplx ? h[2 * q] : h[q];
+        mu_out[2 * q + 1] = e->cplx ? h[2 * q + 1] : 0.0;
+    }
+    e->mom_M = 0;
+    e->mom_a0 = e->mom_a1 = -2;
+    if (e->profiling) prof_flush(e);
+    return FK_OK;
+}
+}  // namespace
+
+int fk_engine_moments2_v2(fk_engine* e, int M, int j1_nnzb, const int* j1_row_ptr, const int* j1_col_idx,
+                          const double* j1_val, int j2_nnzb, const int* j2_row_ptr, const int* j2_col_idx,
+                          const double* j2_val, const double* R2, double* mu) {
+    if (!e || !mu || !j1_row_ptr || !j2_row_ptr) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    const int nnzb[2] = {j1_nnzb, j2_nnzb};
+    const int* rp[2] = {j1_row_ptr, j2_row_ptr};
+    const int* ci[2] = {j1_col_idx, j2_col_idx};
+    const double* val[2] = {j1_val, j2_val};
+    return moments2_v2(e, M, nnzb, rp, ci, val, R2, mu);
 }
 
 int fk_engine_moments2_v1(fk_engine* e, int M, int j1_nnzb, const int* j1_row_ptr, const int* j1_col_idx,

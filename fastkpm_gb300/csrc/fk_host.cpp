@@ -535,9 +535,30 @@ public:
             }
         return mu;
     }
-    Vec<Vec<cx_double>> moments2_v2(int, SpMatBsr<T> const&, SpMatBsr<T> const&, int, int) override {
-        // the reference's GPU engine exits here too (src/engine_cusparse.cpp:904-908)
-        throw std::runtime_error("fkpm: moments2_v2 is not implemented on the GPU");
+    // R2 must have R's shape (the reference asserts it, src/engine_cpu.cpp:175); an empty R2
+    // means R2 = R. The chunk arguments are unused, as in the reference.
+    Vec<Vec<cx_double>> moments2_v2(int M, SpMatBsr<T> const& j1op, SpMatBsr<T> const& j2op, int, int) override {
+        for (auto* j : {&j1op, &j2op})
+            if (j->n_rows != n_rows_ || j->n_cols != n_rows_ || j->b_len != b_len_)
+                throw std::invalid_argument("moments2_v2: j1 and j2 must have H's shape and block size");
+        const bool own_r2 = this->R2.size() != 0;
+        if (own_r2 && (this->R2.n_rows != this->R.n_rows || this->R2.n_cols != this->R.n_cols))
+            throw std::invalid_argument("moments2_v2: R2 must have R's shape");
+        std::vector<double> v1, v2, r2, out(2 * (size_t)M * M);
+        to_doubles(j1op.val.data(), j1op.val.size(), v1);
+        to_doubles(j2op.val.data(), j2op.val.size(), v2);
+        if (own_r2) to_doubles(this->R2.memptr(), this->R2.size(), r2);
+        check(fk_engine_moments2_v2(e_, M, j1op.n_blocks(), j1op.row_ptr.data(), j1op.col_idx.data(), v1.data(),
+                                    j2op.n_blocks(), j2op.row_ptr.data(), j2op.col_idx.data(), v2.data(),
+                                    own_r2 ? r2.data() : nullptr, out.data()),
+              "moments2_v2");
+        Vec<Vec<cx_double>> mu(M, Vec<cx_double>(M));
+        for (int m1 = 0; m1 < M; m1++)
+            for (int m2 = 0; m2 < M; m2++) {
+                const size_t q = (size_t)m1 * M + m2;
+                mu[m1][m2] = cx_double(out[2 * q], out[2 * q + 1]);
+            }
+        return mu;
     }
 
     void stoch_matrix(Vec<double> const& c, SpMatBsr<T>& D) override {

@@ -441,9 +441,26 @@ class Engine:
                                                    R_chunk_ncols, _dp(out)), "moments2_v1")
         return out.view(np.complex128).reshape(M, M)
 
-    def moments2_v2(self, *a, **k):
-        raise NotImplementedError("moments2_v2 is not implemented on the GPU (the reference's GPU engine exits "
-                                  "there too, src/engine_cusparse.cpp:904-908)")
+    def moments2_v2(self, M, j1, j2, a_chunk_ncols=0, R_chunk_ncols=0):
+        """mu[m1, m2] = tr(A_m1 B_m2), A_i = R^dag T_i j2 R2, B_i = R2^dag T_i j1 R ((M, M) complex;
+        src/engine_cpu.cpp:162-209). R2 is the public attribute (R itself unless replaced); the
+        chunk arguments are accepted for the reference's signature and unused, as there."""
+        dt = np.complex128 if self.complex_values else np.float64
+        v1 = np.ascontiguousarray(j1.val, dtype=dt)
+        v2 = np.ascontiguousarray(j2.val, dtype=dt)
+        r2p = None
+        if self.R2 is not None and self.R2 is not self.R:
+            r2 = np.asarray(self.R2, dtype=dt)
+            if r2.shape != self.R.shape:
+                raise ValueError("R2 must have R's shape")
+            r2f = np.ascontiguousarray(r2.reshape(-1, order="F"))
+            r2p = _dp(r2f.view(np.float64))
+        out = np.zeros(2 * M * M)
+        self._check(self.lib.fk_engine_moments2_v2(self.h, M, j1.n_blocks(), _ip(j1.row_ptr), _ip(j1.col_idx),
+                                                   _dp(v1.view(np.float64)), j2.n_blocks(), _ip(j2.row_ptr),
+                                                   _ip(j2.col_idx), _dp(v2.view(np.float64)), r2p, _dp(out)),
+                    "moments2_v2")
+        return out.view(np.complex128).reshape(M, M)
 
 
 class Batch:

@@ -14,8 +14,8 @@
 //     mk_engine_cpu<T>() and mk_engine_mpi<T>() throw: neither is part of this
 //     build. mk_engine_cuSPARSE<T>(devices) returns the GB300 engine on
 //     devices[0] (device 0 when empty).
-//   * moments2_v1 runs on the GPU; moments2_v2 throws std::runtime_error (the
-//     reference's GPU engine does not implement it either).
+//   * moments2_v1 and moments2_v2 run on the GPU (the reference's GPU engine exits
+//     in moments2_v2); moments2_v2 takes R2 = R when R2 is empty.
 //   * Errors throw std::runtime_error instead of assert/abort/exit.
 //   * set_H(H) (one argument) is added; it takes the energy scale from
 //     energy_scale(H, 0.01).

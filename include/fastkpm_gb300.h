@@ -153,6 +153,16 @@ int  fk_engine_moments2_v1(fk_engine* e, int M, int j1_nnzb, const int* j1_row_p
                            const double* j1_val, int j2_nnzb, const int* j2_row_ptr, const int* j2_col_idx,
                            const double* j2_val, int a_chunk_ncols, int R_chunk_ncols, double* mu);
 
+/* Engine<T>::moments2_v2(M, j1, j2) (reference src/engine_cpu.cpp:162-209; the reference's GPU
+ * engine exits there, src/engine_cusparse.cpp:904-908): with a second probe block R2 (column-
+ * major n x s like R; NULL: R2 = R), A_i = R^dag T_i(Hs) j2 R2 and B_i = R2^dag T_i(Hs) j1 R,
+ * mu[m1][m2] = tr(A_m1 B_m2); mu[2*(m1*M + m2) + {0,1}] = (re, im). Projections and the
+ * trace are FP64 GEMMs (cuBLAS); holds 2 M ld^2 projected values on the device. Overwrites
+ * the recursion state that moments() leaves for autodiff_matrix(). */
+int  fk_engine_moments2_v2(fk_engine* e, int M, int j1_nnzb, const int* j1_row_ptr, const int* j1_col_idx,
+                           const double* j1_val, int j2_nnzb, const int* j2_row_ptr, const int* j2_col_idx,
+                           const double* j2_val, const double* R2, double* mu);
+
 /* KPM post-processing of the last moments(M) on the device, with no host round trip after
  * the moments: gamma = moment_transform(mu, Mq) (reference src/fastkpm.cpp:236-256), the
  * chemical potential mu_F = filling_to_mu(gamma, es, kT, filling, delta_filling) (:413-427:

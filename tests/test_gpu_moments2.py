@@ -110,3 +110,42 @@ def test_moments2_v1_consumes_the_autodiff_state(gpu):
         eng.moments2_v1(7, j1, j2)
     assert ei.value.status == L.FK_ERR_ARG
     eng.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_moments2_v2_matches_oracle(gpu, prec, cplx):
+    """moments2_v2 (the reference's CPU-only variant, src/engine_cpu.cpp:162-209) with R2 = R and
+    with an independent R2, against the oracle."""
+    H, es, R = _case(cplx)
+    j1, j2 = _ops(H, cplx, 11)
+    M = 12
+    eng = fk.Engine(cplx, prec)
+    eng.set_H(H, es)
+    eng.set_R(R)
+    orc = O.OracleEngine(cplx)
+    orc.set_H(H, es)
+    orc.set_R(R)
+    assert _err(eng.moments2_v2(M, j1, j2), orc.moments2_v2(M, j1, j2)) <= TOL[prec]
+    R2 = fk.probe_uncorrelated(R.shape[0], R.shape[1], fk.RNG(5), complex_values=cplx)
+    eng.R2 = R2
+    assert _err(eng.moments2_v2(M, j1, j2), orc.moments2_v2(M, j1, j2, R2)) <= TOL[prec]
+    eng.close()
+
+
+def test_moments2_v2_identity_probes_give_traces(gpu):
+    H, es, _ = W.cubic_spin_lattice(3, -1.0, 1.0, 6)
+    n = H.n_rows * H.b_len
+    j1, j2 = _ops(H, True, 12)
+    A = (H.to_dense() - es.avg() * np.eye(n)) / es.mag()
+    M = 8
+    T = [np.eye(n, dtype=complex), A.astype(complex)]
+    for m in range(2, M):
+        T.append(2 * A @ T[-1] - T[-2])
+    J1, J2 = j1.to_dense(), j2.to_dense()
+    ref = np.array([[np.trace(J1 @ T[a] @ J2 @ T[b]) for b in range(M)] for a in range(M)])
+    eng = fk.Engine(True, "fp64")
+    eng.set_H(H, es)
+    eng.set_R_identity(n)
+    assert _err(eng.moments2_v2(M, j1, j2), ref) <= 1e-11
+    eng.close()
