@@ -200,14 +200,25 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     if (m.cap_per_sm > 0) occ = std::min(occ, m.cap_per_sm);
     const long long cap = (long long)occ * bt->num_sms;
     bt->sysd.resize(bt->n_sys);
-    std::vector<int> cta_sys;
-    int base = 0;
+    std::vector<int> cta_sys, order(bt->n_sys);
+    std::vector<long long> tiles(bt->n_sys);
+    std::vector<int> ctas(bt->n_sys);
     for (int k = 0; k < bt->n_sys; k++) {
-        const long long tiles = ((long long)bt->n_b[k] * Gp + fk::kThreads - 1) / fk::kThreads;
-        const int ctas = (int)std::max<long long>(1, std::min(tiles, cap));
-        bt->sysd[k] = SysDesc{bt->row_base[k], bt->n_b[k], base, ctas};
-        cta_sys.insert(cta_sys.end(), ctas, k);
-        base += ctas;
+        tiles[k] = ((long long)bt->n_b[k] * Gp + fk::kThreads - 1) / fk::kThreads;
+        ctas[k] = (int)std::max<long long>(1, std::min(tiles[k], cap));
+        order[k] = k;
+    }
+    // CTAs are dispatched roughly in index order: give the systems whose CTAs walk the most
+    // tiles the lowest indices, so the longest CTAs start first and the launch's tail is short.
+    // Only the position of a system's CTA range moves; its CTA count (and so its sums) does not.
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (tiles[a] + ctas[a] - 1) / ctas[a] > (tiles[b] + ctas[b] - 1) / ctas[b];
+    });
+    int base = 0;
+    for (int k : order) {
+        bt->sysd[k] = SysDesc{bt->row_base[k], bt->n_b[k], base, ctas[k]};
+        cta_sys.insert(cta_sys.end(), ctas[k], k);
+        base += ctas[k];
     }
     bt->grid = base;
     BT_TRY(bt->d_sys.ensure(sizeof(SysDesc) * bt->n_sys), "alloc system table");
@@ -499,7 +510,7 @@ int fk_batch_autotune(fk_batch* bt, int trial_steps, int* lanes, int* np_out, in
     for (int np : {1, 2, 4}) {
         int gp = next_pow2((bt->P + np - 1) / np);
         if (gp > 32) gp = 32;
-        for (int cap : {0, 2, 4, 8})
+        for (int cap : {0, 1, 2, 3, 4, 6})
             for (int st : {1, 0}) cands.push_back(Mapping{gp, np, cap, st});
     }
     const int M = 2 * (trial_steps + 1);
