@@ -201,7 +201,7 @@ namespace fkpm {
         // Chebyshev moments: mu_m = tr T_m(Hs) ~ tr R^dagger T_m(Hs) R
         virtual Vec<double> moments(int M) = 0;
 
-        // Conductivity moments (not part of this build: throw std::runtime_error)
+        // Conductivity moments: mu_{m1,m2} = tr(j1 T_m1(Hs) j2 T_m2(Hs)) (both run on the GPU)
         virtual Vec<Vec<cx_double>> moments2_v1(int M, SpMatBsr<T> const& j1op, SpMatBsr<T> const& j2op,
                                                 int a_chunk_ncols = 0, int R_chunk_ncols = 0) = 0;
         virtual Vec<Vec<cx_double>> moments2_v2(int M, SpMatBsr<T> const& j1op, SpMatBsr<T> const& j2op,

@@ -35,7 +35,7 @@ extern "C" {
 #define FK_ERR_CUDA        5   /* CUDA runtime error                                        */
 #define FK_ERR_STATE       6   /* call order violated (e.g. autodiff without moments(M))    */
 #define FK_ERR_NODEV       7   /* no usable CUDA device                                     */
-#define FK_ERR_UNSUPPORTED 8   /* valid request outside what this build implements          */
+#define FK_ERR_UNSUPPORTED 8   /* valid request outside what this library implements        */
 
 /* ---- value kinds at the boundary ---- */
 #define FK_REAL    0   /* double                          */

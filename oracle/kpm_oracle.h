@@ -1,9 +1,9 @@
 /*
  * kpm_oracle.h -- TEST INFRASTRUCTURE ONLY (the oracle).
  *
- * CPU restatement of FastKPM's reference CPU engine and host helpers, used by
- * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
- * checker. Nothing in fastkpm_gb300/ links, loads or calls this library.
+ * CPU restatement of FastKPM's reference CPU engine and host helpers, used only
+ * by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, to check
+ * results. Nothing in fastkpm_gb300/ links, loads or calls this library.
  *
  * PARITY UNPINNED against the reference itself: the reference ships no tests,
  * fixtures or golden vectors, and it cannot be compiled here (its public

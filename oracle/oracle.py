@@ -1,7 +1,7 @@
 """ctypes loader of the oracle (TEST INFRASTRUCTURE ONLY).
 
-CPU restatement of the reference's CPU engine; used by tests/, the smoke test
-and bench.py's CPU-baseline leg as the checker. PARITY UNPINNED against the
+CPU restatement of the reference's CPU engine; used only by tests/, the smoke
+test and bench.py's CPU-baseline leg, to check results. PARITY UNPINNED against the
 reference itself (no reference tests or golden vectors; the reference needs
 Armadillo/Boost and does not build here); pinned against analytic known
 answers in tests/.
