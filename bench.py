@@ -426,7 +426,35 @@ def run_batch(args):
         mu = eng.moments(M)
         t_seq += eng.timer_stop()
         err = max(err, _mu_err(mu_b[k], mu))
+    # full solve (moments + autodiff_matrix with each system's own Fermi-energy coefficients):
+    # batched FP32 vs sequential plain FP64, wall clock around the synchronous calls
+    cs = np.stack([W.fermi_coefficients(M, s["es"], "fermi_energy") for s in systems])
+    bt.moments(M)
+    bt.autodiff_matrix(M, cs)
+    n_solve = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(n_solve):
+        bt.moments(M)
+        Ds_b = bt.autodiff_matrix(M, cs)
+    ms_solve = (time.perf_counter() - t0) * 1e3 / n_solve
+    t_seq_solve = 0.0
+    d_err = 0.0
+    for k, (s, R) in enumerate(zip(systems, Rs)):
+        eng.set_H(s["H"], s["es"])
+        eng.set_R(R)
+        D = s["H"].pattern_like(False)
+        eng.moments(M)
+        eng.autodiff_matrix(cs[k], D)
+        t0 = time.perf_counter()
+        eng.moments(M)
+        eng.autodiff_matrix(cs[k], D)
+        t_seq_solve += (time.perf_counter() - t0) * 1e3
+        d_err = max(d_err, float(np.linalg.norm(Ds_b[k].val - D.val) / np.linalg.norm(D.val)))
     eng.close()
+    solve = {"what": "moments(M) + autodiff_matrix(c_sys) for all 64 systems (host wall clock, D copied out)",
+             "ms": ms_solve, "value": float(total_rows) * M * S / (ms_solve / 1e3), "unit": UNIT,
+             "sequential_fp64_ms": t_seq_solve, "speedup_vs_sequential_fp64": t_seq_solve / ms_solve,
+             "D_rel_fro_vs_fp64": d_err}
     per = float(total_rows) * M * S
     bytes_step = 3 * total_rows * S * 4 + sum(s["H"].n_blocks() * 8 + 4 * (s["H"].n_rows + 1) for s in systems)
     achieved = bytes_step / (ms_b / (M // 2) * 1e-3) / 1e9
@@ -440,7 +468,7 @@ def run_batch(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "kernel": "k_cheb_step (batched)", "peak_source": kind},
             "sequential_fp64_ms": t_seq, "speedup_vs_sequential_fp64": t_seq / ms_b,
-            "moments_max_rel_mu0_vs_fp64": err, "autotune": tune, "clocks": clk.summary()}
+            "moments_max_rel_mu0_vs_fp64": err, "solve": solve, "autotune": tune, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
 

@@ -70,6 +70,7 @@ SIGNATURES = {
     "fk_batch_add": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _d, _d, _i, _dp, _ip]),
     "fk_batch_commit": (_i, [_p]),
     "fk_batch_moments": (_i, [_p, _i, _dp]),
+    "fk_batch_autodiff_matrix": (_i, [_p, _i, _dp, _dp]),
     "fk_batch_set_option": (_i, [_p, _i, _i]),
     "fk_batch_get_option": (_i, [_p, _i, _ip]),
     "fk_batch_autotune": (_i, [_p, _i, _ip, _ip, _ip, _ip, _dp]),

@@ -45,6 +45,8 @@ struct Buf {
 struct PendingSystem {
     fk::PreparedH h;
     int n_b, b, s;
+    double mag;              // energy-scale half width (autodiff divides D by it)
+    std::vector<int> o2a;    // original block -> block of the prepared (diagonal-augmented) pattern
     std::vector<double> R;   // column-major n x s (interleaved complex)
 };
 
@@ -93,7 +95,14 @@ struct fk_batch {
     long long ld = 0, total_rows = 0;
     std::vector<int> row_base, n_b;
     std::vector<int> h_row_ptr;          // global
-    Buf d_row_ptr, d_colc, d_hval, d_R, d_V[2], d_stage;
+    std::vector<int> h_col;              // global block columns of the prepared pattern
+    Buf d_row_ptr, d_colc, d_hval, d_R, d_V[4], d_stage;
+    // autodiff_matrix over the batch: per-system scale, original-pattern maps, D accumulator
+    std::vector<double> mag;
+    std::vector<std::vector<int>> o2a;   // per system: original block -> global prepared block
+    int mom_M = 0;                       // moments(M) state left in V0/V1 (0: none)
+    Buf d_D, d_coef, d_rows, d_cols, d_pair, d_rowscale, d_rowfac;
+    bool d_tables = false;
     // launch tables
     Mapping opt, cur;
     int Gp = 1, NP = 1, slices = 1, W = 1, stage_cap = 0, grid = 0;
@@ -160,6 +169,7 @@ cudaError_t batch_load(fk_batch* bt, const double* src, long long n, int ncols, 
 // Build the launch tables for mapping m (0 fields = automatic).
 int batch_configure(fk_batch* bt, const Mapping& m) {
     bt->configured = false;
+    bt->mom_M = 0;   // a new mapping (or the autotuner's trial runs) leaves no usable alpha state
     bt->drop_graphs();
     const int P = bt->P;
     int Gp, NP;
@@ -304,6 +314,189 @@ int batch_run_moments(fk_batch* bt, int M) {
     return FK_OK;
 }
 
+cudaError_t batch_launch_adjoint(fk_batch* bt, const fk::AdjArgs& a, const fk::Launch& l) {
+    switch (bt->prec) {
+        case fk::kF64: return fk::launch_adjoint_f64(bt->cplx, bt->b, bt->NP, a, l);
+        case fk::kF32: return fk::launch_adjoint_f32(bt->cplx, bt->b, bt->NP, a, l);
+        default: return fk::launch_adjoint_ds(bt->cplx, bt->b, bt->NP, a, l);
+    }
+}
+cudaError_t batch_launch_outer(fk_batch* bt, const fk::OuterArgs& a, const fk::Launch& l) {
+    switch (bt->prec) {
+        case fk::kF64: return fk::launch_outer_f64(bt->cplx, bt->b, bt->NP, a, l);
+        case fk::kF32: return fk::launch_outer_f32(bt->cplx, bt->b, bt->NP, a, l);
+        default: return fk::launch_outer_ds(bt->cplx, bt->b, bt->NP, a, l);
+    }
+}
+cudaError_t batch_scale_rows(fk_batch* bt, const void* x, void* y, const double* f) {
+    switch (bt->prec) {
+        case fk::kF64: return fk::launch_scale_rows_f64(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, f, bt->stream);
+        case fk::kF32: return fk::launch_scale_rows_f32(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, f, bt->stream);
+        default: return fk::launch_scale_rows_ds(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, f, bt->stream);
+    }
+}
+
+// Tables of the symmetrize step on the prepared pattern: block row, block column and partner
+// (j, i) of every block, and 1 / mag of its system per block row.
+int batch_d_tables(fk_batch* bt) {
+    if (bt->d_tables) return FK_OK;
+    const int rows = (int)bt->h_row_ptr.size() - 1;
+    const size_t nk = bt->h_col.size();
+    std::vector<int> brow(nk), pair(nk);
+    std::vector<double> rscale(rows);
+    for (int sys = 0; sys < bt->n_sys; sys++)
+        for (int i = bt->row_base[sys]; i < bt->row_base[sys] + bt->n_b[sys]; i++) rscale[i] = 1.0 / bt->mag[sys];
+    for (int i = 0; i < rows; i++) {
+        for (int k = bt->h_row_ptr[i]; k < bt->h_row_ptr[i + 1]; k++) {
+            brow[k] = i;
+            const int j = bt->h_col[k];
+            const int* lo = bt->h_col.data() + bt->h_row_ptr[j];
+            const int* hi = bt->h_col.data() + bt->h_row_ptr[j + 1];
+            const int* f = std::lower_bound(lo, hi, i);
+            if (f == hi || *f != i)
+                return bt->fail(FK_ERR_PATTERN, "batch_autodiff_matrix: H's pattern is not symmetric (block %d, %d)", i, j);
+            pair[k] = (int)(f - bt->h_col.data());
+        }
+    }
+    BT_TRY(bt->d_rows.ensure(sizeof(int) * std::max<size_t>(nk, 1)), "alloc D tables");
+    BT_TRY(bt->d_cols.ensure(sizeof(int) * std::max<size_t>(nk, 1)), "alloc D tables");
+    BT_TRY(bt->d_pair.ensure(sizeof(int) * std::max<size_t>(nk, 1)), "alloc D tables");
+    BT_TRY(bt->d_rowscale.ensure(sizeof(double) * rows), "alloc D tables");
+    BT_TRY(cudaMemcpy(bt->d_rows.p, brow.data(), sizeof(int) * nk, cudaMemcpyHostToDevice), "upload D tables");
+    BT_TRY(cudaMemcpy(bt->d_cols.p, bt->h_col.data(), sizeof(int) * nk, cudaMemcpyHostToDevice), "upload D tables");
+    BT_TRY(cudaMemcpy(bt->d_pair.p, pair.data(), sizeof(int) * nk, cudaMemcpyHostToDevice), "upload D tables");
+    BT_TRY(cudaMemcpy(bt->d_rowscale.p, rscale.data(), sizeof(double) * rows, cudaMemcpyHostToDevice), "upload D tables");
+    bt->d_tables = true;
+    return FK_OK;
+}
+
+// autodiff_matrix for every system of the batch at once (the single engine's reverse recursion,
+// src/engine_cpu.cpp:255-304, with per-system coefficients c[sys * M + m]): D on each system's
+// own H pattern, symmetrized and divided by that system's mag. The adjoint and outer-product
+// kernels run with the batch's system tables, so every system's CTAs stay its own.
+int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
+    if (M < 2 || M % 2) return bt->fail(FK_ERR_ARG, "batch_autodiff_matrix: M must be even and >= 2");
+    if (bt->mom_M != M)
+        return bt->fail(FK_ERR_STATE, "batch_autodiff_matrix(M=%d) needs batch_moments(%d) first", M, M);
+    int rc = batch_d_tables(bt);
+    if (rc != FK_OK) return rc;
+    const size_t vb = (size_t)bt->total_rows * bt->ld * bt->esize();
+    BT_TRY(bt->d_V[2].ensure(vb), "alloc work vector");
+    BT_TRY(bt->d_V[3].ensure(vb), "alloc work vector");
+    const int rows = (int)bt->h_row_ptr.size() - 1, nsys = bt->n_sys;
+    const size_t nk = bt->h_col.size(), bb = (size_t)bt->b * bt->b, cw = bt->cplx ? 2 : 1;
+    const size_t dn = nk * bb * cw;
+    BT_TRY(bt->d_D.ensure(sizeof(double) * std::max<size_t>(dn, 1)), "alloc D");
+    BT_TRY(cudaMemsetAsync(bt->d_D.p, 0, sizeof(double) * dn, bt->stream), "clear D");
+    // per adjoint step q (m = M/2-1-q) and system: {4 c_2m, 2 c_2m+1, 2 c_2m-1 or diag}
+    const int nsteps = M / 2 - 1;
+    std::vector<double> coef(3 * (size_t)std::max(nsteps, 1) * nsys, 0.0), f_first(rows), f_diag(rows);
+    for (int sys = 0; sys < nsys; sys++) {
+        const double* cs = c + (size_t)sys * M;
+        double diag = cs[1];
+        for (int m = 1; m < M / 2; m++) diag -= cs[2 * m + 1];
+        for (int m = M / 2 - 1, q = 0; m >= 1; m--, q++) {
+            double* t = &coef[3 * ((size_t)q * nsys + sys)];
+            t[0] = 4 * cs[2 * m];
+            t[1] = 2 * cs[2 * m + 1];
+            t[2] = m > 1 ? 2 * cs[2 * m - 1] : diag;
+        }
+        for (int i = bt->row_base[sys]; i < bt->row_base[sys] + bt->n_b[sys]; i++) {
+            f_first[i] = 2 * cs[M - 1];
+            f_diag[i] = diag;
+        }
+    }
+    BT_TRY(bt->d_coef.ensure(sizeof(double) * coef.size()), "alloc coefficients");
+    BT_TRY(bt->d_rowfac.ensure(sizeof(double) * rows), "alloc factors");
+    BT_TRY(cudaMemcpyAsync(bt->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, bt->stream),
+           "upload coefficients");
+    BT_TRY(cudaMemcpyAsync(bt->d_rowfac.p, M > 2 ? f_first.data() : f_diag.data(), sizeof(double) * rows,
+                           cudaMemcpyHostToDevice, bt->stream), "upload factors");
+    // moments(M) left alpha_{M/2} in V[(M/2-1)&1] and alpha_{M/2-1} in V[(M/2)&1] (R when M = 2)
+    void* V[4] = {bt->d_V[0].p, bt->d_V[1].p, bt->d_V[2].p, bt->d_V[3].p};
+    void* A = M / 2 >= 2 ? V[(M / 2) & 1] : bt->d_R.p;
+    void* Ap = V[(M / 2 - 1) & 1];
+    void* Bv = V[2];
+    void* Bp = V[3];
+    const bool fuse = bt->prec != fk::kDS;   // the single engine's default
+    auto outer = [&](const void* a, const void* bv, double alpha) -> int {
+        fk::OuterArgs o;
+        o.sys = bt->d_sys.as<SysDesc>();
+        o.cta_sys = bt->d_cta_sys.as<int>();
+        o.Gp = bt->Gp;
+        o.P = bt->P;
+        o.ld = bt->ld;
+        o.row_ptr = bt->d_row_ptr.as<int>();
+        o.colc = bt->d_colc.as<unsigned>();
+        o.A = a;
+        o.Bv = bv;
+        o.alpha = alpha;
+        o.two_terms = 0;
+        o.Dacc = bt->d_D.as<double>();
+        BT_TRY(batch_launch_outer(bt, o, fk::Launch{bt->grid, 0, bt->stream}), "batched outer-product launch");
+        return FK_OK;
+    };
+    BT_TRY(batch_scale_rows(bt, A, Bv, bt->d_rowfac.as<double>()), "scale kernel");
+    if (M > 2) {
+        BT_TRY(cudaMemsetAsync(Bp, 0, vb, bt->stream), "clear beta");
+        for (int q = 0; q < nsteps; q++) {
+            if (!fuse) {
+                rc = outer(A, Bv, 2.0);
+                if (rc != FK_OK) return rc;
+            }
+            fk::AdjArgs a;
+            a.sys = bt->d_sys.as<SysDesc>();
+            a.cta_sys = bt->d_cta_sys.as<int>();
+            a.Gp = bt->Gp;
+            a.P = bt->P;
+            a.ld = bt->ld;
+            a.row_ptr = bt->d_row_ptr.as<int>();
+            a.colc = bt->d_colc.as<unsigned>();
+            a.hval = bt->d_hval.p;
+            a.A = A;
+            a.Ap = Ap;
+            a.Bv = Bv;
+            a.Bp = Bp;
+            a.coef = bt->d_coef.as<double>() + 3 * (size_t)q * nsys;
+            a.cstride = 3;
+            a.Dacc = fuse ? bt->d_D.as<double>() : nullptr;
+            a.dscale = 2.0;
+            a.stage_cap = bt->stage_cap;
+            BT_TRY(batch_launch_adjoint(bt, a, fk::Launch{bt->grid, bt->smem, bt->stream}), "batched adjoint launch");
+            std::swap(A, Ap);
+            std::swap(Bv, Bp);
+        }
+    }
+    rc = outer(A, Bv, 1.0);
+    if (rc != FK_OK) return rc;
+    if (bt->prec != fk::kF64) {   // float-float accumulator -> double
+        const int g = (int)std::max<long long>(1, std::min<long long>(((long long)dn + 255) / 256, 152LL * 16));
+        fk::k_ds_to_double<<<g, 256, 0, bt->stream>>>(bt->d_D.as<double>(), (long long)dn);
+        BT_TRY(cudaGetLastError(), "accumulator conversion");
+    }
+    {
+        const long long work = (long long)nk * bb;
+        const int g = (int)std::max<long long>(1, std::min<long long>((work + 255) / 256, 152LL * 16));
+        fk::k_symmetrize_scale<<<g, 256, 0, bt->stream>>>(bt->d_D.as<double>(), bt->d_rows.as<int>(), bt->d_cols.as<int>(),
+                                                          bt->d_pair.as<int>(), (int)nk, bt->b, bt->cplx, 0.0,
+                                                          bt->d_rowscale.as<double>());
+        BT_TRY(cudaGetLastError(), "symmetrize launch");
+    }
+    std::vector<double> h(dn);
+    BT_TRY(cudaMemcpyAsync(h.data(), bt->d_D.p, sizeof(double) * dn, cudaMemcpyDeviceToHost, bt->stream), "copy D");
+    BT_TRY(cudaStreamSynchronize(bt->stream), "batch autodiff");
+    size_t off = 0;
+    const size_t per = bb * cw;
+    for (int sys = 0; sys < nsys; sys++) {
+        for (int g : bt->o2a[sys]) {
+            std::copy(h.begin() + (size_t)g * per, h.begin() + (size_t)(g + 1) * per, D_out + off);
+            off += per;
+        }
+    }
+    bt->mom_M = 0;   // the alpha state is consumed
+    return FK_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -336,8 +529,9 @@ int fk_batch_destroy(fk_batch* bt) {
     cudaSetDevice(bt->device);
     cudaStreamSynchronize(bt->stream);
     bt->drop_graphs();
-    Buf* bufs[] = {&bt->d_row_ptr, &bt->d_colc, &bt->d_hval, &bt->d_R, &bt->d_V[0], &bt->d_V[1], &bt->d_stage,
-                   &bt->d_sys, &bt->d_cta_sys, &bt->d_partials, &bt->d_raw};
+    Buf* bufs[] = {&bt->d_row_ptr, &bt->d_colc, &bt->d_hval, &bt->d_R, &bt->d_V[0], &bt->d_V[1], &bt->d_V[2],
+                   &bt->d_V[3], &bt->d_stage, &bt->d_sys, &bt->d_cta_sys, &bt->d_partials, &bt->d_raw, &bt->d_D,
+                   &bt->d_coef, &bt->d_rows, &bt->d_cols, &bt->d_pair, &bt->d_rowscale, &bt->d_rowfac};
     for (auto* b : bufs) b->release();
     if (bt->t0) cudaEventDestroy(bt->t0);
     if (bt->t1) cudaEventDestroy(bt->t1);
@@ -362,6 +556,15 @@ int fk_batch_add(fk_batch* bt, int n_b, int b, int nnzb, const int* row_ptr, con
     ps.n_b = n_b;
     ps.b = b;
     ps.s = s;
+    ps.mag = (es_hi - es_lo) / 2.0;
+    ps.o2a.resize(nnzb);
+    for (int i = 0; i < n_b; i++) {   // the prepared row holds the original blocks in order plus maybe a diagonal
+        int a = ps.h.row_ptr[i];
+        for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+            while (ps.h.col[a] != col_idx[k]) a++;
+            ps.o2a[k] = a++;
+        }
+    }
     ps.R.assign(R, R + (size_t)n_b * b * s * (bt->cplx ? 2 : 1));
     bt->pending.push_back(std::move(ps));
     if (index) *index = bt->n_sys + (int)bt->pending.size() - 1;
@@ -383,6 +586,8 @@ int fk_batch_commit(fk_batch* bt) {
     long long rows = 0, nk = 0;
     bt->row_base.resize(bt->n_sys);
     bt->n_b.resize(bt->n_sys);
+    bt->mag.resize(bt->n_sys);
+    bt->o2a.resize(bt->n_sys);
     for (int k = 0; k < bt->n_sys; k++) {
         bt->row_base[k] = (int)rows;
         bt->n_b[k] = ps[k].n_b;
@@ -403,8 +608,13 @@ int fk_batch_commit(fk_batch* bt) {
             const unsigned cls = cc >> 30, col = cc & fk::kColMask;
             colc.push_back((col + (unsigned)bt->row_base[k]) | (cls << 30));
         }
+        bt->mag[k] = ps[k].mag;
+        bt->o2a[k] = std::move(ps[k].o2a);
+        for (int& v : bt->o2a[k]) v += kb;
         hval.insert(hval.end(), ps[k].h.hval.begin(), ps[k].h.hval.end());
     }
+    bt->h_col.resize(colc.size());
+    for (size_t q = 0; q < colc.size(); q++) bt->h_col[q] = (int)(colc[q] & fk::kColMask);
     BT_TRY(bt->d_row_ptr.ensure(sizeof(int) * (rows + 1)), "alloc H row_ptr");
     BT_TRY(bt->d_colc.ensure(sizeof(unsigned) * std::max<size_t>(colc.size(), 1)), "alloc H columns");
     BT_TRY(bt->d_hval.ensure(std::max<size_t>(hval.size(), 16)), "alloc H values");
@@ -446,6 +656,7 @@ int fk_batch_moments(fk_batch* bt, int M, double* mu) {
     cudaSetDevice(bt->device);
     int rc = batch_run_moments(bt, M);
     if (rc != FK_OK) return rc;
+    bt->mom_M = M;
     const int nsteps = M / 2;
     bt->h_raw.resize(2 * (size_t)nsteps * bt->n_sys);
     BT_TRY(cudaMemcpyAsync(bt->h_raw.data(), bt->d_raw.p, sizeof(double) * bt->h_raw.size(), cudaMemcpyDeviceToHost,
@@ -463,6 +674,13 @@ int fk_batch_moments(fk_batch* bt, int M, double* mu) {
         }
     }
     return FK_OK;
+}
+
+int fk_batch_autodiff_matrix(fk_batch* bt, int M, const double* c, double* D_val) {
+    if (!bt || !c || !D_val) return FK_ERR_ARG;
+    if (!bt->configured) return bt->fail(FK_ERR_STATE, "batch_autodiff_matrix: commit the batch first");
+    cudaSetDevice(bt->device);
+    return batch_autodiff(bt, M, c, D_val);
 }
 
 int fk_batch_set_option(fk_batch* bt, int option, int value) {

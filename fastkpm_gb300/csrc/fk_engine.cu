@@ -832,7 +832,7 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
             ProfScope ps(e, fk::kHelper);
             fk::k_symmetrize_scale<<<std::max(grid, 1), 256, 0, e->stream>>>(
                 e->dd_acc.as<double>(), e->dd_rows.as<int>(), e->dd_colc.as<int>(), e->dd_pair.as<int>(), d_nnzb, e->b,
-                e->cplx, 1.0 / mag);
+                e->cplx, 1.0 / mag, nullptr);
             FK_TRY(cudaGetLastError(), "symmetrize launch");
         }
         return FK_OK;

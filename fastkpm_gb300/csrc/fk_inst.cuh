@@ -130,5 +130,12 @@ cudaError_t FK_CAT(launch_export_panel, FK_PREC_NAME)(int cplx, const void* src,
     else k_export_panel<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(src), n, ld, c0, w, dst);
     return cudaGetLastError();
 }
+cudaError_t FK_CAT(launch_scale_rows, FK_PREC_NAME)(int cplx, const void* x, void* y, long long n_rows, long long ld,
+                                                  int b, const double* f, cudaStream_t st) {
+    const int g = helper_grid(n_rows * ld);
+    if (cplx) k_scale_rows<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(x), reinterpret_cast<FK_SYS_C::E*>(y), n_rows, ld, b, f);
+    else k_scale_rows<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(x), reinterpret_cast<FK_SYS_R::E*>(y), n_rows, ld, b, f);
+    return cudaGetLastError();
+}
 
 }  // namespace fk

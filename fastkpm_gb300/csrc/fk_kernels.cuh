@@ -734,6 +734,16 @@ __global__ void k_export_panel(const typename S::E* src, long long n, long long 
     }
 }
 
+// y[r, :] = f[block row of r] * x[r, :] over rows r < n_rows of row-major n x ld vectors (the
+// batched engine's per-system factors, one entry per block row of b rows).
+template <class S>
+__global__ void k_scale_rows(const typename S::E* x, typename S::E* y, long long n_rows, long long ld, int b,
+                             const double* f) {
+    const long long total = n_rows * ld;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
+        y[q] = S::scale(S::coef(f[(q / ld) / b]), x[q]);
+}
+
 // Row-major device vector -> column-major double host layout (for reading back R / state).
 template <class S>
 __global__ void k_store_colmajor(const typename S::E* src, long long n, int ncols, long long ld, double* dst) {
@@ -757,11 +767,11 @@ __global__ void k_scale(const typename S::E* x, typename S::E* y, long long n_el
         y[q] = S::scale(cc, x[q]);
 }
 
-// D <- (D + D^T-pair^dagger)/2 blockwise, then * scale (SpMatBsr::symmetrize and
+// D <- (D + D^T-pair^dagger)/2 blockwise, then * scale (row_scale[i] per block row when given) (SpMatBsr::symmetrize and
 // scale, src/spmat.cpp:171-198, done on the device). pair[k] is the block index of
 // (j, i) for k = (i, j). Each unordered pair is handled by the block with i >= j.
 static __global__ void k_symmetrize_scale(double* D, const int* rows, const int* cols, const int* pair, int nnzb, int b,
-                                          int cplx, double scale) {
+                                          int cplx, double scale_all, const double* row_scale) {
     const int bb = b * b;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)nnzb * bb;
          q += (long long)gridDim.x * blockDim.x) {
@@ -774,6 +784,7 @@ static __global__ void k_symmetrize_scale(double* D, const int* rows, const int*
         const size_t q1 = (size_t)k * bb + bj * b + bi;    // (bi, bj) of block k
         const size_t q2 = (size_t)kt * bb + bi * b + bj;   // (bj, bi) of block kt
         if (i == j && bi < bj) continue;                   // diagonal block: each entry pair once
+        const double scale = row_scale ? row_scale[i] : scale_all;   // per block row (batched systems)
         if (cplx) {
             const double r1 = D[2 * q1], i1 = D[2 * q1 + 1], r2 = D[2 * q2], i2 = D[2 * q2 + 1];
             const double sr = (r1 + r2) / 2.0, si = (i1 - i2) / 2.0;

@@ -477,6 +477,7 @@ class Batch:
             raise L.FkError(st, "batch_create")
         self.h = h
         self.n = 0
+        self.patterns = []   # per system: (block rows, b, row_ptr, col_idx) as added
 
     def _check(self, st, where):
         if st != L.FK_OK:
@@ -505,6 +506,7 @@ class Batch:
                                           _dp(_as_doubles(H.val)), es.lo, es.hi, s, _dp(_as_doubles(flat)),
                                           C.byref(idx)), "batch_add")
         self.n += 1
+        self.patterns.append((H.n_rows, H.b_len, H.row_ptr.copy(), H.col_idx.copy()))
         return idx.value
 
     def commit(self):
@@ -514,6 +516,22 @@ class Batch:
         mu = np.zeros(self.n * M)
         self._check(self.lib.fk_batch_moments(self.h, M, _dp(mu)), "batch_moments")
         return mu.reshape(self.n, M)
+
+    def autodiff_matrix(self, M, c):
+        """Engine.autodiff_matrix for every system after moments(M): c is (systems, M), one row of
+        coefficients per system; returns one SpMatBsr per system on its own H pattern."""
+        c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.n, M)
+        dt = np.complex128 if self.complex_values else np.float64
+        total = sum(len(ci) * b * b for (_, b, _, ci) in self.patterns)
+        out = np.zeros(total, dt)
+        self._check(self.lib.fk_batch_autodiff_matrix(self.h, M, _dp(c), _dp(out.view(np.float64))),
+                    "batch_autodiff_matrix")
+        Ds, off = [], 0
+        for (n_rows, b, rp, ci) in self.patterns:
+            k = len(ci) * b * b
+            Ds.append(SpMatBsr(n_rows, b, rp, ci, out[off:off + k], complex_values=self.complex_values))
+            off += k
+        return Ds
 
     def set_option(self, opt, value):
         self._check(self.lib.fk_batch_set_option(self.h, opt, int(value)), "batch_set_option")

@@ -213,6 +213,12 @@ int  fk_batch_commit(fk_batch* bt);
 /* mu[index * M + m] for every system, even M >= 2: M/2 launches, each covering all systems,
  * replayed from a CUDA graph when FK_OPT_GRAPHS is on. */
 int  fk_batch_moments(fk_batch* bt, int M, double* mu);
+/* Engine<T>::autodiff_matrix(c, D) (reference src/engine_cpu.cpp:391-440) for every system of the
+ * batch in the same launches, after fk_batch_moments with the same M (FK_ERR_STATE otherwise).
+ * c[sys*M + m]: each system's coefficients. D_val: each system's D on its own H pattern (as added),
+ * systems in index order, b*b (complex: interleaved) values per block; symmetrized and divided by
+ * that system's energy scale. H patterns must be symmetric (FK_ERR_PATTERN). */
+int  fk_batch_autodiff_matrix(fk_batch* bt, int M, const double* c, double* D_val);
 int  fk_batch_set_option(fk_batch* bt, int option, int value);
 int  fk_batch_get_option(const fk_batch* bt, int option, int* value);
 /* Choose lanes per block row, packets per lane, CTA cap and H staging by timing trial_steps

@@ -8,6 +8,7 @@ import fastkpm_gb300 as fk
 from fastkpm_gb300 import _lib as L
 from fastkpm_gb300 import workloads as W
 from oracle import oracle as O
+from tests.conftest import rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -108,3 +109,73 @@ def test_batch_rejects_mixed_shapes(gpu):
     with pytest.raises(L.FkError) as ei:
         fk.Batch(False, "fp32").moments(10)
     assert ei.value.status == L.FK_ERR_STATE
+
+
+def _spin_systems(Ls=(3, 4, 2, 5)):
+    out = []
+    for k, L_ in enumerate(Ls):
+        H, es, _ = W.cubic_spin_lattice(L_, -1.0, 1.0, seed=40 + k)
+        R = W.phase_probes(np.arange(2 * H.n_rows) % 8, 1, seed=40 + k)
+        out.append((H, es, R))
+    return out
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("ds", 1e-10), ("fp32", 1e-4)])
+def test_batch_autodiff_matches_oracle_per_system(gpu, cplx, prec, tol):
+    systems = _spin_systems() if cplx else make_systems(4, 16, 11, Ls=(6, 9, 4, 11))
+    M = 24
+    bt = fk.Batch(cplx, prec)
+    for H, es, R in systems:
+        bt.add(H, es, R)
+    bt.commit()
+    bt.moments(M)
+    # a different Fermi level per system: the coefficient rows are the systems' own
+    cs = np.stack([W.fermi_coefficients(M, es, "fermi_energy", mu=0.2 * k) for k, (_, es, _) in enumerate(systems)])
+    Ds = bt.autodiff_matrix(M, cs)
+    assert len(Ds) == len(systems)
+    for k, (H, es, R) in enumerate(systems):
+        o = O.OracleEngine(cplx)
+        o.set_H(H, es)
+        o.set_R(R)
+        o.moments(M)
+        ref = o.autodiff_matrix(cs[k], H.pattern_like(cplx))
+        assert rel_err(Ds[k].val, ref) <= tol, k
+    # the alpha state is consumed: a second call needs moments(M) again
+    with pytest.raises(L.FkError) as ei:
+        bt.autodiff_matrix(M, cs)
+    assert ei.value.status == L.FK_ERR_STATE
+
+
+def _without_diagonal(H):
+    keep = H.col_idx != H.row_idx
+    rp = np.concatenate([[0], np.cumsum(np.bincount(H.row_idx[keep], minlength=H.n_rows))]).astype(np.int32)
+    bb = H.b_len * H.b_len
+    val = H.val.reshape(-1, bb)[keep].reshape(-1)
+    return fk.SpMatBsr(H.n_rows, H.b_len, rp, H.col_idx[keep], val)
+
+
+def test_batch_autodiff_keeps_h_pattern_without_diagonal(gpu):
+    H0, es0 = W.square_lattice(7, -1.0, 0.5, seed=3)
+    H0 = _without_diagonal(H0)
+    assert np.all(H0.col_idx != H0.row_idx)
+    H1, es1 = W.square_lattice(5, -1.0, 2.0, seed=4)
+    S, M = 8, 16
+    R0 = fk.probe_uncorrelated(H0.n_rows, S, fk.RNG(5))
+    R1 = fk.probe_uncorrelated(H1.n_rows, S, fk.RNG(6))
+    bt = fk.Batch(False, "fp64")
+    bt.add(H0, es0, R0)
+    bt.add(H1, es1, R1)
+    bt.commit()
+    bt.moments(M)
+    cs = np.stack([W.fermi_coefficients(M, es0, "fermi_energy"), W.fermi_coefficients(M, es1, "fermi_energy", mu=0.3)])
+    Ds = bt.autodiff_matrix(M, cs)
+    for k, (H, es, R) in enumerate([(H0, es0, R0), (H1, es1, R1)]):
+        eng = fk.Engine(False, "fp64")
+        eng.set_H(H, es)
+        eng.set_R(R)
+        eng.moments(M)
+        D = H.pattern_like(False)
+        eng.autodiff_matrix(cs[k], D)
+        assert np.array_equal(Ds[k].col_idx, H.col_idx)
+        assert np.max(np.abs(Ds[k].val - D.val)) <= 1e-12 * max(1.0, np.max(np.abs(D.val))), k
