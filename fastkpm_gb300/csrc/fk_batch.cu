@@ -101,8 +101,10 @@ struct fk_batch {
     std::vector<double> mag;
     std::vector<std::vector<int>> o2a;   // per system: original block -> global prepared block
     int mom_M = 0;                       // moments(M) state left in V0/V1 (0: none)
-    Buf d_D, d_coef, d_rows, d_cols, d_pair, d_rowscale, d_rowfac;
+    Buf d_D, d_coef, d_rows, d_cols, d_pair, d_rowscale, d_rowsys, d_rowfac, d_gather, d_Dout;
     bool d_tables = false;
+    bool d_gather_identity = true;   // no diagonal blocks were added: D leaves in the prepared order
+    long long n_out_blocks = 0;
     // launch tables
     Mapping opt, cur;
     int Gp = 1, NP = 1, slices = 1, W = 1, stage_cap = 0, grid = 0;
@@ -330,9 +332,9 @@ cudaError_t batch_launch_outer(fk_batch* bt, const fk::OuterArgs& a, const fk::L
 }
 cudaError_t batch_scale_rows(fk_batch* bt, const void* x, void* y, const double* f) {
     switch (bt->prec) {
-        case fk::kF64: return fk::launch_scale_rows_f64(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, f, bt->stream);
-        case fk::kF32: return fk::launch_scale_rows_f32(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, f, bt->stream);
-        default: return fk::launch_scale_rows_ds(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, f, bt->stream);
+        case fk::kF64: return fk::launch_scale_rows_f64(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, bt->d_rowsys.as<int>(), f, bt->stream);
+        case fk::kF32: return fk::launch_scale_rows_f32(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, bt->d_rowsys.as<int>(), f, bt->stream);
+        default: return fk::launch_scale_rows_ds(bt->cplx, x, y, bt->total_rows, bt->ld, bt->b, bt->d_rowsys.as<int>(), f, bt->stream);
     }
 }
 
@@ -344,8 +346,12 @@ int batch_d_tables(fk_batch* bt) {
     const size_t nk = bt->h_col.size();
     std::vector<int> brow(nk), pair(nk);
     std::vector<double> rscale(rows);
+    std::vector<int> rsys(rows);
     for (int sys = 0; sys < bt->n_sys; sys++)
-        for (int i = bt->row_base[sys]; i < bt->row_base[sys] + bt->n_b[sys]; i++) rscale[i] = 1.0 / bt->mag[sys];
+        for (int i = bt->row_base[sys]; i < bt->row_base[sys] + bt->n_b[sys]; i++) {
+            rscale[i] = 1.0 / bt->mag[sys];
+            rsys[i] = sys;
+        }
     for (int i = 0; i < rows; i++) {
         for (int k = bt->h_row_ptr[i]; k < bt->h_row_ptr[i + 1]; k++) {
             brow[k] = i;
@@ -362,10 +368,22 @@ int batch_d_tables(fk_batch* bt) {
     BT_TRY(bt->d_cols.ensure(sizeof(int) * std::max<size_t>(nk, 1)), "alloc D tables");
     BT_TRY(bt->d_pair.ensure(sizeof(int) * std::max<size_t>(nk, 1)), "alloc D tables");
     BT_TRY(bt->d_rowscale.ensure(sizeof(double) * rows), "alloc D tables");
+    BT_TRY(bt->d_rowsys.ensure(sizeof(int) * rows), "alloc D tables");
+    BT_TRY(cudaMemcpy(bt->d_rowsys.p, rsys.data(), sizeof(int) * rows, cudaMemcpyHostToDevice), "upload D tables");
     BT_TRY(cudaMemcpy(bt->d_rows.p, brow.data(), sizeof(int) * nk, cudaMemcpyHostToDevice), "upload D tables");
     BT_TRY(cudaMemcpy(bt->d_cols.p, bt->h_col.data(), sizeof(int) * nk, cudaMemcpyHostToDevice), "upload D tables");
     BT_TRY(cudaMemcpy(bt->d_pair.p, pair.data(), sizeof(int) * nk, cudaMemcpyHostToDevice), "upload D tables");
     BT_TRY(cudaMemcpy(bt->d_rowscale.p, rscale.data(), sizeof(double) * rows, cudaMemcpyHostToDevice), "upload D tables");
+    // output order: each system's blocks as added, systems in index order
+    std::vector<int> gl;
+    for (int sys = 0; sys < bt->n_sys; sys++) gl.insert(gl.end(), bt->o2a[sys].begin(), bt->o2a[sys].end());
+    bt->n_out_blocks = (long long)gl.size();
+    bt->d_gather_identity = gl.size() == nk;
+    for (size_t q = 0; q < gl.size() && bt->d_gather_identity; q++) bt->d_gather_identity = gl[q] == (int)q;
+    if (!bt->d_gather_identity) {
+        BT_TRY(bt->d_gather.ensure(sizeof(int) * std::max<size_t>(gl.size(), 1)), "alloc D tables");
+        BT_TRY(cudaMemcpy(bt->d_gather.p, gl.data(), sizeof(int) * gl.size(), cudaMemcpyHostToDevice), "upload D tables");
+    }
     bt->d_tables = true;
     return FK_OK;
 }
@@ -383,14 +401,14 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
     const size_t vb = (size_t)bt->total_rows * bt->ld * bt->esize();
     BT_TRY(bt->d_V[2].ensure(vb), "alloc work vector");
     BT_TRY(bt->d_V[3].ensure(vb), "alloc work vector");
-    const int rows = (int)bt->h_row_ptr.size() - 1, nsys = bt->n_sys;
+    const int nsys = bt->n_sys;
     const size_t nk = bt->h_col.size(), bb = (size_t)bt->b * bt->b, cw = bt->cplx ? 2 : 1;
     const size_t dn = nk * bb * cw;
     BT_TRY(bt->d_D.ensure(sizeof(double) * std::max<size_t>(dn, 1)), "alloc D");
     BT_TRY(cudaMemsetAsync(bt->d_D.p, 0, sizeof(double) * dn, bt->stream), "clear D");
     // per adjoint step q (m = M/2-1-q) and system: {4 c_2m, 2 c_2m+1, 2 c_2m-1 or diag}
     const int nsteps = M / 2 - 1;
-    std::vector<double> coef(3 * (size_t)std::max(nsteps, 1) * nsys, 0.0), f_first(rows), f_diag(rows);
+    std::vector<double> coef(3 * (size_t)std::max(nsteps, 1) * nsys, 0.0), fac(nsys);
     for (int sys = 0; sys < nsys; sys++) {
         const double* cs = c + (size_t)sys * M;
         double diag = cs[1];
@@ -401,17 +419,14 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
             t[1] = 2 * cs[2 * m + 1];
             t[2] = m > 1 ? 2 * cs[2 * m - 1] : diag;
         }
-        for (int i = bt->row_base[sys]; i < bt->row_base[sys] + bt->n_b[sys]; i++) {
-            f_first[i] = 2 * cs[M - 1];
-            f_diag[i] = diag;
-        }
+        fac[sys] = M > 2 ? 2 * cs[M - 1] : diag;   // beta_{M/2} = fac alpha_{M/2-1}
     }
     BT_TRY(bt->d_coef.ensure(sizeof(double) * coef.size()), "alloc coefficients");
-    BT_TRY(bt->d_rowfac.ensure(sizeof(double) * rows), "alloc factors");
+    BT_TRY(bt->d_rowfac.ensure(sizeof(double) * nsys), "alloc factors");
     BT_TRY(cudaMemcpyAsync(bt->d_coef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, bt->stream),
            "upload coefficients");
-    BT_TRY(cudaMemcpyAsync(bt->d_rowfac.p, M > 2 ? f_first.data() : f_diag.data(), sizeof(double) * rows,
-                           cudaMemcpyHostToDevice, bt->stream), "upload factors");
+    BT_TRY(cudaMemcpyAsync(bt->d_rowfac.p, fac.data(), sizeof(double) * nsys, cudaMemcpyHostToDevice, bt->stream),
+           "upload factors");
     // moments(M) left alpha_{M/2} in V[(M/2-1)&1] and alpha_{M/2-1} in V[(M/2)&1] (R when M = 2)
     void* V[4] = {bt->d_V[0].p, bt->d_V[1].p, bt->d_V[2].p, bt->d_V[3].p};
     void* A = M / 2 >= 2 ? V[(M / 2) & 1] : bt->d_R.p;
@@ -482,17 +497,20 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
                                                           bt->d_rowscale.as<double>());
         BT_TRY(cudaGetLastError(), "symmetrize launch");
     }
-    std::vector<double> h(dn);
-    BT_TRY(cudaMemcpyAsync(h.data(), bt->d_D.p, sizeof(double) * dn, cudaMemcpyDeviceToHost, bt->stream), "copy D");
-    BT_TRY(cudaStreamSynchronize(bt->stream), "batch autodiff");
-    size_t off = 0;
-    const size_t per = bb * cw;
-    for (int sys = 0; sys < nsys; sys++) {
-        for (int g : bt->o2a[sys]) {
-            std::copy(h.begin() + (size_t)g * per, h.begin() + (size_t)(g + 1) * per, D_out + off);
-            off += per;
-        }
+    // back to each system's own block order on the device, then one copy into the caller's buffer
+    const int per = (int)(bb * cw);
+    const size_t nout = (size_t)bt->n_out_blocks * per;
+    const double* src = bt->d_D.as<double>();
+    if (!bt->d_gather_identity) {
+        BT_TRY(bt->d_Dout.ensure(sizeof(double) * std::max<size_t>(nout, 1)), "alloc D");
+        const int g = (int)std::max<long long>(1, std::min<long long>(((long long)nout + 255) / 256, 152LL * 16));
+        fk::k_gather_blocks<<<g, 256, 0, bt->stream>>>(src, bt->d_gather.as<int>(), bt->n_out_blocks, per,
+                                                       bt->d_Dout.as<double>());
+        BT_TRY(cudaGetLastError(), "gather launch");
+        src = bt->d_Dout.as<double>();
     }
+    if (nout) BT_TRY(cudaMemcpyAsync(D_out, src, sizeof(double) * nout, cudaMemcpyDeviceToHost, bt->stream), "copy D");
+    BT_TRY(cudaStreamSynchronize(bt->stream), "batch autodiff");
     bt->mom_M = 0;   // the alpha state is consumed
     return FK_OK;
 }
@@ -531,7 +549,8 @@ int fk_batch_destroy(fk_batch* bt) {
     bt->drop_graphs();
     Buf* bufs[] = {&bt->d_row_ptr, &bt->d_colc, &bt->d_hval, &bt->d_R, &bt->d_V[0], &bt->d_V[1], &bt->d_V[2],
                    &bt->d_V[3], &bt->d_stage, &bt->d_sys, &bt->d_cta_sys, &bt->d_partials, &bt->d_raw, &bt->d_D,
-                   &bt->d_coef, &bt->d_rows, &bt->d_cols, &bt->d_pair, &bt->d_rowscale, &bt->d_rowfac};
+                   &bt->d_coef, &bt->d_rows, &bt->d_cols, &bt->d_pair, &bt->d_rowscale, &bt->d_rowfac,
+                   &bt->d_rowsys, &bt->d_gather, &bt->d_Dout};
     for (auto* b : bufs) b->release();
     if (bt->t0) cudaEventDestroy(bt->t0);
     if (bt->t1) cudaEventDestroy(bt->t1);

@@ -131,10 +131,10 @@ cudaError_t FK_CAT(launch_export_panel, FK_PREC_NAME)(int cplx, const void* src,
     return cudaGetLastError();
 }
 cudaError_t FK_CAT(launch_scale_rows, FK_PREC_NAME)(int cplx, const void* x, void* y, long long n_rows, long long ld,
-                                                  int b, const double* f, cudaStream_t st) {
+                                                  int b, const int* row_sys, const double* f, cudaStream_t st) {
     const int g = helper_grid(n_rows * ld);
-    if (cplx) k_scale_rows<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(x), reinterpret_cast<FK_SYS_C::E*>(y), n_rows, ld, b, f);
-    else k_scale_rows<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(x), reinterpret_cast<FK_SYS_R::E*>(y), n_rows, ld, b, f);
+    if (cplx) k_scale_rows<FK_SYS_C><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_C::E*>(x), reinterpret_cast<FK_SYS_C::E*>(y), n_rows, ld, b, row_sys, f);
+    else k_scale_rows<FK_SYS_R><<<g, 256, 0, st>>>(reinterpret_cast<const FK_SYS_R::E*>(x), reinterpret_cast<FK_SYS_R::E*>(y), n_rows, ld, b, row_sys, f);
     return cudaGetLastError();
 }
 

@@ -465,8 +465,11 @@ static __global__ void k_ds_to_double(double* D, long long n_reals) {
 //   D_k += dscale * sum_s alpha_m[b i + bi, s] conj(beta_{m+1}[b j + bj, s])
 // reusing the gathered beta_{m+1} rows of block k = (i, j).
 // ---------------------------------------------------------------------------------
+// Light configurations (kLightStep) are held to 64 registers, 4 CTAs per SM: on 64 square
+// lattices (b=1, S=32, FP32, 7.4M blocks) a reverse step took 0.32 ms against 0.53 ms at the
+// 96 registers (2 CTAs) the compiler picks otherwise; 3 and 5 CTAs measured 0.38 and 0.36 ms.
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads, 2) k_adjoint_step(AdjArgs a) {
+__global__ void __launch_bounds__(kThreads, kLightStep<S, B, NP> ? 4 : 2) k_adjoint_step(AdjArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
     constexpr int EPT = NP * S::EPP;
@@ -734,14 +737,14 @@ __global__ void k_export_panel(const typename S::E* src, long long n, long long 
     }
 }
 
-// y[r, :] = f[block row of r] * x[r, :] over rows r < n_rows of row-major n x ld vectors (the
-// batched engine's per-system factors, one entry per block row of b rows).
+// y[r, :] = f[row_sys[block row of r]] * x[r, :] over rows r < n_rows of row-major n x ld
+// vectors (the batched engine's per-system factors; row_sys maps a block row of b rows to its system).
 template <class S>
 __global__ void k_scale_rows(const typename S::E* x, typename S::E* y, long long n_rows, long long ld, int b,
-                             const double* f) {
+                             const int* row_sys, const double* f) {
     const long long total = n_rows * ld;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
-        y[q] = S::scale(S::coef(f[(q / ld) / b]), x[q]);
+        y[q] = S::scale(S::coef(f[row_sys[(q / ld) / b]]), x[q]);
 }
 
 // Row-major device vector -> column-major double host layout (for reading back R / state).
@@ -765,6 +768,15 @@ __global__ void k_scale(const typename S::E* x, typename S::E* y, long long n_el
     const typename S::Coef cc = S::coef(c_dev ? *c_dev : c);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_elems; q += (long long)gridDim.x * blockDim.x)
         y[q] = S::scale(cc, x[q]);
+}
+
+// dst block q <- src block idx[q] (per doubles each): D of the prepared patterns back to the
+// caller's block order, in one pass before the copy to the host.
+static __global__ void k_gather_blocks(const double* src, const int* idx, long long n_out, int per, double* dst) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_out * per; q += (long long)gridDim.x * blockDim.x) {
+        const long long blk = q / per;
+        dst[q] = src[(size_t)idx[blk] * per + (q - blk * per)];
+    }
 }
 
 // D <- (D + D^T-pair^dagger)/2 blockwise, then * scale (row_scale[i] per block row when given) (SpMatBsr::symmetrize and

@@ -125,6 +125,15 @@ class SpMatBsr:
         return SpMatBsr(self.n_rows, self.b_len, self.row_ptr.copy(), self.col_idx.copy(), self.val.copy(),
                         complex_values=self.is_complex)
 
+    def with_values(self, val):
+        """A matrix on this pattern whose values are `val` (no copy); the pattern arrays are shared."""
+        m = object.__new__(SpMatBsr)
+        m.n_rows = m.n_cols = self.n_rows
+        m.b_len = self.b_len
+        m.row_ptr, m.col_idx, m.row_idx = self.row_ptr, self.col_idx, self.row_idx
+        m.val = val.reshape(-1)
+        return m
+
     def pattern_like(self, complex_values=None):
         """Same pattern, zero values (the D argument of stoch/autodiff)."""
         cplx = self.is_complex if complex_values is None else complex_values
@@ -477,7 +486,7 @@ class Batch:
             raise L.FkError(st, "batch_create")
         self.h = h
         self.n = 0
-        self.patterns = []   # per system: (block rows, b, row_ptr, col_idx) as added
+        self.patterns = []   # per system: its H pattern as added (values left empty)
 
     def _check(self, st, where):
         if st != L.FK_OK:
@@ -506,7 +515,7 @@ class Batch:
                                           _dp(_as_doubles(H.val)), es.lo, es.hi, s, _dp(_as_doubles(flat)),
                                           C.byref(idx)), "batch_add")
         self.n += 1
-        self.patterns.append((H.n_rows, H.b_len, H.row_ptr.copy(), H.col_idx.copy()))
+        self.patterns.append(SpMatBsr(H.n_rows, H.b_len, H.row_ptr.copy(), H.col_idx.copy(), np.zeros(0)))
         return idx.value
 
     def commit(self):
@@ -517,19 +526,24 @@ class Batch:
         self._check(self.lib.fk_batch_moments(self.h, M, _dp(mu)), "batch_moments")
         return mu.reshape(self.n, M)
 
-    def autodiff_matrix(self, M, c):
+    def autodiff_matrix(self, M, c, out=None):
         """Engine.autodiff_matrix for every system after moments(M): c is (systems, M), one row of
-        coefficients per system; returns one SpMatBsr per system on its own H pattern."""
+        coefficients per system; returns one SpMatBsr per system on its own H pattern. `out` (optional):
+        a contiguous array of all systems' block values, reused across calls (pinned with
+        fk_host_register it is filled at copy-engine speed); the returned matrices are views of it."""
         c = np.ascontiguousarray(c, dtype=np.float64).reshape(self.n, M)
         dt = np.complex128 if self.complex_values else np.float64
-        total = sum(len(ci) * b * b for (_, b, _, ci) in self.patterns)
-        out = np.zeros(total, dt)
+        total = sum(P.n_blocks() * P.b_len ** 2 for P in self.patterns)
+        if out is None:
+            out = np.zeros(total, dt)
+        elif out.dtype != dt or out.size != total or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous %s array of %d values" % (np.dtype(dt).name, total))
         self._check(self.lib.fk_batch_autodiff_matrix(self.h, M, _dp(c), _dp(out.view(np.float64))),
                     "batch_autodiff_matrix")
         Ds, off = [], 0
-        for (n_rows, b, rp, ci) in self.patterns:
-            k = len(ci) * b * b
-            Ds.append(SpMatBsr(n_rows, b, rp, ci, out[off:off + k], complex_values=self.complex_values))
+        for P in self.patterns:
+            k = P.n_blocks() * P.b_len ** 2
+            Ds.append(P.with_values(out[off:off + k]))
             off += k
         return Ds
 

@@ -145,6 +145,12 @@ def test_batch_autodiff_matches_oracle_per_system(gpu, cplx, prec, tol):
     with pytest.raises(L.FkError) as ei:
         bt.autodiff_matrix(M, cs)
     assert ei.value.status == L.FK_ERR_STATE
+    # a caller-provided output buffer: same values, returned matrices are views of it
+    bt.moments(M)
+    out = np.full(sum(D.val.size for D in Ds), np.nan, dtype=Ds[0].val.dtype)
+    Ds2 = bt.autodiff_matrix(M, cs, out=out)
+    assert all(np.array_equal(a.val, b_.val) for a, b_ in zip(Ds, Ds2))
+    assert np.shares_memory(Ds2[-1].val, out)
 
 
 def _without_diagonal(H):
