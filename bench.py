@@ -589,6 +589,13 @@ def run_serve(args):
             "serial_fp64_probe_steps_per_s": work / t_ser, "speedup_vs_serial_fp64": (work / t_ser and
                                                                                   st["probe_steps_per_s"] / (work / t_ser)),
             "moments_max_rel_mu0_vs_fp64": worst, "serial_fp64_requests": n_ser}
+    peak, kind = peaks()
+    gbs = st["algorithmic_bytes"] / max(st["busy_s"], 1e-9) / 1e9
+    line["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                        "over": "time with at least one solve in service (%.2f s of %.2f s wall)"
+                                % (st["busy_s"], st["wall_s"]),
+                        "bytes": "sum of each solve's algorithmic bytes (forward steps + fused reverse steps)",
+                        "peak_source": kind}
     print(json.dumps(line), flush=True)
 
 

@@ -54,6 +54,23 @@ class Request:
     def probe_steps(self):
         return float(self.R.shape[0]) * self.M * self.R.shape[1]
 
+    def algorithmic_bytes(self):
+        """HBM bytes the solve must move at least: M/2 forward steps (read x, z, write y, H once)
+        and, for autodiff, M/2 - 1 reverse steps (read alpha_m, alpha_{m+1}, beta_{m+1},
+        beta_{m+2}, write alpha_{m-1}, beta_m, H once, D read and written as 8-byte reals).
+        A stoch request counts its moments only (a lower bound)."""
+        n, s = self.R.shape
+        sv = {"fp64": 8, "ds": 8, "fp32": 4}[self.precision] * (2 if self.complex_values else 1)
+        b = self.H.b_len
+        nnzb = self.H.n_blocks()
+        h = nnzb * (b * b * sv + 4) + 4 * (self.H.n_rows + 1)
+        fwd = (self.M // 2) * (3.0 * n * s * sv + h)
+        rev = 0.0
+        if self.kind == "autodiff":
+            d = 2.0 * nnzb * b * b * 8 * (2 if self.complex_values else 1)
+            rev = (self.M // 2 - 1) * (6.0 * n * s * sv + h + d)
+        return fwd + rev
+
     def footprint(self):
         """Device bytes an engine needs for this solve (vectors, H, D, scratch)."""
         n, s = self.R.shape
@@ -239,7 +256,16 @@ class Server:
         t0 = min((r.arrival for r in self.completed), default=0.0)
         t1 = max((r.finished for r in self.completed), default=0.0)
         work = sum(r.probe_steps() for r in self.completed)
-        return {"completed": len(self.completed), "rejected": len(self.rejected),
+        # time with at least one solve in service (union of the admitted..finished intervals)
+        busy, end = 0.0, None
+        for a, f in sorted((r.admitted, r.finished) for r in self.completed if r.admitted is not None):
+            if end is None or a > end:
+                busy += f - a
+                end = f
+            elif f > end:
+                busy += f - end
+                end = f
+        return {"busy_s": busy, "algorithmic_bytes": sum(r.algorithmic_bytes() for r in self.completed),"completed": len(self.completed), "rejected": len(self.rejected),
                 "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                 "probe_steps_per_s": work / max(t1 - t0, 1e-9), "wall_s": t1 - t0,
                 "max_concurrent": self.max_concurrent, "budget_bytes": self.budget}
