@@ -374,18 +374,33 @@ int check_staged_error(fk_engine* e) {
     return FK_OK;
 }
 
+// Packets per lane when no option sets them, for rows of P 16-byte packets (measured on GB300;
+// FP32 on 10^6-site and DS / FP64 on 3x10^5-site cubic lattices, b=1 real and b=2 complex, S=32..128,
+// and cubic L=64 S=256 for the widest rows):
+//  * step: 4 from P = 16 (FP32) or 32 (FP64, DS) up, else 2. FP32 b=2 S=64 (P=32): 0.85 ms vs 1.34
+//    with 2; FP64 b=2 S=32 (P=32): 0.96 vs 1.85; FP32 b=1 S=32 (P=8): 0.107 with 2 vs 0.142 with 4.
+//  * outer product: 4 from P = 16 up (DS b=1 S=32: 0.10 vs 0.16 ms; FP64 b=2 S=32: 1.87 vs 2.31).
+//  * adjoint: FP64 4 from P = 16 up (b=2 S=32: 3.74 vs 5.07 ms); DS 4 for b=1 from P = 16 up
+//    (S=128: 0.60 vs 0.74), 2 for b=2 (S=64: 1.61 vs 2.53; cubic L=64 S=256: 5.9 vs 9.3); FP32 4 for
+//    P = 32..64 (b=1 S=128: 0.97 vs 1.11; b=2 S=64: 3.16 vs 3.38), else 2 (b=2 S=32: 1.67 vs 1.95;
+//    cubic L=64 S=256 fused: 3.24 vs 3.52).
+int default_np(int kind, int prec, int P, int b) {
+    if (P < 2) return 1;
+    if (kind == fk::kStep) return P >= (prec == fk::kF32 ? 16 : 32) ? 4 : 2;
+    if (kind == fk::kOuter) return P >= 16 ? 4 : 2;
+    if (prec == fk::kF64) return P >= 16 ? 4 : 2;
+    if (prec == fk::kDS) return b == 1 && P >= 16 ? 4 : 2;
+    return P >= 32 && P <= 64 ? 4 : 2;
+}
+
 int configure(fk_engine* e) {
     for (auto& c : e->cfg) c.valid = false;
     if (e->n_b == 0 || e->s == 0 || e->n != e->n_b * e->b) return FK_OK;   // configured once both are set
     const int P = e->P;
     // Gp lanes per block row, NP packets per lane and column chunk; the kernels walk
     // the row's ceil(P / (Gp * NP)) chunks themselves, so one launch covers all columns.
-    // Each kernel kind has its own NP (register use vs. loads in flight): defaults measured
-    // on the cubic L=64, S=256 workload are 4 for the step and outer kernels and 2 for the
-    // adjoint kernel, whose fused epilogue holds the most live values.
+    // Each kernel kind has its own NP (register use vs. loads in flight, default_np).
     const int slices = 1, W = P;
-    // {step, adjoint, outer} on rows wider than 32 packets
-    const int kDefaultNP[fk::kHelper] = {4, e->prec == fk::kF64 ? 4 : 2, 4};
     const size_t per_blk = (size_t)e->b * e->b * e->hsize() + sizeof(unsigned);
     for (int kind = 0; kind < fk::kHelper; kind++) {
         int NP, Gp;
@@ -393,14 +408,10 @@ int configure(fk_engine* e) {
         if (want > 0) {
             NP = want;
             Gp = std::min(32, next_pow2((P + NP - 1) / NP));
-        } else if (P <= 32) {
-            // narrow rows: two packets per lane (b=1 real FP32, S=32 on a 1024^2 square lattice:
-            // 0.12 ms per step with 4 lanes x 2 packets vs 0.20 ms with 8 lanes x 1)
-            NP = P >= 2 ? 2 : 1;
-            Gp = next_pow2((P + NP - 1) / NP);
         } else {
-            NP = kDefaultNP[kind];
-            Gp = 32;
+            // the lanes that cover a row in one chunk of NP packets each, at most a warp
+            NP = default_np(kind, e->prec, P, e->b);
+            Gp = std::min(32, next_pow2((P + NP - 1) / NP));
         }
         // H blocks per tile of kThreads items: the shared-memory stage size
         const long long items = (long long)e->n_b * Gp;

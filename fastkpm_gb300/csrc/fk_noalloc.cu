@@ -101,7 +101,7 @@ extern "C" int fk_moments_noalloc(int kind, int n_b, int b, const int* d_row_ptr
     const int P = (int)(ld / epp);
     int NP, Gp;
     if (P <= 32) { NP = 1; Gp = next_pow2(P); }
-    else { NP = 4; Gp = 32; }
+    else { NP = 4; Gp = std::min(32, next_pow2((P + 3) / 4)); }   // every lane holds packets
     int occ = 0;
     if (fk::occupancy_f64(fk::kStep, cplx, b, NP, 0, &occ) != cudaSuccess || occ < 1) { cudaGetLastError(); return FK_ERR_CUDA; }
     int dev = 0, sms = 1;
