@@ -232,8 +232,22 @@ __device__ __forceinline__ Tile tile_range(const int* row_ptr, const SysDesc& sd
 template <class S, int B, int NP>
 constexpr bool kLightStep = B * NP * S::EPP * (int)sizeof(typename S::E) <= 32;
 
+// CTAs per SM each kernel is compiled for (the register cap is 65536 / (256 x CTAs)). Measured
+// per launch on GB300 against 2 CTAs (128 registers):
+//  * step, FP32 and b=1 float-float at 3: cubic L=64 S=256 b=2 FP32 0.78 vs 0.92 ms; b=2 S=128
+//    (10^6 sites) 1.65 vs 2.13; b=1 S=128 FP32 0.31 vs 0.39, float-float 0.32 vs 0.37; b=2
+//    float-float stays at 2 (cubic L=64: 3.04 ms at 3 vs 2.65, spills);
+//  * outer product, b=1 at 3: S=128 FP32 0.42 vs 0.51 ms, float-float 0.34 vs 0.38; b=2 at 2
+//    (FP32 cubic L=64: 1.59 ms at 3 vs 1.36).
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads, kLightStep<S, B, NP> ? 6 : 2) k_cheb_step(StepArgs a) {
+constexpr int kStepCtas = kLightStep<S, B, NP> ? 6 : (S::PREC == 1 || (S::PREC == 2 && B == 1)) ? 3 : 2;
+template <class S, int B, int NP>
+constexpr int kOuterCtas = (B == 1 && S::PREC != 0) ? 3 : 2;
+template <class S, int B, int NP>
+constexpr int kAdjointCtas = kLightStep<S, B, NP> ? 4 : 2;
+
+template <class S, int B, int NP>
+__global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(StepArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
     constexpr int EPT = NP * S::EPP;
@@ -465,11 +479,11 @@ static __global__ void k_ds_to_double(double* D, long long n_reals) {
 //   D_k += dscale * sum_s alpha_m[b i + bi, s] conj(beta_{m+1}[b j + bj, s])
 // reusing the gathered beta_{m+1} rows of block k = (i, j).
 // ---------------------------------------------------------------------------------
-// Light configurations (kLightStep) are held to 64 registers, 4 CTAs per SM: on 64 square
+// kAdjointCtas: light configurations (kLightStep) are held to 64 registers, 4 CTAs per SM: on 64 square
 // lattices (b=1, S=32, FP32, 7.4M blocks) a reverse step took 0.32 ms against 0.53 ms at the
 // 96 registers (2 CTAs) the compiler picks otherwise; 3 and 5 CTAs measured 0.38 and 0.36 ms.
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads, kLightStep<S, B, NP> ? 4 : 2) k_adjoint_step(AdjArgs a) {
+__global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_step(AdjArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
     constexpr int EPT = NP * S::EPP;
@@ -604,7 +618,7 @@ __global__ void __launch_bounds__(kThreads, kLightStep<S, B, NP> ? 4 : 2) k_adjo
 // the lanes, FP64 accumulation into Dacc.
 // ---------------------------------------------------------------------------------
 template <class S, int B, int NP>
-__global__ void __launch_bounds__(kThreads, 2) k_outer(OuterArgs a) {
+__global__ void __launch_bounds__(kThreads, kOuterCtas<S, B, NP>) k_outer(OuterArgs a) {
     typedef typename S::E E;
     constexpr int EPT = NP * S::EPP;
     const int sidx = a.cta_sys[blockIdx.x];

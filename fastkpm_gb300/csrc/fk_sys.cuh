@@ -69,7 +69,7 @@ __device__ __forceinline__ double ds_to_double(float2 a) { return (double)a.x + 
 struct SysF64R {
     typedef double E; typedef double H; typedef double Hr; typedef double Acc;
     typedef double Coef; typedef double RowDot; typedef double Dot; typedef double OAcc;
-    static constexpr bool CPLX = false; static constexpr int EPP = 2;
+    static constexpr bool CPLX = false; static constexpr int EPP = 2; static constexpr int PREC = 0;   // 0 FP64, 1 FP32, 2 float-float
     __device__ static Coef coef(double c) { return c; }
     __device__ static Acc zero() { return 0.0; }
     __device__ static Hr hreal(H h) { return h; }
@@ -106,7 +106,7 @@ struct SysF64R {
 struct SysF64C {
     typedef double2 E; typedef double2 H; typedef double Hr; typedef double2 Acc;
     typedef double Coef; typedef double RowDot; typedef double Dot; typedef double2 OAcc;
-    static constexpr bool CPLX = true; static constexpr int EPP = 1;
+    static constexpr bool CPLX = true; static constexpr int EPP = 1; static constexpr int PREC = 0;   // 0 FP64, 1 FP32, 2 float-float
     __device__ static Coef coef(double c) { return c; }
     __device__ static Acc zero() { return make_double2(0.0, 0.0); }
     __device__ static Hr hreal(H h) { return h.x; }
@@ -153,7 +153,7 @@ struct SysF64C {
 struct SysF32R {
     typedef float E; typedef float H; typedef float Hr; typedef float Acc;
     typedef float Coef; typedef float RowDot; typedef float2 Dot; typedef float OAcc;
-    static constexpr bool CPLX = false; static constexpr int EPP = 4;
+    static constexpr bool CPLX = false; static constexpr int EPP = 4; static constexpr int PREC = 1;   // 0 FP64, 1 FP32, 2 float-float
     __device__ static Coef coef(double c) { return __double2float_rn(c); }
     __device__ static Acc zero() { return 0.f; }
     __device__ static Hr hreal(H h) { return h; }
@@ -194,7 +194,7 @@ struct SysF32R {
 struct SysF32C {
     typedef float2 E; typedef float2 H; typedef float Hr; typedef float2 Acc;
     typedef float Coef; typedef float RowDot; typedef float2 Dot; typedef float2 OAcc;
-    static constexpr bool CPLX = true; static constexpr int EPP = 2;
+    static constexpr bool CPLX = true; static constexpr int EPP = 2; static constexpr int PREC = 1;   // 0 FP64, 1 FP32, 2 float-float
     __device__ static Coef coef(double c) { return __double2float_rn(c); }
     __device__ static Acc zero() { return make_float2(0.f, 0.f); }
     __device__ static Hr hreal(H h) { return h.x; }
@@ -246,7 +246,7 @@ struct SysF32C {
 struct SysDSR {
     typedef float2 E; typedef float2 H; typedef float2 Hr; typedef float2 Acc;
     typedef float2 Coef; typedef float2 RowDot; typedef float2 Dot; typedef float2 OAcc;
-    static constexpr bool CPLX = false; static constexpr int EPP = 2;
+    static constexpr bool CPLX = false; static constexpr int EPP = 2; static constexpr int PREC = 2;   // 0 FP64, 1 FP32, 2 float-float
     __device__ static Coef coef(double c) { return ds_from_double(c); }
     __device__ static Acc zero() { return make_float2(0.f, 0.f); }
     __device__ static Hr hreal(H h) { return h; }
@@ -295,7 +295,7 @@ struct SysDSR {
 struct SysDSC {
     typedef float4 E; typedef float4 H; typedef float2 Hr; typedef float4 Acc;
     typedef float2 Coef; typedef float2 RowDot; typedef float2 Dot; typedef float4 OAcc;
-    static constexpr bool CPLX = true; static constexpr int EPP = 1;
+    static constexpr bool CPLX = true; static constexpr int EPP = 1; static constexpr int PREC = 2;   // 0 FP64, 1 FP32, 2 float-float
     __device__ static float2 re(float4 v) { return make_float2(v.x, v.y); }
     __device__ static float2 im(float4 v) { return make_float2(v.z, v.w); }
     __device__ static float4 pack(float2 r, float2 i) { return make_float4(r.x, r.y, i.x, i.y); }
