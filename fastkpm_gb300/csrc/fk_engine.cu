@@ -417,10 +417,11 @@ int configure(fk_engine* e) {
         const long long items = (long long)e->n_b * Gp;
         const long long tiles = (items + fk::kThreads - 1) / fk::kThreads;
         const int nk_max = fk::max_tile_blocks(e->h_row_ptr.data(), e->n_b, Gp);
-        // FK_OPT_STAGE_H 2 (default): stage except in the FP32 step kernel, where the barrier
-        // around the stage cost more than the re-read H blocks (0.96 vs 1.03 ms per step on
-        // cubic L=64, S=256); the FP64 and DS step kernels run 12-25% faster staged.
-        const bool stage = e->opt_stage == 2 ? !(kind == fk::kStep && e->prec == fk::kF32) : e->opt_stage != 0;
+        // FK_OPT_STAGE_H 2 (default): stage except in FP32 kernels, where the barrier around the
+        // stage costs more than the re-read H blocks (cubic L=64, S=256: step 0.96 vs 1.03 ms,
+        // adjoint 3.13 vs 3.24; 10^6-site cubic b=1 S=128 adjoint 0.82 vs 0.97); the FP64 and
+        // DS step kernels run 12-25% faster staged.
+        const bool stage = e->opt_stage == 2 ? e->prec != fk::kF32 : e->opt_stage != 0;
         const int stage_cap = (stage && nk_max * per_blk <= 48 * 1024) ? nk_max : 0;
         KCfg& c = e->cfg[kind];
         c.Gp = Gp; c.NP = NP; c.slices = slices; c.W = W;
@@ -1420,16 +1421,17 @@ int fk_engine_set_H(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, 
 
 namespace {
 // Device address through which kernels can read the host buffer [R, R + bytes), or null.
+// Registered (pinned) buffers are read through their device mapping; other host memory is read
+// by its own address where the system gives the GPU pageable-memory access.
 const double* device_readable(const fk_engine* e, const double* R, size_t bytes) {
-    if (e->pageable_access) return R;
     cudaPointerAttributes a0, a1;
-    if (cudaPointerGetAttributes(&a0, R) != cudaSuccess || cudaPointerGetAttributes(&a1, (const char*)R + bytes - 1) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer) return nullptr;
-    if ((const char*)a1.devicePointer - (const char*)a0.devicePointer != (ptrdiff_t)(bytes - 1)) return nullptr;
-    return reinterpret_cast<const double*>(a0.devicePointer);
+    if (cudaPointerGetAttributes(&a0, R) == cudaSuccess &&
+        cudaPointerGetAttributes(&a1, (const char*)R + bytes - 1) == cudaSuccess && a0.type == cudaMemoryTypeHost &&
+        a1.type == cudaMemoryTypeHost && a0.devicePointer && a1.devicePointer &&
+        (const char*)a1.devicePointer - (const char*)a0.devicePointer == (ptrdiff_t)(bytes - 1))
+        return reinterpret_cast<const double*>(a0.devicePointer);
+    cudaGetLastError();
+    return e->pageable_access ? R : nullptr;
 }
 }  // namespace
 

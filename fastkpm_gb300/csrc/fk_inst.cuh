@@ -8,9 +8,14 @@
 namespace fk {
 
 namespace {
+// Rows whose chunks are all whole (P a multiple of Gp * NP, e.g. every power-of-two S) run the
+// instance without packet masks: 2-5% faster per launch (float-float cubic L=64 S=256: step
+// 2.55 vs 2.65 ms, outer product 5.12 vs 5.39).
+inline bool whole_chunks(int P, int Gp, int NP) { return Gp > 0 && P % (Gp * NP) == 0; }
 template <class S, int B, int NP>
 cudaError_t step_one(const StepArgs& a, const Launch& l) {
-    k_cheb_step<S, B, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    if (whole_chunks(a.P, a.Gp, NP)) k_cheb_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    else k_cheb_step<S, B, NP, false><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     return cudaGetLastError();
 }
 template <class S, int B, int NP, bool TMA>
@@ -29,12 +34,14 @@ cudaError_t staged_one(const StepArgs& a, const StageTables& t, const Launch& l,
 }
 template <class S, int B, int NP>
 cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
-    k_adjoint_step<S, B, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    if (whole_chunks(a.P, a.Gp, NP)) k_adjoint_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    else k_adjoint_step<S, B, NP, false><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     return cudaGetLastError();
 }
 template <class S, int B, int NP>
 cudaError_t outer_one(const OuterArgs& a, const Launch& l) {
-    k_outer<S, B, NP><<<l.grid, kThreads, 0, l.stream>>>(a);
+    if (whole_chunks(a.P, a.Gp, NP)) k_outer<S, B, NP, true><<<l.grid, kThreads, 0, l.stream>>>(a);
+    else k_outer<S, B, NP, false><<<l.grid, kThreads, 0, l.stream>>>(a);
     return cudaGetLastError();
 }
 template <class S, int B, int NP>

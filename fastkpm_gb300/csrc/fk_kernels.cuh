@@ -95,9 +95,10 @@ union Packet {
     E e[EPP];
 };
 
-// Packets base + g + q*Gp (q < NP) of one row, masked to pk < P.
+// Packets base + g + q*Gp (q < NP) of one row, masked to pk < P (FULL: every chunk of the
+// row is whole, P a multiple of Gp * NP, and no mask is needed).
 // Gathered rows are read-only for the whole kernel: non-coherent path.
-template <class S, int NP>
+template <class S, int NP, bool FULL = false>
 __device__ __forceinline__ void ld_nc(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int base, int g,
                                       int Gp, int P) {
     constexpr int EPP = S::EPP;
@@ -106,12 +107,12 @@ __device__ __forceinline__ void ld_nc(typename S::E (&v)[NP * S::EPP], const typ
         const int pk = base + g + Gp * q;
         Packet<typename S::E, EPP> pkt;
         pkt.u = make_uint4(0u, 0u, 0u, 0u);
-        if (pk < P) pkt.u = __ldg(reinterpret_cast<const uint4*>(row) + pk);
+        if (FULL || pk < P) pkt.u = __ldg(reinterpret_cast<const uint4*>(row) + pk);
 #pragma unroll
         for (int e = 0; e < EPP; e++) v[q * EPP + e] = pkt.e[e];
     }
 }
-template <class S, int NP>
+template <class S, int NP, bool FULL = false>
 __device__ __forceinline__ void ld_rw(typename S::E (&v)[NP * S::EPP], const typename S::E* row, int base, int g,
                                       int Gp, int P) {
     constexpr int EPP = S::EPP;
@@ -120,12 +121,12 @@ __device__ __forceinline__ void ld_rw(typename S::E (&v)[NP * S::EPP], const typ
         const int pk = base + g + Gp * q;
         Packet<typename S::E, EPP> pkt;
         pkt.u = make_uint4(0u, 0u, 0u, 0u);
-        if (pk < P) pkt.u = reinterpret_cast<const uint4*>(row)[pk];
+        if (FULL || pk < P) pkt.u = reinterpret_cast<const uint4*>(row)[pk];
 #pragma unroll
         for (int e = 0; e < EPP; e++) v[q * EPP + e] = pkt.e[e];
     }
 }
-template <class S, int NP>
+template <class S, int NP, bool FULL = false>
 __device__ __forceinline__ void st(typename S::E* row, const typename S::E (&v)[NP * S::EPP], int base, int g, int Gp,
                                    int P) {
     constexpr int EPP = S::EPP;
@@ -135,7 +136,7 @@ __device__ __forceinline__ void st(typename S::E* row, const typename S::E (&v)[
         Packet<typename S::E, EPP> pkt;
 #pragma unroll
         for (int e = 0; e < EPP; e++) pkt.e[e] = v[q * EPP + e];
-        if (pk < P) reinterpret_cast<uint4*>(row)[pk] = pkt.u;
+        if (FULL || pk < P) reinterpret_cast<uint4*>(row)[pk] = pkt.u;
     }
 }
 
@@ -246,7 +247,7 @@ constexpr int kOuterCtas = (B == 1 && S::PREC != 0) ? 3 : 2;
 template <class S, int B, int NP>
 constexpr int kAdjointCtas = kLightStep<S, B, NP> ? 4 : 2;
 
-template <class S, int B, int NP>
+template <class S, int B, int NP, bool FULL = false>
 __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(StepArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
@@ -301,7 +302,7 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(Ste
 #pragma unroll
                 for (int bj = 0; bj < B; bj++) {
                     E xv[EPT];
-                    ld_nc<S, NP>(xv, x + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                    ld_nc<S, NP, FULL>(xv, x + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
                     mac_block<S, B, NP>(acc, cc >> 30, hk, xv, bj);
                 }
             }
@@ -310,17 +311,17 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(Ste
             for (int bi = 0; bi < B; bi++) {
                 const size_t roff = (size_t)(B * i + bi) * a.ld;
                 E zv[EPT], yv[EPT];
-                if (a.has_z) ld_rw<S, NP>(zv, z + roff, base, g, Gp, P);
+                if (a.has_z) ld_rw<S, NP, FULL>(zv, z + roff, base, g, Gp, P);
                 else {
 #pragma unroll
                     for (int e = 0; e < EPT; e++) zv[e] = S::to(S::zero());
                 }
 #pragma unroll
                 for (int e = 0; e < EPT; e++) yv[e] = S::fin(acc[bi][e], a.two != 0, a.has_z != 0, zv[e]);
-                st<S, NP>(y + roff, yv, base, g, Gp, P);
+                st<S, NP, FULL>(y + roff, yv, base, g, Gp, P);
                 if (a.want_dots || a.xi_mode == 1) {
                     E xo[EPT];
-                    ld_nc<S, NP>(xo, x + roff, base, g, Gp, P);
+                    ld_nc<S, NP, FULL>(xo, x + roff, base, g, Gp, P);
                     if (a.want_dots) {
 #pragma unroll
                         for (int e = 0; e < EPT; e++) { S::rd_nrm(rxx, xo[e]); S::rd_re(ryx, yv[e], xo[e]); }
@@ -334,19 +335,19 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(Ste
                             S::axpy(t2, c1, yv[e]);
                             xv2[e] = S::to(t2);
                         }
-                        st<S, NP>(xi + roff, xv2, base, g, Gp, P);
+                        st<S, NP, FULL>(xi + roff, xv2, base, g, Gp, P);
                     }
                 }
                 if (a.xi_mode == 2) {
                     E xv2[EPT];
-                    ld_rw<S, NP>(xv2, xi + roff, base, g, Gp, P);
+                    ld_rw<S, NP, FULL>(xv2, xi + roff, base, g, Gp, P);
 #pragma unroll
                     for (int e = 0; e < EPT; e++) {
                         typename S::Acc t2 = S::from(xv2[e]);
                         S::axpy(t2, c1, yv[e]);
                         xv2[e] = S::to(t2);
                     }
-                    st<S, NP>(xi + roff, xv2, base, g, Gp, P);
+                    st<S, NP, FULL>(xi + roff, xv2, base, g, Gp, P);
                 }
             }
             if (a.want_dots) { S::dot_add(dxx, rxx); S::dot_add(dyx, ryx); }
@@ -482,7 +483,7 @@ static __global__ void k_ds_to_double(double* D, long long n_reals) {
 // kAdjointCtas: light configurations (kLightStep) are held to 64 registers, 4 CTAs per SM: on 64 square
 // lattices (b=1, S=32, FP32, 7.4M blocks) a reverse step took 0.32 ms against 0.53 ms at the
 // 96 registers (2 CTAs) the compiler picks otherwise; 3 and 5 CTAs measured 0.38 and 0.36 ms.
-template <class S, int B, int NP>
+template <class S, int B, int NP, bool FULL = false>
 __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_step(AdjArgs a) {
     typedef typename S::E E;
     typedef typename S::H H;
@@ -537,7 +538,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
             E Ai[B][EPT];
 #pragma unroll
             for (int bi = 0; bi < B; bi++) {
-                if (active) ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                if (active) ld_nc<S, NP, FULL>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
                 else {
 #pragma unroll
                     for (int e = 0; e < EPT; e++) Ai[bi][e] = S::to(S::zero());
@@ -567,8 +568,8 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
                 for (int bj = 0; bj < B; bj++) {
                     E av[EPT], bv[EPT];
                     if (has) {
-                        ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
-                        ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        ld_nc<S, NP, FULL>(av, A + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        ld_nc<S, NP, FULL>(bv, Bv + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
                         mac_block<S, B, NP>(accA, cc >> 30, hk, av, bj);
                         mac_block<S, B, NP>(accB, cc >> 30, hk, bv, bj);
                     } else {
@@ -589,8 +590,8 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
                 for (int bi = 0; bi < B; bi++) {
                     const size_t roff = (size_t)(B * i + bi) * a.ld;
                     E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
-                    ld_rw<S, NP>(apv, Ap + roff, base, g, Gp, P);
-                    ld_rw<S, NP>(bpv, Bp + roff, base, g, Gp, P);
+                    ld_rw<S, NP, FULL>(apv, Ap + roff, base, g, Gp, P);
+                    ld_rw<S, NP, FULL>(bpv, Bp + roff, base, g, Gp, P);
 #pragma unroll
                     for (int e = 0; e < EPT; e++) {
                         an[e] = S::fin(accA[bi][e], true, true, apv[e]);
@@ -600,8 +601,8 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
                         S::axpy(tb, cAn, an[e]);
                         bn[e] = S::to(tb);
                     }
-                    st<S, NP>(Ap + roff, an, base, g, Gp, P);
-                    st<S, NP>(Bp + roff, bn, base, g, Gp, P);
+                    st<S, NP, FULL>(Ap + roff, an, base, g, Gp, P);
+                    st<S, NP, FULL>(Bp + roff, bn, base, g, Gp, P);
                 }
             }
         }
@@ -617,7 +618,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
 // column chunk, partner rows gathered once per block, transposed reduction over
 // the lanes, FP64 accumulation into Dacc.
 // ---------------------------------------------------------------------------------
-template <class S, int B, int NP>
+template <class S, int B, int NP, bool FULL = false>
 __global__ void __launch_bounds__(kThreads, kOuterCtas<S, B, NP>) k_outer(OuterArgs a) {
     typedef typename S::E E;
     constexpr int EPT = NP * S::EPP;
@@ -650,8 +651,8 @@ __global__ void __launch_bounds__(kThreads, kOuterCtas<S, B, NP>) k_outer(OuterA
 #pragma unroll
             for (int bi = 0; bi < B; bi++) {
                 if (active) {
-                    ld_nc<S, NP>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
-                    if (two_terms) ld_nc<S, NP>(Bi[bi], Bv + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                    ld_nc<S, NP, FULL>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                    if (two_terms) ld_nc<S, NP, FULL>(Bi[bi], Bv + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
                     else {
 #pragma unroll
                         for (int e = 0; e < EPT; e++) Bi[bi][e] = S::to(S::zero());
@@ -675,8 +676,8 @@ __global__ void __launch_bounds__(kThreads, kOuterCtas<S, B, NP>) k_outer(OuterA
                 for (int bj = 0; bj < B; bj++) {
                     E bv[EPT], av[EPT];
                     if (has) {
-                        ld_nc<S, NP>(bv, Bv + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
-                        if (two_terms) ld_nc<S, NP>(av, A + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        ld_nc<S, NP, FULL>(bv, Bv + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        if (two_terms) ld_nc<S, NP, FULL>(av, A + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
                         else {
 #pragma unroll
                             for (int e = 0; e < EPT; e++) av[e] = S::to(S::zero());

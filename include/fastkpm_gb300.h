@@ -73,7 +73,7 @@ int  fk_engine_synchronize(fk_engine* e);
 #define FK_OPT_FUSE_D      0   /* fuse the outer product into the adjoint step when D's pattern is H's: 1 always, 0 never, 2 (default): FP32, FP64 */
 #define FK_OPT_NP          1   /* packets per lane: 0 auto, or 1, 2, 4                                           */
 #define FK_OPT_CTAS_PER_SM 2   /* 0 auto (occupancy), else a cap on CTAs per SM                                   */
-#define FK_OPT_STAGE_H     3   /* 1: stage H blocks in shared memory, 0: never, 2 (default): not in the FP32 step */
+#define FK_OPT_STAGE_H     3   /* 1: stage H blocks in shared memory, 0: never, 2 (default): not in FP32 kernels */
 #define FK_OPT_GRAPHS      4   /* 1: capture the M-step recursions in CUDA graphs and replay them                 */
 #define FK_OPT_NP_STEP     5   /* packets per lane of the step kernel only (0: FK_OPT_NP / default)               */
 #define FK_OPT_NP_ADJOINT  6   /* ... of the adjoint kernel only                                                  */
