@@ -404,11 +404,10 @@ __device__ __forceinline__ void group_sum_transposed(typename S::OAcc (&v)[V], i
             off >>= 1;
         }
     }
-    for (; off > 0; off >>= 1) {
-#pragma unroll
-        for (int i = 0; i < V; i++)
-            if (i < cur) v[i] = S::oa_add(v[i], S::oa_shfl(v[i], off));
-    }
+    // lanes left over after the transposed levels: those levels ran all log2(V) times, so one
+    // value per lane remains (cur == 1) and plain butterflies finish it
+    (void)cur;
+    for (; off > 0; off >>= 1) v[0] = S::oa_add(v[0], S::oa_shfl(v[0], off));
 }
 
 // Early read of the first D entry a writer lane updates for block k (8 bytes per real:
