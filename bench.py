@@ -157,9 +157,9 @@ def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
 
 
 # DRAM bytes per row of one DS adjoint launch from the ncu capture on the cubic L=32 case
-# (profiles/k_adjoint_step_ds_cubic32.md: 1.253 GB read + 0.508 GB written for 65,536 rows);
+# (profiles/k_adjoint_step_ds_cubic32.md: 1.269 GB read + 0.508 GB written for 65,536 rows);
 # traffic grows in proportion to the rows, so the L=64 launch's traffic is this times N.
-ADJ_DS_TRAFFIC_PER_ROW = (1.252655e9 + 0.507823e9) / 65536
+ADJ_DS_TRAFFIC_PER_ROW = (1.269302e9 + 0.508060e9) / 65536
 
 
 # ---------------------------------------------------------------------------- arms

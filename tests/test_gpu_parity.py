@@ -115,6 +115,22 @@ def test_launch_options_do_not_change_results(gpu, opts):
     assert rel_err(D, D_ref) <= 1e-10
 
 
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+@pytest.mark.parametrize("S", [32, 40])
+@pytest.mark.parametrize("fuse", [0, 1])
+def test_whole_and_ragged_column_chunks(gpu, prec, S, fuse):
+    # S = 32 complex: every kernel's rows split into whole chunks (the unmasked instances);
+    # S = 40: the last chunk is ragged (the masked instances). Both against the oracle.
+    H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=9)
+    R = fk.probe_uncorrelated(H.n_rows * H.b_len, S, fk.RNG(9), complex_values=True)
+    M = 16
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    for kind in ("autodiff", "stoch"):
+        mu, mu_ref, D, D_ref = run_pair(H, es, R, True, prec, M, c, kind, {L.FK_OPT_FUSE_D: fuse})
+        assert mu_err(mu, mu_ref) <= TOL_MU[prec]
+        assert rel_err(D, D_ref) <= TOL_D[prec]
+
+
 @pytest.mark.parametrize("M", [2, 4, 6])
 def test_autodiff_small_orders(gpu, M):
     H, es, R = small_real_case(6, 8, 2)
