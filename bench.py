@@ -156,10 +156,10 @@ def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
     return vec + h + d
 
 
-# DRAM bytes per row of one DS adjoint launch from the ncu capture on the cubic L=32 case
-# (profiles/k_adjoint_step_ds_cubic32.md: 1.269 GB read + 0.508 GB written for 65,536 rows);
+# DRAM bytes per row of one fused DS adjoint launch from the ncu capture on the cubic L=32 case
+# (profiles/k_adjoint_step_ds_cubic32.md: 1.277 GB read + 0.522 GB written for 65,536 rows);
 # traffic grows in proportion to the rows, so the L=64 launch's traffic is this times N.
-ADJ_DS_TRAFFIC_PER_ROW = (1.269302e9 + 0.508060e9) / 65536
+ADJ_DS_TRAFFIC_PER_ROW = (1.277403e9 + 0.521811e9) / 65536
 
 
 # ---------------------------------------------------------------------------- arms
@@ -204,12 +204,12 @@ def run_gb300(args, rank, ws, dist):
     n_step, t_step = prof[0]
     sv = 8 if args.precision == "fp32" else 16
     fuse_opt = eng.get_option(Lb.FK_OPT_FUSE_D)
-    fused = fuse_opt == 1 or (fuse_opt == 2 and args.precision != "ds")
+    fused = fuse_opt != 0
     bytes_adj = adjoint_bytes_per_launch(N, S, H.n_blocks(), 2, sv, fused)
     avg_adj_ms = t_adj / max(n_adj, 1)
     achieved = bytes_adj / (avg_adj_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    traffic = ADJ_DS_TRAFFIC_PER_ROW * N if (args.precision == "ds" and S == 256 and not fused) else None
+    traffic = ADJ_DS_TRAFFIC_PER_ROW * N if (args.precision == "ds" and S == 256 and fused) else None
     launches = sum(v[0] for v in prof.values())
 
     # ---- end to end through the public API with pinned host buffers ----

@@ -799,11 +799,11 @@ int autodiff_enqueue(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb
         fk::k_adjoint_coefs<<<1, fk::kPostThreads, 0, e->stream>>>(c_dev, M, e->d_coef.as<double>());
         FK_TRY(cudaGetLastError(), "coefficient table launch");
     }
-    // FK_OPT_FUSE_D: 1 always fuse (when D's pattern is H's), 0 never, 2 (default) by precision.
-    // Measured per reverse step on cubic L=64, S=256: FP32 fused 3.24 ms vs 3.52 apart (the fused
-    // kernel saves two gathered vector reads), FP64 29.2 vs 30.4 (the outer product is FP64-pipe
-    // bound either way), DS 11.7 vs 11.4 (float-float epilogue registers cost the adjoint more).
-    const bool fuse_pref = e->opt_fuse_d == 2 ? e->prec != fk::kDS : e->opt_fuse_d != 0;
+    // FK_OPT_FUSE_D: 0 never fuse, otherwise (1, 2 = default) fuse when D's pattern is H's.
+    // Measured per reverse step on cubic L=64, S=256 (the fused kernel saves the outer product's
+    // two gathered vector reads): FP32 3.10 ms fused vs 3.28 apart, DS 10.66 vs 10.92, FP64
+    // 29.2 vs 30.4; 10^6-site cubic b=1 S=128: FP32 0.80 vs 1.00, DS 0.82 vs 0.91.
+    const bool fuse_pref = e->opt_fuse_d != 0;
     const bool fuse = fuse_pref && e->d_same_as_H;
     // buffers: alpha_m in A, alpha_{m+1} in Ap (moments left alpha_{M/2-1}, alpha_{M/2})
     const double* scales = e->d_coef.as<double>() + nadj;   // [2 c_{M-1}, diag]

@@ -70,7 +70,7 @@ const char* fk_engine_last_error(const fk_engine* e);
 int  fk_engine_set_stream(fk_engine* e, void* cuda_stream);
 int  fk_engine_synchronize(fk_engine* e);
 /* Engine options: FK_OPT_* below. */
-#define FK_OPT_FUSE_D      0   /* fuse the outer product into the adjoint step when D's pattern is H's: 1 always, 0 never, 2 (default): FP32, FP64 */
+#define FK_OPT_FUSE_D      0   /* fuse the outer product into the adjoint step when D's pattern is H's: 1 or 2 (default) yes, 0 never */
 #define FK_OPT_NP          1   /* packets per lane: 0 auto, or 1, 2, 4                                           */
 #define FK_OPT_CTAS_PER_SM 2   /* 0 auto (occupancy), else a cap on CTAs per SM                                   */
 #define FK_OPT_STAGE_H     3   /* 1: stage H blocks in shared memory, 0: never, 2 (default): not in FP32 kernels */
