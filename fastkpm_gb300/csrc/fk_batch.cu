@@ -433,7 +433,7 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
     void* Ap = V[(M / 2 - 1) & 1];
     void* Bv = V[2];
     void* Bp = V[3];
-    const bool fuse = bt->prec != fk::kDS;   // the single engine's default
+    const bool fuse = true;   // the single engine's default: the D epilogue rides on the adjoint step
     auto outer = [&](const void* a, const void* bv, double alpha) -> int {
         fk::OuterArgs o;
         o.sys = bt->d_sys.as<SysDesc>();
