@@ -162,6 +162,79 @@ def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
 ADJ_DS_TRAFFIC_PER_ROW = (1.277403e9 + 0.521811e9) / 65536
 
 
+def probe_entries(R):
+    """Nonzeros of a probe block, k per row (k = the most any row has; shorter rows padded with
+    column 0 and value 0, which adds nothing): (s, cols (n, k), vals (n, k))."""
+    nz = R != 0
+    k = max(1, int(nz.sum(axis=1).max()))
+    n = R.shape[0]
+    cols = np.zeros((n, k), np.int32)
+    vals = np.zeros((n, k), R.dtype)
+    rows, cs = np.nonzero(nz)
+    slot = np.arange(len(rows)) - np.searchsorted(rows, rows)
+    cols[rows, slot] = cs
+    vals[rows, slot] = R[rows, cs]
+    return R.shape[1], cols, vals
+
+
+def run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse):
+    """moments + autodiff_matrix through the public API, every step uploading H and the probes
+    from pinned host memory and reading mu and D back; wall and device clocks, max over ranks."""
+    lib = Lb.load()
+    hv = np.ascontiguousarray(H.val)
+    if sparse:
+        s, cols, vals = probe_entries(R)
+        cols = np.ascontiguousarray(cols)
+        vals = np.ascontiguousarray(vals)
+        probe_bufs = [cols, vals]
+    else:
+        Rf = np.asfortranarray(R)
+        probe_bufs = [Rf]
+    pinned = all(lib.fk_host_register(b.ctypes.data, b.nbytes) == 0 for b in probe_bufs + [hv])
+    e2 = fk.Engine(True, args.precision, device=dev)
+
+    def set_probes():
+        if sparse:
+            e2.set_R_sparse(R.shape[0], s, cols, vals)
+        else:
+            e2.set_R(Rf)
+
+    e2.set_H(H, es)
+    set_probes()
+    e2.moments(M)
+    e2.autodiff_matrix(c, D)
+    barrier(dist)
+    e2.synchronize()
+    phases = np.zeros(4)   # wall ms per step: set_H, set_R, moments (+ mu read), autodiff (+ D read)
+    t0 = time.perf_counter()
+    e2.timer_start()
+    for _ in range(args.steps):
+        tp = [time.perf_counter()]
+        e2.set_H(H, es)
+        tp.append(time.perf_counter())
+        set_probes()
+        tp.append(time.perf_counter())
+        e2.moments(M)
+        tp.append(time.perf_counter())
+        e2.autodiff_matrix(c, D)
+        tp.append(time.perf_counter())
+        phases += np.diff(tp) * 1e3
+    e2_ms_dev = e2.timer_stop()
+    e2_ms_wall = (time.perf_counter() - t0) * 1e3
+    barrier(dist)
+    e2_ms = max_over_ranks(dist, max(e2_ms_dev, e2_ms_wall))
+    h2d = int(H.row_ptr.nbytes + H.col_idx.nbytes + hv.nbytes + sum(b.nbytes for b in probe_bufs))
+    d2h = int(M * 8 + D.val.nbytes)
+    for b in probe_bufs + [hv]:
+        lib.fk_host_unregister(b.ctypes.data)
+    e2.close()
+    return {"value": per_solve * args.steps * ws / (e2_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": e2_ms / args.steps, "host_buffers_pinned": pinned,
+            "probes": "nonzeros (set_R_sparse)" if sparse else "dense n x S (set_R)",
+            "phases_ms_per_step": {k: float(v) / args.steps for k, v in
+                                   zip(["set_H", "set_R", "moments", "autodiff_matrix"], phases)}}
+
+
 # ---------------------------------------------------------------------------- arms
 def run_gb300(args, rank, ws, dist):
     import fastkpm_gb300 as fk
@@ -213,49 +286,13 @@ def run_gb300(args, rank, ws, dist):
     launches = sum(v[0] for v in prof.values())
 
     # ---- end to end through the public API with pinned host buffers ----
-    e2e = None
+    # The probe block goes up as its nonzeros (set_R_sparse: colour probes have one entry per row
+    # and realisation, 21 MB here) for "e2e", and as the dense column-major n x S block (set_R,
+    # what the reference's transfer_R moves, 2.1 GB) for "e2e_dense_R"; H, mu and D as in both.
+    e2e = e2e_dense = None
     if not args.no_e2e:
-        lib = Lb.load()
-        Rf = np.asfortranarray(R)
-        hv = np.ascontiguousarray(H.val)
-        pinned = lib.fk_host_register(Rf.ctypes.data, Rf.nbytes) == 0
-        pinned = (lib.fk_host_register(hv.ctypes.data, hv.nbytes) == 0) and pinned
-        e2 = fk.Engine(True, args.precision, device=dev)
-        mu_h = np.zeros(M)
-        for _ in range(1):
-            e2.set_H(H, es)
-            e2.set_R(Rf)
-            e2.moments(M)
-            e2.autodiff_matrix(c, D)
-        barrier(dist)
-        e2.synchronize()
-        phases = np.zeros(4)   # wall ms per step: set_H, set_R, moments (+ mu read), autodiff (+ D read)
-        t0 = time.perf_counter()
-        e2.timer_start()
-        for _ in range(args.steps):
-            tp = [time.perf_counter()]
-            e2.set_H(H, es)
-            tp.append(time.perf_counter())
-            e2.set_R(Rf)
-            tp.append(time.perf_counter())
-            mu_h = e2.moments(M)
-            tp.append(time.perf_counter())
-            e2.autodiff_matrix(c, D)
-            tp.append(time.perf_counter())
-            phases += np.diff(tp) * 1e3
-        e2_ms_dev = e2.timer_stop()
-        e2_ms_wall = (time.perf_counter() - t0) * 1e3
-        barrier(dist)
-        e2_ms = max_over_ranks(dist, max(e2_ms_dev, e2_ms_wall))
-        h2d = int(H.row_ptr.nbytes + H.col_idx.nbytes + hv.nbytes + Rf.nbytes)
-        d2h = int(M * 8 + D.val.nbytes)
-        e2e = {"value": per_solve * args.steps * ws / (e2_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2_ms / args.steps, "host_buffers_pinned": pinned,
-               "phases_ms_per_step": {k: float(v) / args.steps for k, v in
-                                      zip(["set_H", "set_R", "moments", "autodiff_matrix"], phases)}}
-        lib.fk_host_unregister(Rf.ctypes.data)
-        lib.fk_host_unregister(hv.ctypes.data)
-        e2.close()
+        e2e = run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse=True)
+        e2e_dense = run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse=False)
 
     # ---- error vs the FP64 engine on the same workload (bounded: M = 40) ----
     err = None
@@ -278,7 +315,7 @@ def run_gb300(args, rank, ws, dist):
                "vs": "native FP64 GPU engine, same H and R, M=%d" % Mv}
     eng.close()
     return dict(value=value, ms=ms_max, clocks=clk.summary(), prof=prof, achieved=achieved, peak=peak,
-                peak_kind=peak_kind, traffic=traffic, launches=launches, e2e=e2e, err=err, N=N, S=S, M=M,
+                peak_kind=peak_kind, traffic=traffic, launches=launches, e2e=e2e, e2e_dense=e2e_dense, err=err, N=N, S=S, M=M,
                 nnzb=H.n_blocks(), mu0=float(mu[0]), bytes_adj=bytes_adj, fused=fused, avg_adj_ms=avg_adj_ms,
                 avg_step_ms=t_step / max(n_step, 1), n_adj=n_adj, n_step=n_step)
 
@@ -515,9 +552,10 @@ def serve_requests(n_req, seed, max_sites):
                 H, es = W.square_lattice(L, -1.0, 1.0, seed + k)
                 px, py = {32: (8, 4), 64: (8, 8), 128: (16, 8)}[S]
                 groups = W.square_colour_groups(L, px, py)
-        R = W.phase_probes(groups, 1, seed + k, complex_values=spin)
+        # colour probes travel as their nonzeros (one per row): Engine.set_R_sparse
+        entries = W.phase_probe_entries(groups, 1, seed + k, complex_values=spin)
         c = W.fermi_coefficients(M, es, "fermi_energy")
-        reqs.append(dict(H=H, es=es, R=R, M=M, c=c, t=t, spin=spin))
+        reqs.append(dict(H=H, es=es, entries=entries, n=len(groups), M=M, c=c, t=t, spin=spin))
     return reqs
 
 
@@ -552,7 +590,8 @@ def run_serve(args):
         now = time.perf_counter() - t0
         if r["t"] > now:
             time.sleep(r["t"] - now)
-        tickets.append(srv.submit(Request(r["H"], r["es"], r["R"], r["M"], r["c"], "autodiff", "fp32")))
+        tickets.append(srv.submit(Request(r["H"], r["es"], None, r["M"], r["c"], "autodiff", "fp32",
+                                          R_entries=r["entries"])))
     srv.drain()
     st = srv.stats()
     srv.stop()
@@ -567,14 +606,14 @@ def run_serve(args):
             break
         eng = fk.Engine(r["spin"], "fp64")
         eng.set_H(r["H"], r["es"])
-        eng.set_R(r["R"])
+        eng.set_R_sparse(r["n"], *r["entries"])
         t = time.perf_counter()
         mu = eng.moments(r["M"])
         D = r["H"].pattern_like(r["spin"])
         eng.autodiff_matrix(r["c"], D)
         t_ser += time.perf_counter() - t
         eng.close()
-        work_ser += float(r["R"].shape[0]) * r["M"] * r["R"].shape[1]
+        work_ser += float(r["n"]) * r["M"] * r["entries"][0]
         n_ser += 1
         if tk.error is None:
             worst = max(worst, _mu_err(tk.mu, mu))
@@ -734,6 +773,7 @@ def main():
                      "avg_launch_ms": r["avg_adj_ms"], "launches": r["n_adj"]},
         "cpu_baseline": cpu,
         "e2e": r["e2e"],
+        "e2e_dense_R": r["e2e_dense"],
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "err_vs_fp64": r["err"],

@@ -42,6 +42,7 @@ SIGNATURES = {
     "fk_engine_set_H": (_i, [_p, _i, _i, _i, _ip, _ip, _dp, _d, _d]),
     "fk_engine_set_R": (_i, [_p, _i, _i, _dp]),
     "fk_engine_get_R": (_i, [_p, _dp]),
+    "fk_engine_set_R_sparse": (_i, [_p, _i, _i, _i, _ip, _dp]),
     "fk_engine_moments": (_i, [_p, _i, _dp]),
     "fk_engine_moments_async": (_i, [_p, _i]),
     "fk_engine_fetch_moments": (_i, [_p, _dp]),

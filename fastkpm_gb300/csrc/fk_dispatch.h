@@ -42,7 +42,9 @@ inline int elems_per_packet(int prec, int cplx) { return 16 / elem_bytes(prec, c
     cudaError_t launch_export_panel_##P(int cplx, const void* src, long long n, long long ld, long long c0, \
                                         int w, double* dst, cudaStream_t st);                               \
     cudaError_t launch_scale_rows_##P(int cplx, const void* x, void* y, long long n_rows, long long ld,     \
-                                      int b, const int* row_sys, const double* f, cudaStream_t st);
+                                      int b, const int* row_sys, const double* f, cudaStream_t st);        \
+    cudaError_t launch_expand_sparse_##P(int cplx, const int* cols, const double* vals, long long n, int k,  \
+                                         long long ld, void* dst, cudaStream_t st);
 FK_DECLARE_PREC(f64)
 FK_DECLARE_PREC(f32)
 FK_DECLARE_PREC(ds)

@@ -205,6 +205,13 @@ cudaError_t prec_load_colmajor(fk_engine* e, const double* src, long long n, int
         default: return fk::launch_load_colmajor_ds(e->cplx, src, n, ncols, c0, e->ld, dst, e->stream);
     }
 }
+cudaError_t prec_expand_sparse(fk_engine* e, const int* cols, const double* vals, long long n, int k, void* dst) {
+    switch (e->prec) {
+        case fk::kF64: return fk::launch_expand_sparse_f64(e->cplx, cols, vals, n, k, e->ld, dst, e->stream);
+        case fk::kF32: return fk::launch_expand_sparse_f32(e->cplx, cols, vals, n, k, e->ld, dst, e->stream);
+        default: return fk::launch_expand_sparse_ds(e->cplx, cols, vals, n, k, e->ld, dst, e->stream);
+    }
+}
 cudaError_t prec_store_colmajor(fk_engine* e, const void* src, long long n, int ncols, double* dst) {
     switch (e->prec) {
         case fk::kF64: return fk::launch_store_colmajor_f64(e->cplx, src, n, ncols, e->ld, dst, e->stream);
@@ -1496,6 +1503,42 @@ int fk_engine_set_R(fk_engine* e, int n, int s, const double* R) {
     for (auto& v : e->d_V) FK_TRY(cudaMemsetAsync(v.p, 0, e->vec_bytes(), e->stream), "clear work vector");
     rc = upload_colmajor(e, R, n, s, e->d_R.p);
     if (rc != FK_OK) return rc;
+    e->mom_M = 0;
+    e->mom_a0 = e->mom_a1 = -2;
+    return configure(e);
+}
+
+int fk_engine_set_R_sparse(fk_engine* e, int n, int s, int k, const int* cols, const double* vals) {
+    if (!e) return FK_ERR_ARG;
+    cudaSetDevice(e->device);
+    if (n <= 0) return e->fail(FK_ERR_ARG, "set_R_sparse: n must be positive");
+    if (s <= 0) return e->fail(FK_ERR_ARG, "set_R_sparse: cannot handle an empty R (s = %d)", s);
+    if (k <= 0 || !cols || !vals) return e->fail(FK_ERR_ARG, "set_R_sparse: need k >= 1 entries per row and their arrays");
+    const size_t nk = (size_t)n * k;
+    for (size_t t = 0; t < nk; t++)
+        if (cols[t] < 0 || cols[t] >= s)
+            return e->fail(FK_ERR_ARG, "set_R_sparse: column %d of entry %zu outside [0, %d)", cols[t], t, s);
+    const int epp = e->epp();
+    e->n = n;
+    e->s = s;
+    e->ld = ((long long)s + epp - 1) / epp * epp;
+    e->P = (int)(e->ld / epp);
+    int rc = ensure_vectors(e);
+    if (rc != FK_OK) return rc;
+    FK_TRY(cudaMemsetAsync(e->d_R.p, 0, e->vec_bytes(), e->stream), "clear R");
+    for (auto& v : e->d_V) FK_TRY(cudaMemsetAsync(v.p, 0, e->vec_bytes(), e->stream), "clear work vector");
+    const size_t cw = e->cplx ? 2 : 1;
+    const size_t col_bytes = (sizeof(int) * nk + 15) / 16 * 16;
+    FK_TRY(e->d_stage.ensure(col_bytes + sizeof(double) * nk * cw), "alloc probe entries");
+    int* d_cols = e->d_stage.as<int>();
+    double* d_vals = reinterpret_cast<double*>(e->d_stage.as<char>() + col_bytes);
+    FK_TRY(cudaMemcpyAsync(d_cols, cols, sizeof(int) * nk, cudaMemcpyHostToDevice, e->stream), "upload probe columns");
+    FK_TRY(cudaMemcpyAsync(d_vals, vals, sizeof(double) * nk * cw, cudaMemcpyHostToDevice, e->stream), "upload probe values");
+    {
+        ProfScope ps(e, fk::kHelper);
+        FK_TRY(prec_expand_sparse(e, d_cols, d_vals, n, k, e->d_R.p), "probe expansion kernel");
+    }
+    FK_TRY(cudaStreamSynchronize(e->stream), "set_R_sparse");
     e->mom_M = 0;
     e->mom_a0 = e->mom_a1 = -2;
     return configure(e);

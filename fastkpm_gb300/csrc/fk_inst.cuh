@@ -145,4 +145,12 @@ cudaError_t FK_CAT(launch_scale_rows, FK_PREC_NAME)(int cplx, const void* x, voi
     return cudaGetLastError();
 }
 
+cudaError_t FK_CAT(launch_expand_sparse, FK_PREC_NAME)(int cplx, const int* cols, const double* vals, long long n, int k,
+                                                     long long ld, void* dst, cudaStream_t st) {
+    const int g = helper_grid(n);
+    if (cplx) k_expand_sparse<FK_SYS_C><<<g, 256, 0, st>>>(cols, vals, n, k, ld, reinterpret_cast<FK_SYS_C::E*>(dst));
+    else k_expand_sparse<FK_SYS_R><<<g, 256, 0, st>>>(cols, vals, n, k, ld, reinterpret_cast<FK_SYS_R::E*>(dst));
+    return cudaGetLastError();
+}
+
 }  // namespace fk

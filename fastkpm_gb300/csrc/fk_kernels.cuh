@@ -709,6 +709,24 @@ __global__ void __launch_bounds__(kThreads, kOuterCtas<S, B, NP>) k_outer(OuterA
 // transposed through shared memory so that both the column reads and the row writes are
 // contiguous across a warp (launched with 32 x 8 threads).
 constexpr int kTransposeTile = 32;
+// Sparse probe block -> row-major engine vector (already zeroed): row i holds k entries,
+// R[i, cols[i k + q]] += vals[i k + q] (complex: interleaved (re, im) pairs). One thread per
+// row, so repeated columns of a row add up without races. Colour (correlated) probes have
+// one entry per row and realisation: ~20 bytes per row instead of S elements.
+template <class S>
+__global__ void k_expand_sparse(const int* cols, const double* vals, long long n, int k, long long ld,
+                                typename S::E* dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        for (int q = 0; q < k; q++) {
+            const long long t = i * k + q;
+            typename S::E* p = dst + i * ld + cols[t];
+            const double2 add = S::CPLX ? make_double2(vals[2 * t], vals[2 * t + 1]) : make_double2(vals[t], 0.0);
+            const double2 cur = S::to_double2(*p);
+            *p = S::from_double2(make_double2(cur.x + add.x, cur.y + add.y));
+        }
+    }
+}
+
 template <class S>
 __global__ void k_load_colmajor(const double* src, long long n, int ncols, int c0, long long ld, typename S::E* dst) {
     constexpr int T = kTransposeTile;

@@ -262,6 +262,7 @@ class Engine:
         self.h = h
         self.R = None
         self.R2 = None
+        self._r_shape = None
         self.es = None
         self._H = None
 
@@ -339,9 +340,21 @@ class Engine:
         flat = _as_doubles(R.reshape(-1, order="F")) if not np.iscomplexobj(R) else \
             np.ascontiguousarray(R.reshape(-1, order="F"), dtype=np.complex128).view(np.float64)
         self._check(self.lib.fk_engine_set_R(self.h, n, s, _dp(flat)), "transfer_R")
+        self._r_shape = (n, s)
+
+    def set_R_sparse(self, n, s, cols, vals):
+        """Upload the probe block from its nonzeros, k per row: R[i, cols[i, q]] += vals[i, q]
+        (cols, vals of shape (n, k)); every other entry is zero. The public R is not kept."""
+        dt = np.complex128 if self.complex_values else np.float64
+        cols = np.ascontiguousarray(cols, dtype=np.int32).reshape(n, -1)
+        vals = np.ascontiguousarray(vals, dtype=dt).reshape(cols.shape)
+        self._check(self.lib.fk_engine_set_R_sparse(self.h, n, s, cols.shape[1], _ip(cols),
+                                                    _dp(vals.view(np.float64))), "set_R_sparse")
+        self.R = self.R2 = None
+        self._r_shape = (n, s)
 
     def get_R(self):
-        n, s = self.R.shape
+        n, s = self._r_shape
         dt = np.complex128 if self.complex_values else np.float64
         flat = np.zeros(n * s, dt)
         self._check(self.lib.fk_engine_get_R(self.h, _dp(flat.view(np.float64))), "get_R")

@@ -26,19 +26,33 @@ from .engine import Engine
 
 class Request:
     """One KPM solve: moments(M), then autodiff_matrix(c, D) ("autodiff") or
-    stoch_matrix(c, D) ("stoch") on H's pattern."""
+    stoch_matrix(c, D) ("stoch") on H's pattern. The probe block is R (dense, n x s) or, for
+    colour probes, R_entries = (s, cols, vals): its nonzeros, k per row (Engine.set_R_sparse)."""
 
     _next = 0
     _lock = threading.Lock()
 
-    def __init__(self, H, es, R, M, c, kind="autodiff", precision="fp32", arrival=None):
+    def __init__(self, H, es, R, M, c, kind="autodiff", precision="fp32", arrival=None, R_entries=None):
         with Request._lock:
             self.id = Request._next
             Request._next += 1
-        self.H, self.es, self.R, self.M, self.c = H, es, np.asfortranarray(R), int(M), np.asarray(c, float)
+        if (R is None) == (R_entries is None):
+            raise ValueError("give the probe block as R or as R_entries, not both")
+        self.H, self.es, self.M, self.c = H, es, int(M), np.asarray(c, float)
+        if R is not None:
+            self.R = np.asfortranarray(R)
+            self.R_entries = None
+            self.n_rows, self.s = self.R.shape
+            cplx_r = np.iscomplexobj(R)
+        else:
+            s, cols, vals = R_entries
+            self.R = None
+            self.R_entries = (int(s), np.asarray(cols), np.asarray(vals))
+            self.n_rows, self.s = len(self.R_entries[1]), int(s)
+            cplx_r = np.iscomplexobj(vals)
         self.kind = kind
         self.precision = precision
-        self.complex_values = bool(np.iscomplexobj(R) or H.is_complex)
+        self.complex_values = bool(cplx_r or H.is_complex)
         self.arrival = time.perf_counter() if arrival is None else arrival
         self.admitted = None
         self.finished = None
@@ -52,14 +66,14 @@ class Request:
         return None if self.finished is None else self.finished - self.arrival
 
     def probe_steps(self):
-        return float(self.R.shape[0]) * self.M * self.R.shape[1]
+        return float(self.n_rows) * self.M * self.s
 
     def algorithmic_bytes(self):
         """HBM bytes the solve must move at least: M/2 forward steps (read x, z, write y, H once)
         and, for autodiff, M/2 - 1 reverse steps (read alpha_m, alpha_{m+1}, beta_{m+1},
         beta_{m+2}, write alpha_{m-1}, beta_m, H once, D read and written as 8-byte reals).
         A stoch request counts its moments only (a lower bound)."""
-        n, s = self.R.shape
+        n, s = self.n_rows, self.s
         sv = {"fp64": 8, "ds": 8, "fp32": 4}[self.precision] * (2 if self.complex_values else 1)
         b = self.H.b_len
         nnzb = self.H.n_blocks()
@@ -73,7 +87,7 @@ class Request:
 
     def footprint(self):
         """Device bytes an engine needs for this solve (vectors, H, D, scratch)."""
-        n, s = self.R.shape
+        n, s = self.n_rows, self.s
         es = {"fp64": 8, "ds": 8, "fp32": 4}[self.precision] * (2 if self.complex_values else 1)
         epp = 16 // es
         ld = (s + epp - 1) // epp * epp
@@ -120,7 +134,11 @@ class _Slot:
             try:
                 eng = self.engine(req)
                 eng.set_H(req.H, req.es)
-                eng.set_R(req.R)
+                if req.R is not None:
+                    eng.set_R(req.R)
+                else:
+                    s, cols, vals = req.R_entries
+                    eng.set_R_sparse(req.n_rows, s, cols, vals)
                 req.mu = eng.moments(req.M)
                 D = req.H.pattern_like(req.complex_values)
                 if req.kind == "autodiff":

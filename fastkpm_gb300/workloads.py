@@ -145,6 +145,25 @@ def phase_probes(groups, realisations=1, seed=0, complex_values=True):
     return R
 
 
+def phase_probe_entries(groups, realisations=1, seed=0, complex_values=True):
+    """phase_probes as its nonzeros: (s, cols, vals) with cols, vals of shape (n, realisations), the
+    same seeded phases, so that R[i, cols[i, r]] = vals[i, r] is phase_probes(groups, ...)."""
+    rng = np.random.default_rng(seed)
+    groups = np.asarray(groups)
+    n = len(groups)
+    G = int(groups.max()) + 1
+    cols = np.empty((n, realisations), np.int32)
+    vals = np.empty((n, realisations), np.complex128 if complex_values else np.float64)
+    for r in range(realisations):
+        if complex_values:
+            ph = np.exp(2j * np.pi * rng.random(n))
+        else:
+            ph = rng.choice([-1.0, 1.0], n)
+        cols[:, r] = r * G + groups
+        vals[:, r] = ph / np.sqrt(realisations)
+    return realisations * G, cols, vals
+
+
 def fermi_coefficients(M, es, kind="fermi_density", kT=0.0, mu=0.0, Mq=None):
     """Jackson-damped zero-temperature Fermi expansion (Mq = 2M unless given)."""
     return expansion_coefficients(M, Mq or 2 * M, kind, kT, mu, es)

@@ -97,6 +97,11 @@ int  fk_engine_set_H(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr,
 /* Engine<T>::transfer_R() (reference src/engine_cusparse.cpp:675-699): upload the column-major
  * n x s probe block R. s must be >= 1 (the reference exits on an empty R). */
 int  fk_engine_set_R(fk_engine* e, int n, int s, const double* R);
+/* The same probe block given by its nonzeros, k per row (the structure set_R_correlated produces,
+ * reference src/engine.cpp:76-116: one entry per row and realisation): R[i, cols[i*k+q]] += vals[i*k+q]
+ * (complex: interleaved pairs), every other entry zero. Uploads ~(4 + 8 or 16) k bytes per row
+ * instead of s values. Columns must lie in [0, s) (FK_ERR_ARG otherwise). */
+int  fk_engine_set_R_sparse(fk_engine* e, int n, int s, int k, const int* cols, const double* vals);
 /* Read back the device copy of R (column-major n x s), converted to double. */
 int  fk_engine_get_R(fk_engine* e, double* R);
 

@@ -131,6 +131,40 @@ def test_whole_and_ragged_column_chunks(gpu, prec, S, fuse):
         assert rel_err(D, D_ref) <= TOL_D[prec]
 
 
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+def test_sparse_probe_upload_equals_dense(gpu, prec):
+    # set_R_sparse (nonzeros, k per row) builds the same device R as set_R of the dense block
+    H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=4)
+    groups = W.cubic_colour_groups(4, 2)
+    R = W.phase_probes(groups, realisations=2, seed=6)
+    s, cols, vals = W.phase_probe_entries(groups, realisations=2, seed=6)
+    M = 16
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    out = []
+    for sparse in (False, True):
+        eng = fk.Engine(True, prec)
+        eng.set_H(H, es)
+        if sparse:
+            eng.set_R_sparse(R.shape[0], s, cols, vals)
+        else:
+            eng.set_R(R)
+        assert np.array_equal(eng.get_R(), R.astype(np.complex128)) or prec != "fp64"
+        mu = eng.moments(M)
+        D = H.pattern_like(True)
+        eng.autodiff_matrix(c, D)
+        out.append((mu, D.val))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    # repeated columns of a row add up; a column outside [0, s) is refused
+    eng = fk.Engine(False, prec)
+    eng.set_H(*W.square_lattice(4, -1.0, 1.0, 1))
+    eng.set_R_sparse(16, 3, np.tile([[1, 1]], (16, 1)), np.full((16, 2), 0.5))
+    Rr = eng.get_R()
+    assert np.allclose(Rr[:, 1], 1.0) and np.allclose(Rr[:, [0, 2]], 0.0)
+    with pytest.raises(L.FkError) as ei:
+        eng.set_R_sparse(16, 3, np.full((16, 1), 3), np.ones((16, 1)))
+    assert ei.value.status == L.FK_ERR_ARG
+
+
 @pytest.mark.parametrize("M", [2, 4, 6])
 def test_autodiff_small_orders(gpu, M):
     H, es, R = small_real_case(6, 8, 2)

@@ -37,3 +37,25 @@ def test_algorithmic_bytes_formula():
     assert r.algorithmic_bytes() == fwd + rev
     r2 = Request(H, es, np.ones((n, S)), M, np.zeros(M), "stoch", "fp32")
     assert r2.algorithmic_bytes() == fwd
+
+
+def test_phase_probe_entries_expand_to_phase_probes():
+    groups = W.cubic_colour_groups(4, 2)
+    for cplx in (True, False):
+        for real in (1, 2):
+            R = W.phase_probes(groups, realisations=real, seed=5, complex_values=cplx)
+            s, cols, vals = W.phase_probe_entries(groups, realisations=real, seed=5, complex_values=cplx)
+            D = np.zeros((len(groups), s), vals.dtype)
+            for q in range(cols.shape[1]):
+                np.add.at(D, (np.arange(len(groups)), cols[:, q]), vals[:, q])
+            assert D.shape == R.shape and np.array_equal(D, R)
+
+
+def test_request_with_probe_entries():
+    H, es = W.square_lattice(5, -1.0, 1.0, seed=2)
+    s, cols, vals = W.phase_probe_entries(np.arange(H.n_rows) % 4, 1, seed=3, complex_values=False)
+    r = Request(H, es, None, 10, np.zeros(10), "autodiff", "fp32", R_entries=(s, cols, vals))
+    assert (r.n_rows, r.s) == (H.n_rows, 4) and r.probe_steps() == H.n_rows * 10 * 4
+    import pytest
+    with pytest.raises(ValueError):
+        Request(H, es, np.ones((H.n_rows, 4)), 10, np.zeros(10), R_entries=(s, cols, vals))
