@@ -160,6 +160,11 @@ def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
 # (profiles/k_adjoint_step_ds_cubic32.md: 1.277 GB read + 0.522 GB written for 65,536 rows);
 # traffic grows in proportion to the rows, so the L=64 launch's traffic is this times N.
 ADJ_DS_TRAFFIC_PER_ROW = (1.277403e9 + 0.521811e9) / 65536
+# Warp instructions per row of the same launch (smsp__inst_executed.sum = 1,084,435,072 for 65,536
+# rows): the fused float-float adjoint is bound by instruction issue, not by DRAM. Issue peak of
+# the GPU: 152 SMs x 4 schedulers x 1 warp instruction per cycle at the maximum SM clock.
+ADJ_DS_WARP_INST_PER_ROW = 1084435072 / 65536
+ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
 
 
 def probe_entries(R):
@@ -283,6 +288,15 @@ def run_gb300(args, rank, ws, dist):
     achieved = bytes_adj / (avg_adj_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     traffic = ADJ_DS_TRAFFIC_PER_ROW * N if (args.precision == "ds" and S == 256 and fused) else None
+    issue = None
+    if traffic is not None:
+        clk_mhz = max(clk.summary().get("sm_mhz") or 2070.0, 1.0)
+        inst_rate = ADJ_DS_WARP_INST_PER_ROW * N / (avg_adj_ms * 1e-3)          # warp instructions / s
+        peak_rate = ISSUE_PEAK_WARP_INST_PER_CYCLE * clk_mhz * 1e6
+        issue = {"bound": "instruction issue (FP32 pipe: float-float arithmetic)", "achieved": inst_rate / 1e12,
+                 "peak": peak_rate / 1e12, "unit": "T warp-instructions/s", "frac": inst_rate / peak_rate,
+                 "instructions": "ncu smsp__inst_executed.sum of the L=32 launch scaled by rows (profiles/)",
+                 "peak_clock_mhz": clk_mhz}
     launches = sum(v[0] for v in prof.values())
 
     # ---- end to end through the public API with pinned host buffers ----
@@ -315,7 +329,7 @@ def run_gb300(args, rank, ws, dist):
                "vs": "native FP64 GPU engine, same H and R, M=%d" % Mv}
     eng.close()
     return dict(value=value, ms=ms_max, clocks=clk.summary(), prof=prof, achieved=achieved, peak=peak,
-                peak_kind=peak_kind, traffic=traffic, launches=launches, e2e=e2e, e2e_dense=e2e_dense, err=err, N=N, S=S, M=M,
+                peak_kind=peak_kind, traffic=traffic, launches=launches, e2e=e2e, e2e_dense=e2e_dense, issue=issue, err=err, N=N, S=S, M=M,
                 nnzb=H.n_blocks(), mu0=float(mu[0]), bytes_adj=bytes_adj, fused=fused, avg_adj_ms=avg_adj_ms,
                 avg_step_ms=t_step / max(n_step, 1), n_adj=n_adj, n_step=n_step)
 
@@ -772,6 +786,7 @@ def main():
                      "peak_source": r["peak_kind"], "bytes_per_launch": r["bytes_adj"],
                      "avg_launch_ms": r["avg_adj_ms"], "launches": r["n_adj"]},
         "cpu_baseline": cpu,
+        "roofline_issue": r["issue"],
         "e2e": r["e2e"],
         "e2e_dense_R": r["e2e_dense"],
         "gpu_launches": r["launches"],
