@@ -418,6 +418,13 @@ int configure(fk_engine* e) {
         } else {
             // the lanes that cover a row in one chunk of NP packets each, at most a warp
             NP = default_np(kind, e->prec, P, e->b);
+            // small systems: more lanes per row (fewer packets each) until the launch offers one
+            // CTA's worth of (row, lane) items per SM, so that latency-bound solves spread over the
+            // GPU (square L=32, S=64 FP64, 1,024 rows: 8 lanes give 32 CTAs; with 32 lanes a
+            // moments + stoch_matrix solve takes 2.2 ms instead of 3.4)
+            while (NP > 1 && next_pow2((P + NP - 1) / NP) < 32 &&
+                   (long long)e->n_b * next_pow2((P + NP - 1) / NP) < (long long)e->num_sms * fk::kThreads)
+                NP >>= 1;
             Gp = std::min(32, next_pow2((P + NP - 1) / NP));
         }
         // H blocks per tile of kThreads items: the shared-memory stage size
