@@ -17,6 +17,7 @@ FK_KERNEL_STEP, FK_KERNEL_ADJOINT, FK_KERNEL_OUTER, FK_KERNEL_HELPER = 0, 1, 2, 
 FK_OPT_FUSE_D, FK_OPT_NP, FK_OPT_CTAS_PER_SM, FK_OPT_STAGE_H, FK_OPT_GRAPHS = 0, 1, 2, 3, 4
 FK_OPT_NP_STEP, FK_OPT_NP_ADJOINT, FK_OPT_NP_OUTER, FK_OPT_TMA = 5, 6, 7, 8
 FK_OPT_UPLOAD = 9
+FK_OPT_PRIORITY = 10
 
 PRECISIONS = {"fp64": FK_PREC_FP64, "fp32": FK_PREC_FP32, "ds": FK_PREC_DS}
 

@@ -71,6 +71,7 @@ struct fk_engine {
     int num_sms = 1;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    int opt_priority = 0;   // CUDA priority of the engine's own stream
     std::string err;
 
     // options
@@ -1374,6 +1375,20 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             if (value < 0 || value > 1) return e->fail(FK_ERR_ARG, "UPLOAD must be 0 or 1");
             e->opt_upload = value;
             return FK_OK;
+        case FK_OPT_PRIORITY: {
+            if (!e->own_stream) return e->fail(FK_ERR_STATE, "PRIORITY applies to the engine's own stream, not a caller's");
+            int least = 0, greatest = 0;
+            FK_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest), "priority range");
+            const int p = std::max(greatest, std::min(least, value));
+            if (p == e->opt_priority) return FK_OK;
+            cudaStream_t ns = nullptr;
+            FK_TRY(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, p), "stream create");
+            cudaStreamSynchronize(e->stream);
+            cudaStreamDestroy(e->stream);
+            e->stream = ns;
+            e->opt_priority = p;
+            return FK_OK;
+        }
         case FK_OPT_TMA:
             if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "TMA must be 0, 1 or 2");
             e->opt_tma = value;
@@ -1398,6 +1413,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_STAGE_H: *value = e->opt_stage; return FK_OK;
         case FK_OPT_GRAPHS: *value = e->opt_graphs; return FK_OK;
         case FK_OPT_UPLOAD: *value = e->opt_upload; return FK_OK;
+        case FK_OPT_PRIORITY: *value = e->opt_priority; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }

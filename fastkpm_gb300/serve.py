@@ -8,7 +8,9 @@ run concurrently on the device, and a request that arrives while others are
 running starts as soon as a slot and its memory are free. Probe and recursion
 state stay on the device for the whole solve (moments -> autodiff_matrix).
 Every kernel's per-system reduction order depends only on that system, so a
-request's result is the same alone and in any mix.
+request's result is the same alone and in any mix. Solves whose algorithmic traffic is
+below `urgent_bytes` run on a high-priority CUDA stream, so that short requests are not
+queued behind the CTAs of long ones.
 
     srv = Server(max_slots=8, memory_budget=100 << 30)
     t = srv.submit(Request(H, es, R, M, c))
@@ -133,6 +135,10 @@ class _Slot:
                 continue
             try:
                 eng = self.engine(req)
+                # short solves run on an urgent stream so their launches are not queued behind
+                # the CTAs of long solves sharing the GPU (lower p50 latency)
+                urgent = req.algorithmic_bytes() < self.server.urgent_bytes
+                eng.set_option(L.FK_OPT_PRIORITY, -100 if urgent else 0)
                 eng.set_H(req.H, req.es)
                 if req.R is not None:
                     eng.set_R(req.R)
@@ -154,8 +160,10 @@ class _Slot:
 
 
 class Server:
-    def __init__(self, device=0, max_slots=8, memory_budget=None, lookahead=64, max_bypass=16):
+    def __init__(self, device=0, max_slots=8, memory_budget=None, lookahead=64, max_bypass=16,
+                 urgent_bytes=100e9):
         self.device = device
+        self.urgent_bytes = float(urgent_bytes)   # solves moving less than this get the urgent stream
         if memory_budget is None:
             memory_budget = int(0.8 * self.device_free(device))
         self.budget = int(memory_budget)

@@ -165,6 +165,22 @@ def test_sparse_probe_upload_equals_dense(gpu, prec):
     assert ei.value.status == L.FK_ERR_ARG
 
 
+def test_stream_priority_option(gpu):
+    # the engine's own stream can be recreated with a CUDA priority (clamped to the device's
+    # range); results do not depend on it
+    H, es, R = small_real_case(8, 16, 5)
+    M = 20
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    base = run_pair(H, es, R, False, "fp32", M, c, "autodiff")
+    urgent = run_pair(H, es, R, False, "fp32", M, c, "autodiff", {L.FK_OPT_PRIORITY: -100})
+    assert np.array_equal(base[0], urgent[0]) and np.array_equal(base[2], urgent[2])
+    eng = fk.Engine(False, "fp32")
+    eng.set_option(L.FK_OPT_PRIORITY, -100)
+    assert eng.get_option(L.FK_OPT_PRIORITY) <= 0
+    eng.set_option(L.FK_OPT_PRIORITY, 5)
+    assert eng.get_option(L.FK_OPT_PRIORITY) == 0
+
+
 @pytest.mark.parametrize("M", [2, 4, 6])
 def test_autodiff_small_orders(gpu, M):
     H, es, R = small_real_case(6, 8, 2)
