@@ -18,6 +18,7 @@ FK_OPT_FUSE_D, FK_OPT_NP, FK_OPT_CTAS_PER_SM, FK_OPT_STAGE_H, FK_OPT_GRAPHS = 0,
 FK_OPT_NP_STEP, FK_OPT_NP_ADJOINT, FK_OPT_NP_OUTER, FK_OPT_TMA = 5, 6, 7, 8
 FK_OPT_UPLOAD = 9
 FK_OPT_PRIORITY = 10
+FK_OPT_ADJ_SPLIT = 11
 
 PRECISIONS = {"fp64": FK_PREC_FP64, "fp32": FK_PREC_FP32, "ds": FK_PREC_DS}
 

@@ -477,6 +477,7 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
             a.Dacc = fuse ? bt->d_D.as<double>() : nullptr;
             a.dscale = 2.0;
             a.stage_cap = bt->stage_cap;
+            a.split = 0;
             BT_TRY(batch_launch_adjoint(bt, a, fk::Launch{bt->grid, bt->smem, bt->stream}), "batched adjoint launch");
             std::swap(A, Ap);
             std::swap(Bv, Bp);

@@ -10,7 +10,8 @@
 namespace fk {
 
 enum Prec { kF64 = 0, kF32 = 1, kDS = 2 };
-enum KernelKind { kStep = 0, kAdjoint = 1, kOuter = 2, kHelper = 3, kNumKinds = 4, kStepStaged = 5, kStepStagedAsync = 6 };
+enum KernelKind { kStep = 0, kAdjoint = 1, kOuter = 2, kHelper = 3, kNumKinds = 4, kStepStaged = 5, kStepStagedAsync = 6,
+                  kAdjointSplit = 7 };
 
 struct Launch {
     int grid;

@@ -55,6 +55,7 @@ struct KCfg {
     DevBuf sys, cta_sys;
     bool valid = false;
     bool staged = false;   // step kind only: TMA-staged gathers (k_cheb_step_staged)
+    bool split = false;    // adjoint kind only: two passes over the blocks (k_adjoint_split)
     int umax = 0;          // largest per-tile gather list
 };
 
@@ -113,6 +114,7 @@ struct fk_engine {
     cudaStream_t copy_stream = nullptr;
     int pageable_access = 0;   // the GPU reads any host memory (cudaDevAttrPageableMemoryAccess)
     int opt_upload = 0;        // FK_OPT_UPLOAD: 0 read device-readable host R directly, 1 staging copies
+    int opt_adj_split = 2;     // FK_OPT_ADJ_SPLIT: 0 one pass, 1 two passes, 2 (default) by configuration
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
@@ -401,6 +403,16 @@ int default_np(int kind, int prec, int P, int b) {
     return P >= 32 && P <= 64 ? 4 : 2;
 }
 
+// FK_OPT_ADJ_SPLIT: the two-pass adjoint kernel (fewer live registers, 3 CTAs per SM) or the
+// one-pass kernel. Default: two passes for b=1 rows wider than the light configurations in FP32
+// and float-float (10^6-site cubic, S=128: FP32 0.77 vs 0.81 ms, DS 0.78 vs 0.82); one pass for
+// b=2 and FP64 (cubic L=64, S=256: FP32 3.17 vs 3.05 ms, DS 11.6 vs 10.7).
+bool use_adjoint_split(const fk_engine* e, int NP) {
+    if (e->opt_adj_split != 2) return e->opt_adj_split != 0;
+    const bool light = e->b * NP <= 2;   // a lane's slice of a block row is at most 32 bytes (kLightStep)
+    return e->b == 1 && e->prec != fk::kF64 && !light;
+}
+
 int configure(fk_engine* e) {
     for (auto& c : e->cfg) c.valid = false;
     if (e->n_b == 0 || e->s == 0 || e->n != e->n_b * e->b) return FK_OK;   // configured once both are set
@@ -443,12 +455,15 @@ int configure(fk_engine* e) {
         c.stage_cap = kind == fk::kOuter ? 0 : stage_cap;
         c.smem = c.stage_cap ? ((size_t)c.stage_cap * per_blk + 15) / 16 * 16 : 0;
         c.staged = false;
+        c.split = kind == fk::kAdjoint && use_adjoint_split(e, NP);
+        if (c.split) c.smem += 2 * (size_t)fk::kThreads * e->b * NP * 16;   // kept alpha_{m+1}, alpha_{m-1}
         if (kind == fk::kStep && e->opt_tma) {
             int rc = configure_staged(e, c, Gp, nk_max, per_blk);
             if (rc != FK_OK) return rc;
         }
         int occ = 0;
-        const int okind = !c.staged ? kind : (e->opt_tma == 1 ? (int)fk::kStepStaged : (int)fk::kStepStagedAsync);
+        const int okind = c.split ? (int)fk::kAdjointSplit
+                        : !c.staged ? kind : (e->opt_tma == 1 ? (int)fk::kStepStaged : (int)fk::kStepStagedAsync);
         FK_TRY(prec_occupancy(e, okind, c.NP, c.smem, &occ), "occupancy query");
         if (occ < 1) return e->fail(FK_ERR_UNSUPPORTED, "kernel kind %d does not fit on an SM", kind);
         if (e->opt_ctas_per_sm > 0) occ = std::min(occ, e->opt_ctas_per_sm);
@@ -541,6 +556,7 @@ int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp,
         a.Dacc = Dacc;
         a.dscale = 2.0;
         a.stage_cap = c.stage_cap;
+        a.split = c.split ? 1 : 0;
         ProfScope ps(e, fk::kAdjoint);
         FK_TRY(prec_launch_adjoint(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "adjoint kernel launch");
     }
@@ -1375,6 +1391,11 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             if (value < 0 || value > 1) return e->fail(FK_ERR_ARG, "UPLOAD must be 0 or 1");
             e->opt_upload = value;
             return FK_OK;
+        case FK_OPT_ADJ_SPLIT:
+            if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "ADJ_SPLIT must be 0, 1 or 2");
+            e->opt_adj_split = value;
+            drop_graphs(e);
+            return configure(e);
         case FK_OPT_PRIORITY: {
             if (!e->own_stream) return e->fail(FK_ERR_STATE, "PRIORITY applies to the engine's own stream, not a caller's");
             int least = 0, greatest = 0;
@@ -1414,6 +1435,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_GRAPHS: *value = e->opt_graphs; return FK_OK;
         case FK_OPT_UPLOAD: *value = e->opt_upload; return FK_OK;
         case FK_OPT_PRIORITY: *value = e->opt_priority; return FK_OK;
+        case FK_OPT_ADJ_SPLIT: *value = e->opt_adj_split; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }

@@ -32,9 +32,21 @@ template <class S, int B, int NP>
 cudaError_t staged_one(const StepArgs& a, const StageTables& t, const Launch& l, int tma) {
     return tma ? staged_launch<S, B, NP, true>(a, t, l) : staged_launch<S, B, NP, false>(a, t, l);
 }
+template <class S, int B, int NP, bool FULL>
+cudaError_t adj_split_launch(const AdjArgs& a, const Launch& l) {
+    if (l.smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)k_adjoint_split<S, B, NP, FULL>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_adjoint_split<S, B, NP, FULL><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    return cudaGetLastError();
+}
 template <class S, int B, int NP>
 cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
-    if (whole_chunks(a.P, a.Gp, NP)) k_adjoint_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    const bool whole = whole_chunks(a.P, a.Gp, NP);
+    if (a.split) return whole ? adj_split_launch<S, B, NP, true>(a, l) : adj_split_launch<S, B, NP, false>(a, l);
+    if (whole) k_adjoint_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     else k_adjoint_step<S, B, NP, false><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     return cudaGetLastError();
 }
@@ -48,6 +60,7 @@ template <class S, int B, int NP>
 cudaError_t occ_one(int kind, size_t smem, int* n) {
     const void* f = kind == kStep ? (const void*)k_cheb_step<S, B, NP>
                   : kind == kAdjoint ? (const void*)k_adjoint_step<S, B, NP>
+                  : kind == kAdjointSplit ? (const void*)k_adjoint_split<S, B, NP, true>
                   : kind == kStepStaged ? (const void*)k_cheb_step_staged<S, B, NP, true>
                   : kind == kStepStagedAsync ? (const void*)k_cheb_step_staged<S, B, NP, false>
                   : (const void*)k_outer<S, B, NP>;

@@ -73,6 +73,7 @@ struct AdjArgs {
     double* Dacc;         // FP64 D accumulator on H's pattern (null: no fused epilogue)
     double dscale;        // D += dscale * A_i B_j^dagger
     int stage_cap;
+    int split;            // run k_adjoint_split (two passes over the blocks) instead of k_adjoint_step
 };
 
 struct OuterArgs {
@@ -246,6 +247,8 @@ template <class S, int B, int NP>
 constexpr int kOuterCtas = (B == 1 && S::PREC != 0) ? 3 : 2;
 template <class S, int B, int NP>
 constexpr int kAdjointCtas = kLightStep<S, B, NP> ? 4 : 2;
+template <class S, int B, int NP>
+constexpr int kAdjointSplitCtas = kLightStep<S, B, NP> ? 4 : 3;
 
 template <class S, int B, int NP, bool FULL = false>
 __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(StepArgs a) {
@@ -601,6 +604,172 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
                         bn[e] = S::to(tb);
                     }
                     st<S, NP, FULL>(Ap + roff, an, base, g, Gp, P);
+                    st<S, NP, FULL>(Bp + roff, bn, base, g, Gp, P);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// The same reverse step in two passes over the row's blocks, to hold fewer values in
+// registers at a time: pass 1 gathers alpha_m and writes alpha_{m-1} (keeping alpha_{m+1}
+// and alpha_{m-1} of the thread's own rows in shared memory, which only that thread
+// touches); pass 2 gathers beta_{m+1}, runs the D epilogue and writes beta_m from the kept
+// values. Each gathered row is still read once per block; the kept vectors cost
+// 2 x kThreads x B x NP packets of shared memory after the H stage.
+// ---------------------------------------------------------------------------------
+__host__ __device__ inline size_t adj_stage_bytes(int stage_cap, size_t h_block_bytes) {
+    return ((h_block_bytes + sizeof(unsigned)) * (size_t)stage_cap + 15) / 16 * 16;
+}
+template <class S, int B, int NP, bool FULL = false>
+__global__ void __launch_bounds__(kThreads, kAdjointSplitCtas<S, B, NP>) k_adjoint_split(AdjArgs a) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    constexpr int EPT = NP * S::EPP;
+    extern __shared__ __align__(16) unsigned char smem[];
+    H* s_h = reinterpret_cast<H*>(smem);
+    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
+    E* s_ap = reinterpret_cast<E*>(smem + adj_stage_bytes(a.stage_cap, sizeof(H) * B * B));   // alpha_{m+1}
+    E* s_an = s_ap + (size_t)kThreads * B * EPT;                                               // alpha_{m-1}
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int nch = (P + W - 1) / W;
+    const long long items = (long long)sd.n_b * Gp;
+    const E* A = reinterpret_cast<const E*>(a.A);
+    E* Ap = reinterpret_cast<E*>(a.Ap);
+    const E* Bv = reinterpret_cast<const E*>(a.Bv);
+    E* Bp = reinterpret_cast<E*>(a.Bp);
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef cA = S::coef(a.coef[sidx * a.cstride + 0]);
+    const typename S::Coef cAp = S::coef(a.coef[sidx * a.cstride + 1]);
+    const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
+    const bool fuse = a.Dacc != nullptr;
+    const float2 dscale_ds = ds_from_double(a.dscale);
+    const Owner own = transposed_owner<B * B>(Gp, (int)(threadIdx.x % Gp));   // Gp divides kThreads
+
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const Tile tl = tile_range(a.row_ptr, sd, t0, items, Gp, a.stage_cap);
+        if (tl.staged) {
+            __syncthreads();
+            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
+            __syncthreads();
+        }
+        const long long t = t0 + threadIdx.x;
+        const bool active = t < items;
+        const int il = active ? (int)(t / Gp) : 0;
+        const int g = active ? (int)(t - (long long)il * Gp) : (int)(threadIdx.x % Gp);
+        const int i = sd.row_base + il;
+        const int kb = active ? a.row_ptr[i] : 0;
+        const int ke = active ? a.row_ptr[i + 1] : 0;
+        int nmax = ke - kb;
+        if (fuse) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
+        } else if (!active) {
+            continue;
+        }
+        for (int c = 0; c < nch; c++) {
+            const int base = c * W;
+            // pass 1: alpha_{m-1} = 2 Hs alpha_m - alpha_{m+1}
+            if (active) {
+                typename S::Acc accA[B][EPT];
+#pragma unroll
+                for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) accA[bi][e] = S::zero();
+#pragma unroll 1
+                for (int k = kb; k < ke; k++) {
+                    const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
+                    const H* hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
+                    const int j = (int)(cc & kColMask);
+#pragma unroll
+                    for (int bj = 0; bj < B; bj++) {
+                        E av[EPT];
+                        ld_nc<S, NP, FULL>(av, A + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        mac_block<S, B, NP>(accA, cc >> 30, hk, av, bj);
+                    }
+                }
+#pragma unroll
+                for (int bi = 0; bi < B; bi++) {
+                    const size_t roff = (size_t)(B * i + bi) * a.ld;
+                    E apv[EPT], an[EPT];
+                    ld_rw<S, NP, FULL>(apv, Ap + roff, base, g, Gp, P);
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        an[e] = S::fin(accA[bi][e], true, true, apv[e]);
+                        s_ap[(size_t)(bi * EPT + e) * kThreads + threadIdx.x] = apv[e];
+                        s_an[(size_t)(bi * EPT + e) * kThreads + threadIdx.x] = an[e];
+                    }
+                    st<S, NP, FULL>(Ap + roff, an, base, g, Gp, P);
+                }
+            }
+            // pass 2: beta_m = 2 Hs beta_{m+1} - beta_{m+2} + cA alpha_m + cAp alpha_{m+1} + cAn alpha_{m-1},
+            // with D_k += dscale alpha_m[i] beta_{m+1}[j]^dagger on the gathered beta rows
+            E Ai[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                if (active) ld_nc<S, NP, FULL>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                else {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) Ai[bi][e] = S::to(S::zero());
+                }
+            }
+            typename S::Acc accB[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) accB[bi][e] = S::zero();
+            for (int kk = 0; kk < nmax; kk++) {
+                const int k = kb + kk;
+                const bool has = kk < ke - kb;
+                unsigned cc = 0;
+                const H* hk = hval;
+                if (has) {
+                    cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
+                    hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
+                }
+                const int j = (int)(cc & kColMask);
+                const double2 dpre = d_prefetch<S, B>(a.Dacc, (size_t)k, own, fuse && has && own.writer);
+                typename S::OAcc of[B * B];
+#pragma unroll
+                for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    E bv[EPT];
+                    if (has) {
+                        ld_nc<S, NP, FULL>(bv, Bv + (size_t)(B * j + bj) * a.ld, base, g, Gp, P);
+                        mac_block<S, B, NP>(accB, cc >> 30, hk, bv, bj);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) bv[e] = S::to(S::zero());
+                    }
+                    if (fuse) {
+#pragma unroll
+                        for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                            for (int e = 0; e < EPT; e++) S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
+                    }
+                }
+                if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, dscale_ds, a.Dacc, own, dpre);
+            }
+            if (active) {
+#pragma unroll
+                for (int bi = 0; bi < B; bi++) {
+                    const size_t roff = (size_t)(B * i + bi) * a.ld;
+                    E bpv[EPT], bn[EPT];
+                    ld_rw<S, NP, FULL>(bpv, Bp + roff, base, g, Gp, P);
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        typename S::Acc tb = S::from(S::fin(accB[bi][e], true, true, bpv[e]));
+                        S::axpy(tb, cA, Ai[bi][e]);
+                        S::axpy(tb, cAp, s_ap[(size_t)(bi * EPT + e) * kThreads + threadIdx.x]);
+                        S::axpy(tb, cAn, s_an[(size_t)(bi * EPT + e) * kThreads + threadIdx.x]);
+                        bn[e] = S::to(tb);
+                    }
                     st<S, NP, FULL>(Bp + roff, bn, base, g, Gp, P);
                 }
             }

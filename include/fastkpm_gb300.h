@@ -85,6 +85,8 @@ int  fk_engine_synchronize(fk_engine* e);
 #define FK_OPT_UPLOAD      9   /* set_R: 0 (default) the layout kernel reads R in place when the GPU can (pinned
                                 * memory, or any host memory on systems with pageable-memory access); 1 always
                                 * copy through device staging buffers                                          */
+#define FK_OPT_ADJ_SPLIT  11   /* reverse step: 0 one pass over the blocks, 1 two passes (alpha, then beta + D),
+                                * 2 (default): by configuration                                           */
 #define FK_OPT_PRIORITY   10   /* CUDA priority of the engine's own stream (0 default; more negative = more urgent,
                                 * clamped to the device's range); FK_ERR_STATE on a caller-set stream   */
 int  fk_engine_set_option(fk_engine* e, int option, int value);

@@ -165,6 +165,20 @@ def test_sparse_probe_upload_equals_dense(gpu, prec):
     assert ei.value.status == L.FK_ERR_ARG
 
 
+@pytest.mark.parametrize("prec", ["fp64", "ds", "fp32"])
+@pytest.mark.parametrize("S", [32, 40])
+def test_two_pass_adjoint_equals_one_pass(gpu, prec, S):
+    # k_adjoint_split does the same arithmetic in the same order as k_adjoint_step
+    H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=12)
+    R = fk.probe_uncorrelated(H.n_rows * H.b_len, S, fk.RNG(12), complex_values=True)
+    M = 16
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    one = run_pair(H, es, R, True, prec, M, c, "autodiff", {L.FK_OPT_ADJ_SPLIT: 0})
+    two = run_pair(H, es, R, True, prec, M, c, "autodiff", {L.FK_OPT_ADJ_SPLIT: 1})
+    assert np.array_equal(one[0], two[0]) and np.array_equal(one[2], two[2])
+    assert rel_err(two[2], two[3]) <= TOL_D[prec]
+
+
 def test_stream_priority_option(gpu):
     # the engine's own stream can be recreated with a CUDA priority (clamped to the device's
     # range); results do not depend on it
