@@ -19,6 +19,7 @@ FK_OPT_NP_STEP, FK_OPT_NP_ADJOINT, FK_OPT_NP_OUTER, FK_OPT_TMA = 5, 6, 7, 8
 FK_OPT_UPLOAD = 9
 FK_OPT_PRIORITY = 10
 FK_OPT_ADJ_SPLIT = 11
+FK_OPT_PIPE = 12
 
 PRECISIONS = {"fp64": FK_PREC_FP64, "fp32": FK_PREC_FP32, "ds": FK_PREC_DS}
 

@@ -284,6 +284,7 @@ int batch_enqueue_moments(fk_batch* bt, int M) {
             a.xi_mode = 0;
             a.partials = part + per_step * m + (size_t)sl * bt->grid * 2;
             a.stage_cap = bt->stage_cap;
+            a.pipe = 0;
             BT_TRY(batch_launch_step(bt, a, fk::Launch{bt->grid, bt->smem, bt->stream}), "batched step launch");
         }
     }
@@ -478,6 +479,7 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
             a.dscale = 2.0;
             a.stage_cap = bt->stage_cap;
             a.split = 0;
+            a.pipe = 0;
             BT_TRY(batch_launch_adjoint(bt, a, fk::Launch{bt->grid, bt->smem, bt->stream}), "batched adjoint launch");
             std::swap(A, Ap);
             std::swap(Bv, Bp);

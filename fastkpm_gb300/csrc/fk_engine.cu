@@ -56,6 +56,7 @@ struct KCfg {
     bool valid = false;
     bool staged = false;   // step kind only: TMA-staged gathers (k_cheb_step_staged)
     bool split = false;    // adjoint kind only: two passes over the blocks (k_adjoint_split)
+    bool pipe = false;     // step kind only: double-buffered gathers (k_cheb_step_pipe, FP32)
     int umax = 0;          // largest per-tile gather list
 };
 
@@ -115,6 +116,7 @@ struct fk_engine {
     int pageable_access = 0;   // the GPU reads any host memory (cudaDevAttrPageableMemoryAccess)
     int opt_upload = 0;        // FK_OPT_UPLOAD: 0 read device-readable host R directly, 1 staging copies
     int opt_adj_split = 2;     // FK_OPT_ADJ_SPLIT: 0 one pass, 1 two passes, 2 (default) by configuration
+    int opt_pipe = 2;          // FK_OPT_PIPE: 0 plain step, 1 double-buffered gathers (FP32), 2 (default) by configuration
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
@@ -413,6 +415,18 @@ bool use_adjoint_split(const fk_engine* e, int NP) {
     return e->b == 1 && e->prec != fk::kF64 && !light;
 }
 
+// FK_OPT_PIPE: step / adjoint kernels with double-buffered gathers (FP32 only). Default: the
+// step kernel for b=2 (cubic L=64, S=256: 0.67 vs 0.85 ms; 10^6-site cubic S=128: 1.34 vs
+// 1.59; b=1 S=128 stays plain: 0.301 vs 0.293); the adjoint kernel except for light rows
+// (cubic L=64 S=256 fused: 2.44 vs 2.83 ms; 10^6-site cubic b=2 S=128: 4.41 vs 5.85, b=1
+// S=128: 0.75 vs 0.79; b=1 S=32, light, stays plain: 0.39 vs 0.43).
+bool use_pipe(const fk_engine* e, int kind, int NP) {
+    if (e->prec != fk::kF32) return false;
+    if (e->opt_pipe != 2) return e->opt_pipe != 0;
+    if (kind == fk::kStep) return e->b == 2;
+    return e->b * NP > 2;   // not the light configurations
+}
+
 int configure(fk_engine* e) {
     for (auto& c : e->cfg) c.valid = false;
     if (e->n_b == 0 || e->s == 0 || e->n != e->n_b * e->b) return FK_OK;   // configured once both are set
@@ -438,6 +452,9 @@ int configure(fk_engine* e) {
             while (NP > 1 && next_pow2((P + NP - 1) / NP) < 32 &&
                    (long long)e->n_b * next_pow2((P + NP - 1) / NP) < (long long)e->num_sms * fk::kThreads)
                 NP >>= 1;
+            // the double-buffered adjoint keeps 4 x b x NP packets per thread in shared memory:
+            // at most 4 per b so that two CTAs fit an SM (b=2 S=128 with NP=4: 1 CTA, 8.1 vs 5.8 ms)
+            if (kind == fk::kAdjoint && use_pipe(e, fk::kAdjoint, NP) && e->b * NP > 4) NP = 4 / e->b;
             Gp = std::min(32, next_pow2((P + NP - 1) / NP));
         }
         // H blocks per tile of kThreads items: the shared-memory stage size
@@ -455,14 +472,19 @@ int configure(fk_engine* e) {
         c.stage_cap = kind == fk::kOuter ? 0 : stage_cap;
         c.smem = c.stage_cap ? ((size_t)c.stage_cap * per_blk + 15) / 16 * 16 : 0;
         c.staged = false;
-        c.split = kind == fk::kAdjoint && use_adjoint_split(e, NP);
+        const size_t stage_smem = c.smem;
+        c.pipe = (kind == fk::kStep && !e->opt_tma && use_pipe(e, fk::kStep, NP)) ||
+                 (kind == fk::kAdjoint && use_pipe(e, fk::kAdjoint, NP));
+        c.split = kind == fk::kAdjoint && !c.pipe && use_adjoint_split(e, NP);
         if (c.split) c.smem += 2 * (size_t)fk::kThreads * e->b * NP * 16;   // kept alpha_{m+1}, alpha_{m-1}
+        if (c.pipe) c.smem = stage_smem + (kind == fk::kStep ? fk::pipe_smem_bytes(e->b, NP) : fk::adj_pipe_smem_bytes(e->b, NP));
         if (kind == fk::kStep && e->opt_tma) {
             int rc = configure_staged(e, c, Gp, nk_max, per_blk);
             if (rc != FK_OK) return rc;
         }
         int occ = 0;
         const int okind = c.split ? (int)fk::kAdjointSplit
+                        : c.pipe ? (kind == fk::kStep ? (int)fk::kStepPipe : (int)fk::kAdjointPipe)
                         : !c.staged ? kind : (e->opt_tma == 1 ? (int)fk::kStepStaged : (int)fk::kStepStagedAsync);
         FK_TRY(prec_occupancy(e, okind, c.NP, c.smem, &occ), "occupancy query");
         if (occ < 1) return e->fail(FK_ERR_UNSUPPORTED, "kernel kind %d does not fit on an SM", kind);
@@ -515,6 +537,7 @@ int run_step(fk_engine* e, const void* x, const void* z, void* y, bool two, bool
         a.two = two; a.has_z = z != nullptr; a.want_dots = want_dots; a.xi_mode = xi_mode;
         a.partials = want_dots ? partials_step + (size_t)sl * c.ctas * 2 : nullptr;
         a.stage_cap = c.stage_cap;
+        a.pipe = c.pipe ? 1 : 0;
         ProfScope ps(e, fk::kStep);
         if (c.staged) {
             const fk::StageTables tb = stage_tables(e, c);
@@ -557,6 +580,7 @@ int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp,
         a.dscale = 2.0;
         a.stage_cap = c.stage_cap;
         a.split = c.split ? 1 : 0;
+        a.pipe = c.pipe ? 1 : 0;
         ProfScope ps(e, fk::kAdjoint);
         FK_TRY(prec_launch_adjoint(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "adjoint kernel launch");
     }
@@ -995,6 +1019,7 @@ int m2_step(fk_engine* e, const M2Mat& A, const void* x, const void* z, void* y,
     a.partials = nullptr;
     // the staged (TMA) configuration sizes its shared memory differently: run unstaged then
     a.stage_cap = c.staged ? 0 : c.stage_cap;
+    a.pipe = 0;
     ProfScope ps(e, fk::kStep);
     FK_TRY(prec_launch_step(e, c.NP, a, fk::Launch{c.ctas, c.staged ? 0 : c.smem, e->stream}), "moments2 step");
     return FK_OK;
@@ -1391,6 +1416,11 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             if (value < 0 || value > 1) return e->fail(FK_ERR_ARG, "UPLOAD must be 0 or 1");
             e->opt_upload = value;
             return FK_OK;
+        case FK_OPT_PIPE:
+            if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "PIPE must be 0, 1 or 2");
+            e->opt_pipe = value;
+            drop_graphs(e);
+            return configure(e);
         case FK_OPT_ADJ_SPLIT:
             if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "ADJ_SPLIT must be 0, 1 or 2");
             e->opt_adj_split = value;
@@ -1436,6 +1466,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_UPLOAD: *value = e->opt_upload; return FK_OK;
         case FK_OPT_PRIORITY: *value = e->opt_priority; return FK_OK;
         case FK_OPT_ADJ_SPLIT: *value = e->opt_adj_split; return FK_OK;
+        case FK_OPT_PIPE: *value = e->cfg[fk::kStep].valid ? (int)e->cfg[fk::kStep].pipe : e->opt_pipe; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }

@@ -12,9 +12,23 @@ namespace {
 // instance without packet masks: 2-5% faster per launch (float-float cubic L=64 S=256: step
 // 2.55 vs 2.65 ms, outer product 5.12 vs 5.39).
 inline bool whole_chunks(int P, int Gp, int NP) { return Gp > 0 && P % (Gp * NP) == 0; }
+template <class S, int B, int NP, bool FULL>
+cudaError_t step_pipe_launch(const StepArgs& a, const Launch& l) {
+    if (l.smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)k_cheb_step_pipe<S, B, NP, FULL>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_cheb_step_pipe<S, B, NP, FULL><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    return cudaGetLastError();
+}
 template <class S, int B, int NP>
 cudaError_t step_one(const StepArgs& a, const Launch& l) {
-    if (whole_chunks(a.P, a.Gp, NP)) k_cheb_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    const bool whole = whole_chunks(a.P, a.Gp, NP);
+    if constexpr (S::PREC == 1) {   // double-buffered gathers: FP32 systems only
+        if (a.pipe) return whole ? step_pipe_launch<S, B, NP, true>(a, l) : step_pipe_launch<S, B, NP, false>(a, l);
+    }
+    if (whole) k_cheb_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     else k_cheb_step<S, B, NP, false><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     return cudaGetLastError();
 }
@@ -42,9 +56,22 @@ cudaError_t adj_split_launch(const AdjArgs& a, const Launch& l) {
     k_adjoint_split<S, B, NP, FULL><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     return cudaGetLastError();
 }
+template <class S, int B, int NP, bool FULL>
+cudaError_t adj_pipe_launch(const AdjArgs& a, const Launch& l) {
+    if (l.smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)k_adjoint_pipe<S, B, NP, FULL>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_adjoint_pipe<S, B, NP, FULL><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    return cudaGetLastError();
+}
 template <class S, int B, int NP>
 cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
     const bool whole = whole_chunks(a.P, a.Gp, NP);
+    if constexpr (S::PREC == 1) {   // double-buffered gathers: FP32 systems only
+        if (a.pipe) return whole ? adj_pipe_launch<S, B, NP, true>(a, l) : adj_pipe_launch<S, B, NP, false>(a, l);
+    }
     if (a.split) return whole ? adj_split_launch<S, B, NP, true>(a, l) : adj_split_launch<S, B, NP, false>(a, l);
     if (whole) k_adjoint_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     else k_adjoint_step<S, B, NP, false><<<l.grid, kThreads, l.smem, l.stream>>>(a);
@@ -57,8 +84,18 @@ cudaError_t outer_one(const OuterArgs& a, const Launch& l) {
     return cudaGetLastError();
 }
 template <class S, int B, int NP>
+const void* pipe_fn(int kind) {
+    if constexpr (S::PREC == 1)
+        return kind == kStepPipe ? (const void*)k_cheb_step_pipe<S, B, NP, true> : (const void*)k_adjoint_pipe<S, B, NP, true>;
+    else return nullptr;
+}
+template <class S, int B, int NP>
 cudaError_t occ_one(int kind, size_t smem, int* n) {
+    if constexpr (S::PREC != 1) {
+        if (kind == kStepPipe || kind == kAdjointPipe) return cudaErrorInvalidValue;
+    }
     const void* f = kind == kStep ? (const void*)k_cheb_step<S, B, NP>
+                  : (kind == kStepPipe || kind == kAdjointPipe) ? pipe_fn<S, B, NP>(kind)
                   : kind == kAdjoint ? (const void*)k_adjoint_step<S, B, NP>
                   : kind == kAdjointSplit ? (const void*)k_adjoint_split<S, B, NP, true>
                   : kind == kStepStaged ? (const void*)k_cheb_step_staged<S, B, NP, true>

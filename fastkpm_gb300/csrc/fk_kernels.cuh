@@ -54,6 +54,7 @@ struct StepArgs {
     int two, has_z, want_dots, xi_mode;   // xi_mode 1: xi = c0 x + c1 y;  2: xi += c1 y
     double* partials;          // 2 doubles per CTA: <x,x>, Re<y,x>
     int stage_cap;             // blocks that fit the shared-memory stage (0: no staging)
+    int pipe;                  // FP32 systems: run k_cheb_step_pipe (double-buffered gathers)
 };
 
 struct AdjArgs {
@@ -74,6 +75,7 @@ struct AdjArgs {
     double dscale;        // D += dscale * A_i B_j^dagger
     int stage_cap;
     int split;            // run k_adjoint_split (two passes over the blocks) instead of k_adjoint_step
+    int pipe;             // FP32 systems: run k_adjoint_pipe (double-buffered gathers)
 };
 
 struct OuterArgs {

@@ -148,6 +148,7 @@ extern "C" int fk_moments_noalloc(int kind, int n_b, int b, const int* d_row_ptr
         a.xi_mode = 0;
         a.partials = partials;
         a.stage_cap = 0;
+        a.pipe = 0;
         if (fk::launch_step_f64(cplx, b, NP, a, fk::Launch{(int)ctas, 0, st}) != cudaSuccess) { cudaGetLastError(); return FK_ERR_CUDA; }
         k_noalloc_reduce<<<1, 32, 0, st>>>(partials, (int)ctas, raw + 2 * m);
         if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;

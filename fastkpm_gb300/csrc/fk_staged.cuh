@@ -297,4 +297,331 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, St
     }
 }
 
+// ---------------------------------------------------------------------------------
+// Chebyshev step with each thread's gathers double-buffered in shared memory: while the
+// multiply-adds of block k read its x packets from one buffer, 16-byte cp.async copies
+// bring block k+1's packets into the other, so the next round trip overlaps this block's
+// arithmetic without holding the packets in registers. Every thread copies and reads only
+// its own slots (thread-minor layout: conflict-free 16-byte shared accesses), so the only
+// synchronisation is cp.async.wait_group on the thread's own copies; no spin loop. Masked
+// packets (a ragged last chunk) are never copied and read as zero.
+// Shared memory: 2 buffers x B x NP packets per thread after the H stage.
+// ---------------------------------------------------------------------------------
+__host__ __device__ inline size_t pipe_smem_bytes(int B, int NP) { return 2 * (size_t)kThreads * B * NP * 16; }
+
+template <class S, int B, int NP, bool FULL = false>
+__global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step_pipe(StepArgs a) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    constexpr int EPP = S::EPP;
+    constexpr int EPT = NP * EPP;
+    extern __shared__ __align__(16) unsigned char smem[];
+    H* s_h = reinterpret_cast<H*>(smem);
+    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
+    uint4* sbuf = reinterpret_cast<uint4*>(smem + ((sizeof(H) * B * B + sizeof(unsigned)) * (size_t)a.stage_cap + 15) / 16 * 16);
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int nch = (P + W - 1) / W;
+    const long long items = (long long)sd.n_b * Gp;
+    const E* x = reinterpret_cast<const E*>(a.x);
+    const E* z = reinterpret_cast<const E*>(a.z);
+    E* y = reinterpret_cast<E*>(a.y);
+    E* xi = reinterpret_cast<E*>(a.xi);
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef c0 = S::coef(a.xi_mode ? a.coef[sidx * a.cstride + 0] : 0.0);
+    const typename S::Coef c1 = S::coef(a.xi_mode ? a.coef[sidx * a.cstride + 1] : 0.0);
+    // slot of (buffer, bj, q) for this thread
+    auto slot = [&](int buf, int bj, int q) -> uint4* { return sbuf + ((size_t)(buf * B + bj) * NP + q) * kThreads + threadIdx.x; };
+
+    typename S::Dot dxx = S::dot_zero(), dyx = S::dot_zero();
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const Tile tl = tile_range(a.row_ptr, sd, t0, items, Gp, a.stage_cap);
+        if (tl.staged) {
+            __syncthreads();
+            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
+            __syncthreads();
+        }
+        const long long t = t0 + threadIdx.x;
+        if (t >= items) continue;
+        const int il = (int)(t / Gp);
+        const int g = (int)(t - (long long)il * Gp);
+        const int i = sd.row_base + il;
+        const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];
+        for (int c = 0; c < nch; c++) {
+            const int base = c * W;
+            typename S::Acc acc[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) acc[bi][e] = S::zero();
+            // copies of block k's packets into buffer b
+            auto issue = [&](int k, int b) -> unsigned {
+                const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
+                const int j = (int)(cc & kColMask);
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    const uint4* row = reinterpret_cast<const uint4*>(x + (size_t)(B * j + bj) * a.ld);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        const int pk = base + g + Gp * q;
+                        if (FULL || pk < P) cp_async16(slot(b, bj, q), row + pk);
+                    }
+                }
+                return cc;
+            };
+            unsigned cc_next = 0;
+            if (kb < ke) cc_next = issue(kb, 0);
+            cp_async_commit();
+#pragma unroll 1
+            for (int k = kb; k < ke; k++) {
+                const int b = (k - kb) & 1;
+                const unsigned cc = cc_next;
+                if (k + 1 < ke) cc_next = issue(k + 1, b ^ 1);
+                cp_async_commit();
+                cp_async_wait<1>();   // this thread's copies of block k have landed
+                const H* hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    E xv[EPT];
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        const int pk = base + g + Gp * q;
+                        Packet<E, EPP> pkt;
+                        pkt.u = make_uint4(0u, 0u, 0u, 0u);
+                        if (FULL || pk < P) pkt.u = *slot(b, bj, q);
+#pragma unroll
+                        for (int e = 0; e < EPP; e++) xv[q * EPP + e] = pkt.e[e];
+                    }
+                    mac_block<S, B, NP>(acc, cc >> 30, hk, xv, bj);
+                }
+            }
+            cp_async_wait<0>();
+            typename S::RowDot rxx = S::rd_zero(), ryx = S::rd_zero();
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                const size_t roff = (size_t)(B * i + bi) * a.ld;
+                E zv[EPT], yv[EPT];
+                if (a.has_z) ld_rw<S, NP, FULL>(zv, z + roff, base, g, Gp, P);
+                else {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) zv[e] = S::to(S::zero());
+                }
+#pragma unroll
+                for (int e = 0; e < EPT; e++) yv[e] = S::fin(acc[bi][e], a.two != 0, a.has_z != 0, zv[e]);
+                st<S, NP, FULL>(y + roff, yv, base, g, Gp, P);
+                if (a.want_dots || a.xi_mode == 1) {
+                    E xo[EPT];
+                    ld_nc<S, NP, FULL>(xo, x + roff, base, g, Gp, P);
+                    if (a.want_dots) {
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) { S::rd_nrm(rxx, xo[e]); S::rd_re(ryx, yv[e], xo[e]); }
+                    }
+                    if (a.xi_mode == 1) {
+                        E xv2[EPT];
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) {
+                            typename S::Acc t2 = S::zero();
+                            S::axpy(t2, c0, xo[e]);
+                            S::axpy(t2, c1, yv[e]);
+                            xv2[e] = S::to(t2);
+                        }
+                        st<S, NP, FULL>(xi + roff, xv2, base, g, Gp, P);
+                    }
+                }
+                if (a.xi_mode == 2) {
+                    E xv2[EPT];
+                    ld_rw<S, NP, FULL>(xv2, xi + roff, base, g, Gp, P);
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        typename S::Acc t2 = S::from(xv2[e]);
+                        S::axpy(t2, c1, yv[e]);
+                        xv2[e] = S::to(t2);
+                    }
+                    st<S, NP, FULL>(xi + roff, xv2, base, g, Gp, P);
+                }
+            }
+            if (a.want_dots) { S::dot_add(dxx, rxx); S::dot_add(dyx, ryx); }
+        }
+    }
+    if (a.want_dots) {
+        block_reduce2<S>(dxx, dyx);
+        if (threadIdx.x == 0) {
+            a.partials[2 * blockIdx.x + 0] = S::dot_get(dxx);
+            a.partials[2 * blockIdx.x + 1] = S::dot_get(dyx);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// The reverse (adjoint) step with the same double buffering: block k+1's alpha_m and
+// beta_{m+1} packets are copied into shared memory while block k's multiply-adds and D
+// epilogue run. Same arithmetic, in the same order, as k_adjoint_step.
+// Shared memory: 2 buffers x 2 vectors x B x NP packets per thread after the H stage.
+// ---------------------------------------------------------------------------------
+__host__ __device__ inline size_t adj_pipe_smem_bytes(int B, int NP) { return 4 * (size_t)kThreads * B * NP * 16; }
+
+template <class S, int B, int NP, bool FULL = false>
+__global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pipe(AdjArgs a) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    constexpr int EPP = S::EPP;
+    constexpr int EPT = NP * EPP;
+    extern __shared__ __align__(16) unsigned char smem[];
+    H* s_h = reinterpret_cast<H*>(smem);
+    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
+    uint4* sbuf = reinterpret_cast<uint4*>(smem + ((sizeof(H) * B * B + sizeof(unsigned)) * (size_t)a.stage_cap + 15) / 16 * 16);
+    // slot of (buffer, vector v: 0 alpha_m / 1 beta_{m+1}, bj, q) for this thread
+    auto slot = [&](int buf, int v, int bj, int q) -> uint4* {
+        return sbuf + ((size_t)((buf * 2 + v) * B + bj) * NP + q) * kThreads + threadIdx.x;
+    };
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int nch = (P + W - 1) / W;
+    const long long items = (long long)sd.n_b * Gp;
+    const E* A = reinterpret_cast<const E*>(a.A);
+    E* Ap = reinterpret_cast<E*>(a.Ap);
+    const E* Bv = reinterpret_cast<const E*>(a.Bv);
+    E* Bp = reinterpret_cast<E*>(a.Bp);
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef cA = S::coef(a.coef[sidx * a.cstride + 0]);
+    const typename S::Coef cAp = S::coef(a.coef[sidx * a.cstride + 1]);
+    const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
+    const bool fuse = a.Dacc != nullptr;
+    const float2 dscale_ds = ds_from_double(a.dscale);
+    const Owner own = transposed_owner<B * B>(Gp, (int)(threadIdx.x % Gp));   // Gp divides kThreads
+
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const Tile tl = tile_range(a.row_ptr, sd, t0, items, Gp, a.stage_cap);
+        if (tl.staged) {
+            __syncthreads();
+            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
+            __syncthreads();
+        }
+        const long long t = t0 + threadIdx.x;
+        const bool active = t < items;
+        const int il = active ? (int)(t / Gp) : 0;
+        const int g = active ? (int)(t - (long long)il * Gp) : (int)(threadIdx.x % Gp);
+        const int i = sd.row_base + il;
+        const int kb = active ? a.row_ptr[i] : 0;
+        const int ke = active ? a.row_ptr[i + 1] : 0;
+        int nmax = ke - kb;
+        if (fuse) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, off));
+        } else if (!active) {
+            continue;
+        }
+        for (int c = 0; c < nch; c++) {
+            const int base = c * W;
+            E Ai[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++) {
+                if (active) ld_nc<S, NP, FULL>(Ai[bi], A + (size_t)(B * i + bi) * a.ld, base, g, Gp, P);
+                else {
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) Ai[bi][e] = S::to(S::zero());
+                }
+            }
+            typename S::Acc accA[B][EPT], accB[B][EPT];
+#pragma unroll
+            for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) { accA[bi][e] = S::zero(); accB[bi][e] = S::zero(); }
+            // copies of block k's alpha_m and beta_{m+1} packets into buffer b (rows of this thread only)
+            auto issue = [&](int k, int b) -> unsigned {
+                const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
+                const int j = (int)(cc & kColMask);
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    const uint4* ra = reinterpret_cast<const uint4*>(A + (size_t)(B * j + bj) * a.ld);
+                    const uint4* rb = reinterpret_cast<const uint4*>(Bv + (size_t)(B * j + bj) * a.ld);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        const int pk = base + g + Gp * q;
+                        if (FULL || pk < P) {
+                            cp_async16(slot(b, 0, bj, q), ra + pk);
+                            cp_async16(slot(b, 1, bj, q), rb + pk);
+                        }
+                    }
+                }
+                return cc;
+            };
+            const int nrow = ke - kb;
+            unsigned cc_next = 0;
+            if (nrow > 0) cc_next = issue(kb, 0);
+            cp_async_commit();
+            for (int kk = 0; kk < nmax; kk++) {
+                const int k = kb + kk;
+                const bool has = kk < nrow;
+                const int b = kk & 1;
+                const unsigned cc = cc_next;
+                if (kk + 1 < nrow) cc_next = issue(k + 1, b ^ 1);
+                cp_async_commit();
+                cp_async_wait<1>();   // this thread's copies of block k have landed
+                const H* hk = hval;
+                if (has) hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
+                const double2 dpre = d_prefetch<S, B>(a.Dacc, (size_t)k, own, fuse && has && own.writer);
+                typename S::OAcc of[B * B];
+#pragma unroll
+                for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    E av[EPT], bv[EPT];
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        const int pk = base + g + Gp * q;
+                        Packet<E, EPP> pa, pb;
+                        pa.u = make_uint4(0u, 0u, 0u, 0u);
+                        pb.u = make_uint4(0u, 0u, 0u, 0u);
+                        if (has && (FULL || pk < P)) {
+                            pa.u = *slot(b, 0, bj, q);
+                            pb.u = *slot(b, 1, bj, q);
+                        }
+#pragma unroll
+                        for (int e = 0; e < EPP; e++) { av[q * EPP + e] = pa.e[e]; bv[q * EPP + e] = pb.e[e]; }
+                    }
+                    if (has) {
+                        mac_block<S, B, NP>(accA, cc >> 30, hk, av, bj);
+                        mac_block<S, B, NP>(accB, cc >> 30, hk, bv, bj);
+                    }
+                    if (fuse) {
+#pragma unroll
+                        for (int bi = 0; bi < B; bi++)
+#pragma unroll
+                            for (int e = 0; e < EPT; e++) S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
+                    }
+                }
+                if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, dscale_ds, a.Dacc, own, dpre);
+            }
+            cp_async_wait<0>();
+            if (active) {
+#pragma unroll
+                for (int bi = 0; bi < B; bi++) {
+                    const size_t roff = (size_t)(B * i + bi) * a.ld;
+                    E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
+                    ld_rw<S, NP, FULL>(apv, Ap + roff, base, g, Gp, P);
+                    ld_rw<S, NP, FULL>(bpv, Bp + roff, base, g, Gp, P);
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) {
+                        an[e] = S::fin(accA[bi][e], true, true, apv[e]);
+                        typename S::Acc tb = S::from(S::fin(accB[bi][e], true, true, bpv[e]));
+                        S::axpy(tb, cA, Ai[bi][e]);
+                        S::axpy(tb, cAp, apv[e]);
+                        S::axpy(tb, cAn, an[e]);
+                        bn[e] = S::to(tb);
+                    }
+                    st<S, NP, FULL>(Ap + roff, an, base, g, Gp, P);
+                    st<S, NP, FULL>(Bp + roff, bn, base, g, Gp, P);
+                }
+            }
+        }
+    }
+}
+
 }  // namespace fk

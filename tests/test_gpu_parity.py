@@ -179,6 +179,25 @@ def test_two_pass_adjoint_equals_one_pass(gpu, prec, S):
     assert rel_err(two[2], two[3]) <= TOL_D[prec]
 
 
+@pytest.mark.parametrize("cplx", [True, False])
+@pytest.mark.parametrize("S", [32, 40])
+def test_pipelined_step_equals_plain(gpu, cplx, S):
+    # k_cheb_step_pipe and k_adjoint_pipe (gathers double-buffered through shared memory) do the
+    # plain kernels' arithmetic in the same order: identical moments and D, whole and ragged chunks
+    if cplx:
+        H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=13)
+        R = fk.probe_uncorrelated(H.n_rows * H.b_len, S, fk.RNG(13), complex_values=True)
+    else:
+        H, es, R = small_real_case(10, S, 13)
+    M = 16
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    for kind in ("autodiff", "stoch"):
+        plain = run_pair(H, es, R, cplx, "fp32", M, c, kind, {L.FK_OPT_PIPE: 0})
+        piped = run_pair(H, es, R, cplx, "fp32", M, c, kind, {L.FK_OPT_PIPE: 1})
+        assert np.array_equal(plain[0], piped[0]) and np.array_equal(plain[2], piped[2])
+        assert mu_err(piped[0], piped[1]) <= TOL_MU["fp32"]
+
+
 def test_stream_priority_option(gpu):
     # the engine's own stream can be recreated with a CUDA priority (clamped to the device's
     # range); results do not depend on it
