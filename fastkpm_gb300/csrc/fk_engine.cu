@@ -415,14 +415,17 @@ bool use_adjoint_split(const fk_engine* e, int NP) {
     return e->b == 1 && e->prec != fk::kF64 && !light;
 }
 
-// FK_OPT_PIPE: step / adjoint kernels with double-buffered gathers (FP32 only). Default: the
+// FK_OPT_PIPE: step / adjoint kernels with double-buffered gathers (FP32, float-float). FP32: the
 // step kernel for b=2 (cubic L=64, S=256: 0.67 vs 0.85 ms; 10^6-site cubic S=128: 1.34 vs
 // 1.59; b=1 S=128 stays plain: 0.301 vs 0.293); the adjoint kernel except for light rows
 // (cubic L=64 S=256 fused: 2.44 vs 2.83 ms; 10^6-site cubic b=2 S=128: 4.41 vs 5.85, b=1
 // S=128: 0.75 vs 0.79; b=1 S=32, light, stays plain: 0.39 vs 0.43).
 bool use_pipe(const fk_engine* e, int kind, int NP) {
-    if (e->prec != fk::kF32) return false;
+    if (e->prec == fk::kF64) return false;
     if (e->opt_pipe != 2) return e->opt_pipe != 0;
+    // float-float: b=2 only (cubic L=64, S=256: fused adjoint 9.62 vs 10.62 ms, step 2.43 vs 2.54;
+    // b=1 S=128 keeps the two-pass adjoint: 0.77 vs 0.79 piped)
+    if (e->prec == fk::kDS) return e->b == 2;
     if (kind == fk::kStep) return e->b == 2;
     return e->b * NP > 2;   // not the light configurations
 }

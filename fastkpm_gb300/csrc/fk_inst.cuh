@@ -25,7 +25,7 @@ cudaError_t step_pipe_launch(const StepArgs& a, const Launch& l) {
 template <class S, int B, int NP>
 cudaError_t step_one(const StepArgs& a, const Launch& l) {
     const bool whole = whole_chunks(a.P, a.Gp, NP);
-    if constexpr (S::PREC == 1) {   // double-buffered gathers: FP32 systems only
+    if constexpr (S::PREC != 0) {   // double-buffered gathers: FP32 and float-float systems
         if (a.pipe) return whole ? step_pipe_launch<S, B, NP, true>(a, l) : step_pipe_launch<S, B, NP, false>(a, l);
     }
     if (whole) k_cheb_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
@@ -69,7 +69,7 @@ cudaError_t adj_pipe_launch(const AdjArgs& a, const Launch& l) {
 template <class S, int B, int NP>
 cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
     const bool whole = whole_chunks(a.P, a.Gp, NP);
-    if constexpr (S::PREC == 1) {   // double-buffered gathers: FP32 systems only
+    if constexpr (S::PREC != 0) {   // double-buffered gathers: FP32 and float-float systems
         if (a.pipe) return whole ? adj_pipe_launch<S, B, NP, true>(a, l) : adj_pipe_launch<S, B, NP, false>(a, l);
     }
     if (a.split) return whole ? adj_split_launch<S, B, NP, true>(a, l) : adj_split_launch<S, B, NP, false>(a, l);
@@ -85,13 +85,13 @@ cudaError_t outer_one(const OuterArgs& a, const Launch& l) {
 }
 template <class S, int B, int NP>
 const void* pipe_fn(int kind) {
-    if constexpr (S::PREC == 1)
+    if constexpr (S::PREC != 0)
         return kind == kStepPipe ? (const void*)k_cheb_step_pipe<S, B, NP, true> : (const void*)k_adjoint_pipe<S, B, NP, true>;
     else return nullptr;
 }
 template <class S, int B, int NP>
 cudaError_t occ_one(int kind, size_t smem, int* n) {
-    if constexpr (S::PREC != 1) {
+    if constexpr (S::PREC == 0) {
         if (kind == kStepPipe || kind == kAdjointPipe) return cudaErrorInvalidValue;
     }
     const void* f = kind == kStep ? (const void*)k_cheb_step<S, B, NP>

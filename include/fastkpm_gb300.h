@@ -87,9 +87,9 @@ int  fk_engine_synchronize(fk_engine* e);
                                 * copy through device staging buffers                                          */
 #define FK_OPT_ADJ_SPLIT  11   /* reverse step: 0 one pass over the blocks, 1 two passes (alpha, then beta + D),
                                 * 2 (default): by configuration                                           */
-#define FK_OPT_PIPE       12   /* FP32 step kernel: 1 double-buffer each thread's gathers in shared memory with
-                                * cp.async, 0 plain loads, 2 (default): by configuration; reading it back
-                                * returns whether the configured step uses it                              */
+#define FK_OPT_PIPE       12   /* FP32 / float-float step and adjoint kernels: 1 double-buffer each thread's
+                                * gathers in shared memory with cp.async, 0 plain loads, 2 (default): by
+                                * configuration; reading it back returns whether the configured step uses it */
 #define FK_OPT_PRIORITY   10   /* CUDA priority of the engine's own stream (0 default; more negative = more urgent,
                                 * clamped to the device's range); FK_ERR_STATE on a caller-set stream   */
 int  fk_engine_set_option(fk_engine* e, int option, int value);

@@ -179,9 +179,10 @@ def test_two_pass_adjoint_equals_one_pass(gpu, prec, S):
     assert rel_err(two[2], two[3]) <= TOL_D[prec]
 
 
+@pytest.mark.parametrize("prec", ["fp32", "ds"])
 @pytest.mark.parametrize("cplx", [True, False])
 @pytest.mark.parametrize("S", [32, 40])
-def test_pipelined_step_equals_plain(gpu, cplx, S):
+def test_pipelined_step_equals_plain(gpu, prec, cplx, S):
     # k_cheb_step_pipe and k_adjoint_pipe (gathers double-buffered through shared memory) do the
     # plain kernels' arithmetic in the same order: identical moments and D, whole and ragged chunks
     if cplx:
@@ -192,10 +193,10 @@ def test_pipelined_step_equals_plain(gpu, cplx, S):
     M = 16
     c = W.fermi_coefficients(M, es, "fermi_energy")
     for kind in ("autodiff", "stoch"):
-        plain = run_pair(H, es, R, cplx, "fp32", M, c, kind, {L.FK_OPT_PIPE: 0})
-        piped = run_pair(H, es, R, cplx, "fp32", M, c, kind, {L.FK_OPT_PIPE: 1})
+        plain = run_pair(H, es, R, cplx, prec, M, c, kind, {L.FK_OPT_PIPE: 0})
+        piped = run_pair(H, es, R, cplx, prec, M, c, kind, {L.FK_OPT_PIPE: 1})
         assert np.array_equal(plain[0], piped[0]) and np.array_equal(plain[2], piped[2])
-        assert mu_err(piped[0], piped[1]) <= TOL_MU["fp32"]
+        assert mu_err(piped[0], piped[1]) <= TOL_MU[prec]
 
 
 def test_stream_priority_option(gpu):
