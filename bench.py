@@ -156,14 +156,14 @@ def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
     return vec + h + d
 
 
-# DRAM bytes per row of one fused DS adjoint launch from the ncu capture on the cubic L=32 case
-# (profiles/k_adjoint_step_ds_cubic32.md: 1.277 GB read + 0.522 GB written for 65,536 rows);
-# traffic grows in proportion to the rows, so the L=64 launch's traffic is this times N.
-ADJ_DS_TRAFFIC_PER_ROW = (1.277403e9 + 0.521811e9) / 65536
-# Warp instructions per row of the same launch (smsp__inst_executed.sum = 1,084,435,072 for 65,536
+# DRAM bytes per row of one fused DS adjoint launch (k_adjoint_pipe) from the ncu capture on the
+# cubic L=32 case (profiles/k_adjoint_step_ds_cubic32.md: 1.600 GB read + 0.530 GB written for
+# 65,536 rows); traffic grows in proportion to the rows, so the L=64 launch's traffic is this times N.
+ADJ_DS_TRAFFIC_PER_ROW = (1.600211e9 + 0.529769e9) / 65536
+# Warp instructions per row of the same launch (smsp__inst_executed.sum = 1,108,457,856 for 65,536
 # rows): the fused float-float adjoint is bound by instruction issue, not by DRAM. Issue peak of
 # the GPU: 152 SMs x 4 schedulers x 1 warp instruction per cycle at the maximum SM clock.
-ADJ_DS_WARP_INST_PER_ROW = 1084435072 / 65536
+ADJ_DS_WARP_INST_PER_ROW = 1108457856 / 65536
 ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
 
 
