@@ -8,7 +8,11 @@
 #pragma once
 #include <algorithm>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/fastkpm_gb300.h"
@@ -16,7 +20,26 @@
 
 namespace fk {
 
-// row_ptr monotone from 0 to nnzb, columns in [0, n_b) and strictly increasing per row.
+// Runs f(lo, hi) over [0, n) split into contiguous ranges on the host's cores (one range when
+// n is small).
+template <class F>
+inline void parallel_ranges(int n, int min_range, F f) {
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = std::max(1u, std::min(nt, 64u));
+    const int parts = (int)std::min<long long>(nt, std::max<long long>(1, (long long)n / std::max(1, min_range)));
+    if (parts <= 1) { f(0, n); return; }
+    std::vector<std::thread> ts;
+    ts.reserve(parts);
+    for (int p = 0; p < parts; p++) {
+        const int lo = (int)((long long)n * p / parts), hi = (int)((long long)n * (p + 1) / parts);
+        ts.emplace_back(f, lo, hi);
+    }
+    for (auto& t : ts) t.join();
+}
+
+// row_ptr monotone from 0 to nnzb, columns in [0, n_b) and strictly increasing per row. The
+// row_ptr pass runs first, so that no column is read through an out-of-range row bound; the
+// column pass runs over row ranges in parallel and reports the first bad row.
 inline int check_bsr_pattern(int n_b, int nnzb, const int* row_ptr, const int* col_idx, std::string& why) {
     char buf[160];
     if (!row_ptr || (nnzb > 0 && !col_idx)) { why = "null pattern array"; return FK_ERR_ARG; }
@@ -27,27 +50,54 @@ inline int check_bsr_pattern(int n_b, int nnzb, const int* row_ptr, const int* c
             why = buf;
             return FK_ERR_PATTERN;
         }
+    }
+    std::mutex mu;
+    int bad_row = n_b;
+    parallel_ranges(n_b, 1 << 15, [&](int lo, int hi) {
+        for (int i = lo; i < hi; i++) {
+            for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
+                if (col_idx[k] < 0 || col_idx[k] >= n_b || (k > row_ptr[i] && col_idx[k] <= col_idx[k - 1])) {
+                    std::lock_guard<std::mutex> lk(mu);
+                    if (i < bad_row) bad_row = i;
+                    return;
+                }
+            }
+        }
+    });
+    if (bad_row < n_b) {
+        const int i = bad_row;
         for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) {
             if (col_idx[k] < 0 || col_idx[k] >= n_b) {
                 snprintf(buf, sizeof buf, "column %d out of range in row %d", col_idx[k], i);
-                why = buf;
-                return FK_ERR_PATTERN;
+                break;
             }
             if (k > row_ptr[i] && col_idx[k] <= col_idx[k - 1]) {
                 snprintf(buf, sizeof buf, "columns not strictly increasing in row %d", i);
-                why = buf;
-                return FK_ERR_PATTERN;
+                break;
             }
         }
+        why = buf;
+        return FK_ERR_PATTERN;
     }
     return FK_OK;
 }
 
+// Allocator whose resize leaves new elements uninitialised (the buffers below are written in
+// full by prepare_H's parallel pass; zero-filling hundreds of MB first costs a serial pass).
+template <class T>
+struct UninitAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = UninitAlloc<U>; };
+    UninitAlloc() = default;
+    template <class U> UninitAlloc(const UninitAlloc<U>&) {}
+    template <class U> void construct(U* p) noexcept { ::new (static_cast<void*>(p)) U; }
+    template <class U, class... A> void construct(U* p, A&&... a) { ::new (static_cast<void*>(p)) U(std::forward<A>(a)...); }
+};
+
 struct PreparedH {
-    std::vector<int> row_ptr;        // augmented, local (starts at 0)
-    std::vector<int> col;            // augmented local block columns
-    std::vector<unsigned> colc;      // (col + col_offset) | class << 30
-    std::vector<unsigned char> hval; // entries in the engine precision
+    std::vector<int> row_ptr;                                    // augmented, local (starts at 0)
+    std::vector<int> col;                                        // augmented local block columns
+    std::vector<unsigned, UninitAlloc<unsigned>> colc;           // (col + col_offset) | class << 30
+    std::vector<unsigned char, UninitAlloc<unsigned char>> hval; // entries in the engine precision
 };
 
 inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
@@ -59,64 +109,84 @@ inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* ro
     if (rc != FK_OK) return rc;
     const int bb = b * b, cw = cplx ? 2 : 1;
     const double avg = (es_hi + es_lo) / 2.0, mag = (es_hi - es_lo) / 2.0;
-    std::vector<double> hs;
+    // rows without a stored diagonal block get a zero one, at its sorted position
     out.row_ptr.assign(n_b + 1, 0);
-    out.col.clear();
-    out.col.reserve((size_t)nnzb + n_b);
-    hs.reserve(((size_t)nnzb + n_b) * bb * cw);
-    for (int i = 0; i < n_b; i++) {
-        bool diag_done = false;
-        for (int k = row_ptr[i]; k <= row_ptr[i + 1]; k++) {
-            const bool end = k == row_ptr[i + 1];
-            const int j = end ? n_b : col_idx[k];
-            if (!diag_done && j >= i) {
-                out.col.push_back(i);
-                const size_t base = hs.size();
-                if (j == i) hs.insert(hs.end(), val + (size_t)k * bb * cw, val + (size_t)(k + 1) * bb * cw);
-                else hs.insert(hs.end(), (size_t)bb * cw, 0.0);
-                for (int q = 0; q < b; q++) hs[base + (size_t)(q * b + q) * cw] -= avg;
-                diag_done = true;
-                if (j == i) continue;
-            }
-            if (end) break;
-            out.col.push_back(j);
-            hs.insert(hs.end(), val + (size_t)k * bb * cw, val + (size_t)(k + 1) * bb * cw);
+    parallel_ranges(n_b, 1 << 15, [&](int lo, int hi) {
+        for (int i = lo; i < hi; i++) {
+            const int* c0 = col_idx + row_ptr[i];
+            const int* c1 = col_idx + row_ptr[i + 1];
+            const bool has_diag = std::binary_search(c0, c1, i);
+            out.row_ptr[i + 1] = (int)(c1 - c0) + (has_diag ? 0 : 1);
         }
-        out.row_ptr[i + 1] = (int)out.col.size();
-    }
-    for (auto& v : hs) v /= mag;
-    const int nk = (int)out.col.size();
+    });
+    for (int i = 0; i < n_b; i++) out.row_ptr[i + 1] += out.row_ptr[i];
+    const int nk = out.row_ptr[n_b];
+    out.col.resize(nk);
     out.colc.resize(nk);
-    for (int k = 0; k < nk; k++) {
-        const double* v = &hs[(size_t)k * bb * cw];
-        bool real = true, scal = true;
-        for (int q = 0; q < bb; q++)
-            if (cplx && v[q * cw + 1] != 0.0) real = false;
-        for (int bj = 0; bj < b; bj++)
-            for (int bi = 0; bi < b; bi++) {
-                const double re = v[(bj * b + bi) * cw];
-                if (bi != bj && re != 0.0) scal = false;
-                if (bi == bj && re != v[0]) scal = false;
+    const size_t ebytes = (size_t)elem_bytes(prec, cplx) / cw;   // bytes per real entry
+    out.hval.resize((size_t)nk * bb * cw * ebytes);
+    unsigned char* hv = out.hval.data();
+    // every output block: Hs = (H - avg I) / mag in double, classified, converted to the
+    // engine precision; each range of rows writes its own slice of the outputs
+    parallel_ranges(n_b, 1 << 14, [&](int lo, int hi) {
+        double v[8];
+        for (int i = lo; i < hi; i++) {
+            int kout = out.row_ptr[i];
+            bool diag_done = false;
+            for (int k = row_ptr[i]; k <= row_ptr[i + 1]; k++) {
+                const bool end = k == row_ptr[i + 1];
+                const int j = end ? n_b : col_idx[k];
+                for (int pass = 0; pass < 2; pass++) {
+                    // pass 0: the diagonal block (stored or inserted) when this column reaches it;
+                    // pass 1: the stored block k
+                    int jc;
+                    const double* src;
+                    if (pass == 0) {
+                        if (diag_done || j < i) continue;
+                        jc = i;
+                        src = j == i ? val + (size_t)k * bb * cw : nullptr;
+                        diag_done = true;
+                    } else {
+                        if (end || j == i) continue;
+                        jc = j;
+                        src = val + (size_t)k * bb * cw;
+                    }
+                    for (int q = 0; q < bb * cw; q++) v[q] = src ? src[q] : 0.0;
+                    if (jc == i)
+                        for (int q = 0; q < b; q++) v[(size_t)(q * b + q) * cw] -= avg;
+                    for (int q = 0; q < bb * cw; q++) v[q] /= mag;
+                    bool real = true, scal = true;
+                    for (int q = 0; q < bb; q++)
+                        if (cplx && v[q * cw + 1] != 0.0) real = false;
+                    for (int bj = 0; bj < b; bj++)
+                        for (int bi = 0; bi < b; bi++) {
+                            const double re = v[(bj * b + bi) * cw];
+                            if (bi != bj && re != 0.0) scal = false;
+                            if (bi == bj && re != v[0]) scal = false;
+                        }
+                    const unsigned cls = real ? (scal ? 2u : 1u) : 0u;
+                    out.col[kout] = jc;
+                    out.colc[kout] = (unsigned)(jc + col_offset) | (cls << 30);
+                    const size_t base = (size_t)kout * bb * cw;
+                    if (prec == kF64) {
+                        std::memcpy(hv + base * sizeof(double), v, sizeof(double) * bb * cw);
+                    } else if (prec == kF32) {
+                        float* f = reinterpret_cast<float*>(hv) + base;
+                        for (int q = 0; q < bb * cw; q++) f[q] = (float)v[q];
+                    } else {
+                        float* f = reinterpret_cast<float*>(hv) + 2 * base;
+                        for (int q = 0; q < bb * cw; q++) {
+                            const float hi32 = (float)v[q];
+                            f[2 * q] = hi32;
+                            f[2 * q + 1] = (float)(v[q] - (double)hi32);
+                        }
+                    }
+                    kout++;
+                }
+                if (end) break;
             }
-        const unsigned cls = real ? (scal ? 2u : 1u) : 0u;
-        out.colc[k] = (unsigned)(out.col[k] + col_offset) | (cls << 30);
-    }
-    const size_t nval = (size_t)nk * bb * cw;
-    const size_t bytes = (size_t)nk * bb * elem_bytes(prec, cplx);
-    out.hval.assign(bytes, 0);
-    if (prec == kF64) {
-        std::memcpy(out.hval.data(), hs.data(), sizeof(double) * nval);
-    } else if (prec == kF32) {
-        float* f = reinterpret_cast<float*>(out.hval.data());
-        for (size_t q = 0; q < nval; q++) f[q] = (float)hs[q];
-    } else {
-        float* f = reinterpret_cast<float*>(out.hval.data());
-        for (size_t q = 0; q < nval; q++) {
-            const float hi = (float)hs[q];
-            f[2 * q] = hi;
-            f[2 * q + 1] = (float)(hs[q] - (double)hi);
         }
-    }
+    });
     return FK_OK;
 }
 
