@@ -1371,6 +1371,7 @@ int fk_engine_set_stream(fk_engine* e, void* st) {
     if (!e) return FK_ERR_ARG;
     cudaSetDevice(e->device);
     if (e->own_stream && e->stream) { cudaStreamSynchronize(e->stream); cudaStreamDestroy(e->stream); }
+    e->opt_priority = 0;
     if (st) { e->stream = (cudaStream_t)st; e->own_stream = false; }
     else {
         if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) return e->fail(FK_ERR_CUDA, "stream create");
