@@ -455,8 +455,8 @@ int configure(fk_engine* e) {
             while (NP > 1 && next_pow2((P + NP - 1) / NP) < 32 &&
                    (long long)e->n_b * next_pow2((P + NP - 1) / NP) < (long long)e->num_sms * fk::kThreads)
                 NP >>= 1;
-            // the double-buffered adjoint keeps 4 x b x NP packets per thread in shared memory:
-            // at most 4 per b so that two CTAs fit an SM (b=2 S=128 with NP=4: 1 CTA, 8.1 vs 5.8 ms)
+            // the double-buffered adjoint keeps 6 x b x NP packets per thread in shared memory:
+            // b x NP at most 4 so that two CTAs fit an SM (b=2 S=128 with NP=4: 1 CTA, 8.1 vs 5.8 ms)
             if (kind == fk::kAdjoint && use_pipe(e, fk::kAdjoint, NP) && e->b * NP > 4) NP = 4 / e->b;
             Gp = std::min(32, next_pow2((P + NP - 1) / NP));
         }

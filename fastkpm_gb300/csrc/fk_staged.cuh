@@ -459,9 +459,11 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step_pip
 // The reverse (adjoint) step with the same double buffering: block k+1's alpha_m and
 // beta_{m+1} packets are copied into shared memory while block k's multiply-adds and D
 // epilogue run. Same arithmetic, in the same order, as k_adjoint_step.
-// Shared memory: 2 buffers x 2 vectors x B x NP packets per thread after the H stage.
+// The own rows of alpha_{m+1} and beta_{m+2}, needed only when the row's blocks are done, are
+// copied the same way at the start of each column chunk, with the first block's packets.
+// Shared memory: (2 buffers x 2 vectors + 2 own rows) x B x NP packets per thread after the H stage.
 // ---------------------------------------------------------------------------------
-__host__ __device__ inline size_t adj_pipe_smem_bytes(int B, int NP) { return 4 * (size_t)kThreads * B * NP * 16; }
+__host__ __device__ inline size_t adj_pipe_smem_bytes(int B, int NP) { return 6 * (size_t)kThreads * B * NP * 16; }
 
 template <class S, int B, int NP, bool FULL = false>
 __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pipe(AdjArgs a) {
@@ -476,6 +478,11 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
     // slot of (buffer, vector v: 0 alpha_m / 1 beta_{m+1}, bj, q) for this thread
     auto slot = [&](int buf, int v, int bj, int q) -> uint4* {
         return sbuf + ((size_t)((buf * 2 + v) * B + bj) * NP + q) * kThreads + threadIdx.x;
+    };
+    // slot of the own row (v: 0 alpha_{m+1} / 1 beta_{m+2}, bi, q)
+    uint4* sown = sbuf + (size_t)4 * B * NP * kThreads;
+    auto own_slot = [&](int v, int bi, int q) -> uint4* {
+        return sown + ((size_t)(v * B + bi) * NP + q) * kThreads + threadIdx.x;
     };
 
     const int sidx = a.cta_sys[blockIdx.x];
@@ -563,6 +570,21 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
                 return cc;
             };
             const int nrow = ke - kb;
+            if (active) {
+#pragma unroll
+                for (int bi = 0; bi < B; bi++) {
+                    const uint4* rap = reinterpret_cast<const uint4*>(Ap + (size_t)(B * i + bi) * a.ld);
+                    const uint4* rbp = reinterpret_cast<const uint4*>(Bp + (size_t)(B * i + bi) * a.ld);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        const int pk = base + g + Gp * q;
+                        if (FULL || pk < P) {
+                            cp_async16(own_slot(0, bi, q), rap + pk);
+                            cp_async16(own_slot(1, bi, q), rbp + pk);
+                        }
+                    }
+                }
+            }
             unsigned cc_next = 0;
             if (nrow > 0) cc_next = issue(kb, 0);
             cp_async_commit();
@@ -622,8 +644,19 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
                 for (int bi = 0; bi < B; bi++) {
                     const size_t roff = (size_t)(B * i + bi) * a.ld;
                     E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
-                    ld_rw<S, NP, FULL>(apv, Ap + roff, base, g, Gp, P);
-                    ld_rw<S, NP, FULL>(bpv, Bp + roff, base, g, Gp, P);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        const int pk = base + g + Gp * q;
+                        Packet<E, EPP> pa, pb;
+                        pa.u = make_uint4(0u, 0u, 0u, 0u);
+                        pb.u = make_uint4(0u, 0u, 0u, 0u);
+                        if (FULL || pk < P) {
+                            pa.u = *own_slot(0, bi, q);
+                            pb.u = *own_slot(1, bi, q);
+                        }
+#pragma unroll
+                        for (int e = 0; e < EPP; e++) { apv[q * EPP + e] = pa.e[e]; bpv[q * EPP + e] = pb.e[e]; }
+                    }
 #pragma unroll
                     for (int e = 0; e < EPT; e++) {
                         an[e] = S::fin(accA[bi][e], true, true, apv[e]);
