@@ -570,7 +570,10 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
                 return cc;
             };
             const int nrow = ke - kb;
-            if (active) {
+            // FP32: own rows copied now (cubic L=64: 2.08 vs 2.17 ms); float-float, issue-bound,
+            // loads them at the end as the one-pass kernel does (9.77 vs 9.81 ms)
+            constexpr bool kOwnAsync = S::PREC == 1;
+            if (kOwnAsync && active) {
 #pragma unroll
                 for (int bi = 0; bi < B; bi++) {
                     const uint4* rap = reinterpret_cast<const uint4*>(Ap + (size_t)(B * i + bi) * a.ld);
@@ -644,18 +647,23 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
                 for (int bi = 0; bi < B; bi++) {
                     const size_t roff = (size_t)(B * i + bi) * a.ld;
                     E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
+                    if constexpr (kOwnAsync) {
 #pragma unroll
-                    for (int q = 0; q < NP; q++) {
-                        const int pk = base + g + Gp * q;
-                        Packet<E, EPP> pa, pb;
-                        pa.u = make_uint4(0u, 0u, 0u, 0u);
-                        pb.u = make_uint4(0u, 0u, 0u, 0u);
-                        if (FULL || pk < P) {
-                            pa.u = *own_slot(0, bi, q);
-                            pb.u = *own_slot(1, bi, q);
+                        for (int q = 0; q < NP; q++) {
+                            const int pk = base + g + Gp * q;
+                            Packet<E, EPP> pa, pb;
+                            pa.u = make_uint4(0u, 0u, 0u, 0u);
+                            pb.u = make_uint4(0u, 0u, 0u, 0u);
+                            if (FULL || pk < P) {
+                                pa.u = *own_slot(0, bi, q);
+                                pb.u = *own_slot(1, bi, q);
+                            }
+#pragma unroll
+                            for (int e = 0; e < EPP; e++) { apv[q * EPP + e] = pa.e[e]; bpv[q * EPP + e] = pb.e[e]; }
                         }
-#pragma unroll
-                        for (int e = 0; e < EPP; e++) { apv[q * EPP + e] = pa.e[e]; bpv[q * EPP + e] = pb.e[e]; }
+                    } else {
+                        ld_rw<S, NP, FULL>(apv, Ap + roff, base, g, Gp, P);
+                        ld_rw<S, NP, FULL>(bpv, Bp + roff, base, g, Gp, P);
                     }
 #pragma unroll
                     for (int e = 0; e < EPT; e++) {
