@@ -64,6 +64,11 @@ def dist_init():
     return 0, 1, None
 
 
+def replica_value(per_solve, steps, ws, ms_max):
+    """Whole-job rate of N replicas: every rank's solves over the slowest rank's time."""
+    return per_solve * steps * ws / (ms_max / 1e3)
+
+
 def barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -273,7 +278,7 @@ def run_gb300(args, rank, ws, dist):
     prof = {k: eng.profile(k) for k in range(4)}
     eng.set_profiling(0)
     ms_max = max_over_ranks(dist, ms)
-    value = per_solve * args.steps * ws / (ms_max / 1e3)
+    value = replica_value(per_solve, args.steps, ws, ms_max)
     mu = eng.fetch_moments(M)
     eng.fetch_D(D)
 
