@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, St
     typedef typename S::H H;
     constexpr int EPP = S::EPP;
     constexpr int EPT = NP * EPP;
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(16) unsigned char smem[];   // dynamic shared memory starts 16-byte aligned or better
     const int Gp = a.Gp, P = a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem);
