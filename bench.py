@@ -11,7 +11,13 @@ far larger than the 129 MB L2, so no L2 flush is needed between steps.
   value  device-resident throughput: H and R already on the GPU, solves enqueued
          back to back, timed with CUDA events on the engine's stream.
   e2e    the same metric through the public API with host buffers: every step
-         uploads H and R from pinned host memory and reads back mu and D.
+         uploads H and the colour probes' nonzeros (set_R_sparse) from pinned host
+         memory and reads back mu and D; e2e_dense_R does the same with the dense
+         n x S probe block (set_R, what the reference's transfer_R moves).
+  roofline        HBM roofline of the dominant kernel (the fused adjoint step):
+                  algorithmic bytes per launch / live CUDA-event launch time.
+  roofline_issue  (float-float) the same launch against the GPU's warp-instruction
+                  issue rate, from the ncu instruction count of the L=32 capture.
   --impl reference: the reference's CPU engine restated (oracle port), all host
          threads, each step a bounded sample (same workload, smaller M).
 Multi-GPU (torchrun): replicas only -- every rank solves its own copy; value is
