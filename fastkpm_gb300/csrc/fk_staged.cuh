@@ -1,8 +1,15 @@
-// fk_staged.cuh -- Chebyshev step with the neighbour gathers staged by TMA bulk copies.
+// fk_staged.cuh -- step and reverse-step kernels whose neighbour gathers go through
+// shared memory, in two designs:
 //
-// The plain step kernel gathers x rows with per-thread loads and stalls on their
-// latency (long-scoreboard is its top stall; registers cap it at 16 warps/SM).
-// Here a tile of kThreads (row, lane) items is served from shared memory:
+//  1. k_cheb_step_staged (FK_OPT_TMA, off by default): a whole tile's gathers staged
+//     by TMA bulk / cp.async copies from per-tile column lists (below);
+//  2. k_cheb_step_pipe / k_adjoint_pipe (FK_OPT_PIPE, the default for b=2 FP32 and
+//     float-float and for the FP32 adjoint): every thread double-buffers its own
+//     packets of the next block with 16-byte cp.async copies (end of this file).
+//
+// The plain kernels gather rows with per-thread loads and stall on their latency
+// (long-scoreboard is their top stall; registers cap them at 16-24 warps/SM).
+// In design 1 a tile of kThreads (row, lane) items is served from shared memory:
 //   * the host lists, per tile, the distinct block columns its rows touch (own
 //     rows included), sorted, and for every H block its slot in that list;
 //   * per column chunk of W = Gp * NP packets, warp 0 issues one 1-D
