@@ -312,7 +312,7 @@ double mu_to_filling(Vec<double> const& gamma, EnergyScale const& es, double kT,
     const double tot = density_product(gamma, [](double) { return 1.0; }, es);
     return occ / tot;
 }
-// Chemical potential for a filling (src/fastkpm.cpp:413-427): thermal smearing
+// Chemical potential for a filling (src/fastkpm.cpp:418-432): thermal smearing
 // kT' = max(kT, 0.1 mag / Mq), bracket [lo - max(c, 0), hi + max(-c, 0)] with
 // c = kT' log(1/filling - 1), root of mu_to_filling(gamma, es, kT', mu) = filling
 // (two roots at filling +- delta_filling, averaged, when delta_filling != 0). The
@@ -535,7 +535,7 @@ public:
             }
         return mu;
     }
-    // R2 must have R's shape (the reference asserts it, src/engine_cpu.cpp:175); an empty R2
+    // R2 must have R's shape (the reference asserts it, src/engine_cpu.cpp:174); an empty R2
     // means R2 = R. The chunk arguments are unused, as in the reference.
     Vec<Vec<cx_double>> moments2_v2(int M, SpMatBsr<T> const& j1op, SpMatBsr<T> const& j2op, int, int) override {
         for (auto* j : {&j1op, &j2op})

@@ -68,8 +68,8 @@ static __global__ void k_moment_transform(const double* mu, int M, int Mq, doubl
 // Chemical potential for a filling and the electronic energy (one CTA of kPostThreads):
 //   kT' = max(kT, 0.1 mag / Mq) (thermal smearing), bracket [lo - max(c, 0), hi + max(-c, 0)],
 //   c = kT' log(1/filling - 1); root of mu_to_filling(gamma, kT', mu) = filling (+-delta, averaged)
-//   by bisection (filling_to_mu, src/fastkpm.cpp:413-427; the reference solves the same bracket
-//   with toms748 to 30 bits); energy = electronic_energy(gamma, es, kT, filling, mu) (:463-467).
+//   by bisection (filling_to_mu, src/fastkpm.cpp:418-432; the reference solves the same bracket
+//   with toms748 to 30 bits); energy = electronic_energy(gamma, es, kT, filling, mu) (:452-456).
 // out = {mu, energy, n_tot} with n_tot = sum_i gamma_i / Mq.
 static __global__ void k_filling_solve(const double* gamma, const double* energies, int Mq, double lo, double hi,
                                        double kT, double filling, double delta, double* out) {

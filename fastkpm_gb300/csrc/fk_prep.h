@@ -1,7 +1,7 @@
 // fk_prep.h -- host preprocessing of a Hamiltonian for the device kernels, shared by
 // the single engine (fk_engine.cu) and the batched engine (fk_batch.cu).
 //
-// Carries out set_H's scaling Hs = (H - avg I)/mag (reference src/engine_cpu.cpp:189-197,
+// Carries out set_H's scaling Hs = (H - avg I)/mag (reference src/engine_cpu.cpp:53-61,
 // src/engine_cusparse.cpp:701-730), inserts a zero diagonal block in rows that store
 // none, classifies every block (2: real multiple of the identity, 1: real entries,
 // 0: general) and converts the entries to the engine precision.

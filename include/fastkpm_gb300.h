@@ -95,7 +95,7 @@ int  fk_engine_synchronize(fk_engine* e);
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 
-/* Engine<T>::set_H(H, es) (reference src/engine_cusparse.cpp:701-730, src/engine_cpu.cpp:189-197):
+/* Engine<T>::set_H(H, es) (reference src/engine_cusparse.cpp:701-730, src/engine_cpu.cpp:53-61):
  * Hs = (H - avg I)/mag with avg = (lo+hi)/2, mag = (hi-lo)/2. n_b block rows of b x b blocks;
  * row_ptr[n_b+1], col_idx[nnzb] sorted within each row; val[nnzb*b*b] column-major blocks.
  * Rows without a stored diagonal block receive one. b must be 1 or 2. */
@@ -112,20 +112,20 @@ int  fk_engine_set_R_sparse(fk_engine* e, int n, int s, int k, const int* cols, 
 /* Read back the device copy of R (column-major n x s), converted to double. */
 int  fk_engine_get_R(fk_engine* e, double* R);
 
-/* Engine<T>::moments(M) (reference src/engine_cusparse.cpp:755-791, src/engine_cpu.cpp:199-220):
+/* Engine<T>::moments(M) (reference src/engine_cusparse.cpp:755-791, src/engine_cpu.cpp:63-84):
  * mu[M] for even M >= 2. Leaves alpha_{M/2-1}, alpha_{M/2} on the device for autodiff. */
 int  fk_engine_moments(fk_engine* e, int M, double* mu);
 /* Same work, enqueued only; fk_engine_fetch_moments() waits and copies mu[M] out. */
 int  fk_engine_moments_async(fk_engine* e, int M);
 int  fk_engine_fetch_moments(fk_engine* e, double* mu);
 
-/* Engine<T>::stoch_matrix(c, D) (reference src/engine_cusparse.cpp:910-953, src/engine_cpu.cpp:365-389):
+/* Engine<T>::stoch_matrix(c, D) (reference src/engine_cusparse.cpp:910-953, src/engine_cpu.cpp:229-253):
  * D = (R xi^dag + xi R^dag)/2 on D's BSR pattern, xi = sum_{m<M} c_m T_m(Hs) R.
  * D pattern: d_n_b block rows (= H's), d_nnzb blocks, row_ptr/col_idx; D_val[d_nnzb*b*b] out. */
 int  fk_engine_stoch_matrix(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb,
                             const int* d_row_ptr, const int* d_col_idx, double* D_val);
 /* Engine<T>::autodiff_matrix(c, D) (reference src/engine_cusparse.cpp:955-1039,
- * src/engine_cpu.cpp:391-440): reverse-mode derivative of tr g, symmetrized and divided by
+ * src/engine_cpu.cpp:255-304): reverse-mode derivative of tr g, symmetrized and divided by
  * the energy scale. Requires fk_engine_moments with the same M first (FK_ERR_STATE otherwise).
  * D's pattern must be symmetric (FK_ERR_PATTERN otherwise). */
 int  fk_engine_autodiff_matrix(fk_engine* e, int M, const double* c, int d_n_b, int d_nnzb,
@@ -138,7 +138,7 @@ int  fk_engine_autodiff_matrix_async(fk_engine* e, int M, const double* c, int d
 int  fk_engine_fetch_D(fk_engine* e, double* D_val);
 
 /* Engine<T>::energy_scale(H, extend, iters) (reference src/engine_cusparse.cpp:598-673,
- * src/engine_cpu.cpp:150-187): Lanczos on the device (iters SpMV steps from the start vector
+ * src/engine_cpu.cpp:14-51): Lanczos on the device (iters SpMV steps from the start vector
  * v0[n], or a seeded start when v0 is NULL), extremal eigenvalues of the tridiagonal by
  * bisection, widened by extend*(max-min) on each side. */
 int  fk_engine_energy_scale(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr,
@@ -177,10 +177,10 @@ int  fk_engine_moments2_v2(fk_engine* e, int M, int j1_nnzb, const int* j1_row_p
 
 /* KPM post-processing of the last moments(M) on the device, with no host round trip after
  * the moments: gamma = moment_transform(mu, Mq) (reference src/fastkpm.cpp:236-256), the
- * chemical potential mu_F = filling_to_mu(gamma, es, kT, filling, delta_filling) (:413-427:
+ * chemical potential mu_F = filling_to_mu(gamma, es, kT, filling, delta_filling) (:418-432:
  * thermal smearing kT' = max(kT, 0.1 mag / Mq), the same bracket, root by bisection where
  * the reference uses toms748 to 30 bits, so the two agree to that tolerance), and
- * E = electronic_energy(gamma, es, kT, filling, mu_F) (:463-467). result[3] = {mu_F, E, n_tot}
+ * E = electronic_energy(gamma, es, kT, filling, mu_F) (:452-456). result[3] = {mu_F, E, n_tot}
  * with n_tot = density_product(gamma, 1) (:314-322); gamma[Mq] out when not NULL.
  * Needs 0 < filling - delta_filling, filling + delta_filling < 1, Mq >= M. No reference C entry
  * point: it replaces the caller's host calls between moments() and autodiff_matrix(). */
@@ -225,7 +225,7 @@ int  fk_batch_commit(fk_batch* bt);
 /* mu[index * M + m] for every system, even M >= 2: M/2 launches, each covering all systems,
  * replayed from a CUDA graph when FK_OPT_GRAPHS is on. */
 int  fk_batch_moments(fk_batch* bt, int M, double* mu);
-/* Engine<T>::autodiff_matrix(c, D) (reference src/engine_cpu.cpp:391-440) for every system of the
+/* Engine<T>::autodiff_matrix(c, D) (reference src/engine_cpu.cpp:255-304) for every system of the
  * batch in the same launches, after fk_batch_moments with the same M (FK_ERR_STATE otherwise).
  * c[sys*M + m]: each system's coefficients. D_val: each system's D on its own H pattern (as added),
  * systems in index order, b*b (complex: interleaved) values per block; symmetrized and divided by

@@ -93,7 +93,7 @@ struct Engine {
     double mag() const { return (es_hi - es_lo) / 2.0; }   // EnergyScale::mag (fastkpm.h:116)
 
     // y = alpha * Hs * x + beta * z  (row-major n x s); Armadillo's SpMat*Mat in
-    // src/engine_cpu.cpp:207,212,372,376,422,426, with the scalar row sum taken in
+    // src/engine_cpu.cpp:71,76,236,240,286,290, with the scalar row sum taken in
     // ascending column order.
     void spmm(double alpha, const Bsr<T>& H, const std::vector<T>& x, double beta,
               const std::vector<T>* z, std::vector<T>& y) const {
@@ -143,7 +143,7 @@ struct Engine {
         return r;
     }
 
-    // outer_product (src/engine_cpu.cpp:348-362):
+    // outer_product (src/engine_cpu.cpp:212-226):
     // D_k(bi, bj) += alpha * cdot(B.row(b j + bj), A.row(b i + bi)) for k = (i, j)
     void outer_product(T alpha, const std::vector<T>& A, const std::vector<T>& B, int nnzb,
                        const int* rows, const int* cols, int b, T* D) const {
@@ -240,7 +240,7 @@ int set_H(Engine<T>& e, int n_b, int b, int nnzb, const int* row_ptr, const int*
           const T* val, double lo, double hi) {
     if (n_b <= 0 || b <= 0 || nnzb < 0) return 1;
     e.es_lo = lo; e.es_hi = hi;
-    // Hs = (H - avg I)/mag (src/engine_cpu.cpp:189-197). A row without a stored
+    // Hs = (H - avg I)/mag (src/engine_cpu.cpp:53-61). A row without a stored
     // diagonal block receives one (Armadillo inserts the element on Hs(i,i) -= avg).
     Bsr<T>& H = e.Hs;
     H.n_b = n_b; H.b = b;
@@ -316,7 +316,7 @@ int stoch_matrix(Engine<T>& e, int M, const double* c, int nnzb, const int* rows
     std::fill(D, D + size_t(b) * b * nnzb, T(0));
     e.outer_product(T(0.5), e.R, xi, nnzb, rows, cols, b, D);
     e.outer_product(T(0.5), xi, e.R, nnzb, rows, cols, b, D);
-    e.have_moment_state = false;                             // a0, a1 cleared (:386-388)
+    e.have_moment_state = false;                             // a0, a1 cleared (:249-251)
     return 0;
 }
 
@@ -354,7 +354,7 @@ int autodiff_matrix(Engine<T>& e, int M, const double* c, int nnzb, const int* r
     return 0;
 }
 
-// Lanczos (src/engine_cpu.cpp:150-187) with caller-given start vector.
+// Lanczos (src/engine_cpu.cpp:14-51) with caller-given start vector.
 template <typename T>
 int energy_scale(Engine<T>& e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
                  const T* val, double extend, int iters, const T* v_start, double* lo, double* hi) {
@@ -830,9 +830,9 @@ double orc_mu_to_filling(int Mq, const double* gamma, double lo, double hi, doub
     return density_product(Mq, gamma, 0, kT, mu, lo, hi) / density_product(Mq, gamma, -1, kT, mu, lo, hi);
 }
 
-// filling_to_mu (src/fastkpm.cpp:413-427): smearing kT' = max(kT, 0.1 mag / Mq), bracket
+// filling_to_mu (src/fastkpm.cpp:418-432): smearing kT' = max(kT, 0.1 mag / Mq), bracket
 // [lo - max(c, 0), hi + max(-c, 0)] with c = kT' log(1/filling - 1); the reference's toms748
-// root (30-bit tolerance, src/fastkpm.cpp:405-411) is replaced by bisection to 1e-14, so the
+// root (30-bit tolerance, src/fastkpm.cpp:410-416) is replaced by bisection to 1e-14, so the
 // two agree to the reference's tolerance; two roots at filling +- delta are averaged.
 double orc_filling_to_mu(int Mq, const double* gamma, double lo, double hi, double kT, double filling,
                          double delta_filling) {
@@ -853,7 +853,7 @@ double orc_filling_to_mu(int Mq, const double* gamma, double lo, double hi, doub
     return 0.5 * (root(filling + delta_filling) + root(filling - delta_filling));
 }
 
-// electronic_energy (src/fastkpm.cpp:463-467) = electronic_grand_energy (:448-451) + mu n_occ
+// electronic_energy (src/fastkpm.cpp:452-456) = electronic_grand_energy (:440-443) + mu n_occ
 double orc_electronic_energy(int Mq, const double* gamma, double lo, double hi, double kT, double filling, double mu) {
     const double n_tot = density_product(Mq, gamma, -1, kT, mu, lo, hi);
     return density_product(Mq, gamma, 1, kT, mu, lo, hi) + mu * filling * n_tot;

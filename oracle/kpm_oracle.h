@@ -26,25 +26,25 @@ extern "C" {
 
 typedef struct orc_engine orc_engine;
 
-/* Engine_CPU<T> (src/engine_cpu.cpp:141-441); nthreads <= 0 -> all usable cores */
+/* Engine_CPU<T> (src/engine_cpu.cpp:6-305); nthreads <= 0 -> all usable cores */
 orc_engine* orc_engine_create(int cplx, int nthreads);
 void orc_engine_destroy(orc_engine* e);
 int  orc_engine_threads(const orc_engine* e);
-/* set_H (src/engine_cpu.cpp:189-197): Hs = (H - avg I) / mag */
+/* set_H (src/engine_cpu.cpp:53-61): Hs = (H - avg I) / mag */
 int  orc_set_H(orc_engine* e, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
                const double* val, double es_lo, double es_hi);
 /* R (column-major n x s), as left in Engine<T>::R by set_R_* */
 int  orc_set_R(orc_engine* e, int n, int s, const double* R);
-/* moments (src/engine_cpu.cpp:199-220) */
+/* moments (src/engine_cpu.cpp:63-84) */
 int  orc_moments(orc_engine* e, int M, double* mu);
-/* stoch_matrix (src/engine_cpu.cpp:365-389); D pattern given by row/col idx */
+/* stoch_matrix (src/engine_cpu.cpp:229-253); D pattern given by row/col idx */
 int  orc_stoch_matrix(orc_engine* e, int M, const double* c, int nnzb, const int* D_row_idx,
                       const int* D_col_idx, double* D_val);
-/* autodiff_matrix (src/engine_cpu.cpp:391-440); needs orc_moments(M) first */
+/* autodiff_matrix (src/engine_cpu.cpp:255-304); needs orc_moments(M) first */
 int  orc_autodiff_matrix(orc_engine* e, int M, const double* c, int n_b, int nnzb,
                          const int* D_row_ptr, const int* D_row_idx, const int* D_col_idx,
                          double* D_val);
-/* Lanczos energy_scale (src/engine_cpu.cpp:150-187) with a caller-given start vector
+/* Lanczos energy_scale (src/engine_cpu.cpp:14-51) with a caller-given start vector
  * (the reference draws arma::randn, which is not reproducible without Armadillo) and
  * Sturm-bisection eigenvalues of the tridiagonal matrix in place of arma::eig_sym. */
 int  orc_energy_scale(orc_engine* e, int n_b, int b, int nnzb, const int* row_ptr,
@@ -93,7 +93,7 @@ int    orc_moments2_v2(orc_engine* e, int M, int n_b, int b, const int* rp1, con
 int    orc_electrical_conductivity_coefficients(int M, int Mq, double kT, double mu, double omega, double lo,
                                                 double hi, const double* kernel, double* out);
 /* moment_transform, mu_to_filling, filling_to_mu, electronic_energy (src/fastkpm.cpp:236-256,
- * :395-400, :413-427, :463-467); es = [lo, hi] */
+ * :395-400, :418-432, :452-456); es = [lo, hi] */
 void   orc_moment_transform(int M, const double* mu, int Mq, double* gamma);
 double orc_mu_to_filling(int Mq, const double* gamma, double lo, double hi, double kT, double mu);
 double orc_filling_to_mu(int Mq, const double* gamma, double lo, double hi, double kT, double filling,
