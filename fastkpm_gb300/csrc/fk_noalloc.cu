@@ -12,14 +12,15 @@
 // the process exits). No cudaMalloc, cudaFree or allocating library routine is
 // called.
 //
-// The array's name is only a host-side stand-in in host code: its device
-// address is taken with cudaGetSymbolAddress once per device (first call on that
-// device, with the device current) and passed to the kernels. Every call shares
-// the array and it keeps the last call's contents, so calls that overlap on the
-// GPU race with each other.
+// The array's name is only a host-side stand-in in host code: every call looks
+// up its device address with cudaGetSymbolAddress (the current device's copy; the
+// lookup allocates nothing) and passes it to the kernels, so the address is never
+// stale, also after a cudaDeviceReset. Every call shares the array and it keeps
+// the last call's contents, so calls that overlap on the GPU race with each other.
 #include <cuda_runtime.h>
 
-#include <mutex>
+#include <algorithm>
+#include <cstdint>
 
 #include "../../include/fastkpm_gb300.h"
 #include "fk_dispatch.h"
@@ -36,12 +37,12 @@ constexpr size_t kScratchBytes = kCtaOff + sizeof(int) * kMaxCtas;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {nullptr};
-
-__global__ void k_noalloc_sys(fk::SysDesc* sys, int n_b, int ctas) {
-    sys[0] = fk::SysDesc{0, n_b, 0, ctas};
+// The one-system launch tables, written on the caller's stream before the first step of every
+// call: the system descriptor, and the CTA -> system table (all zeros: every CTA serves system 0).
+__global__ void k_noalloc_sys(fk::SysDesc* sys, int* cta_sys, int n_b, int ctas) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) sys[0] = fk::SysDesc{0, n_b, 0, ctas};
+    if (t < kMaxCtas) cta_sys[t] = 0;
 }
 
 // Fixed-order sum of one step's CTA partials into raw[0..1].
@@ -56,23 +57,11 @@ __global__ void k_noalloc_reduce(const double* partials, int ctas, double* raw) 
     if (lane == 0) { raw[0] = a; raw[1] = b; }
 }
 
-// Device address of the scratch array on the current device (set up on first use).
+// Device address of the scratch array on the current device, looked up on every call.
 int scratch_for_current_device(unsigned char** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return FK_ERR_CUDA; }
-    if (dev < 0 || dev >= kMaxDevices) return FK_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) { cudaGetLastError(); return FK_ERR_CUDA; }
-        // the CTA -> system table of a one-system launch is all zeros
-        if (cudaMemset((unsigned char*)p + kCtaOff, 0, sizeof(int) * kMaxCtas) != cudaSuccess) {
-            cudaGetLastError();
-            return FK_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = (unsigned char*)p;
-    }
-    *out = g_scratch_addr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) { cudaGetLastError(); return FK_ERR_CUDA; }
+    *out = (unsigned char*)p;
     return FK_OK;
 }
 
@@ -91,8 +80,10 @@ extern "C" int fk_moments_noalloc(int kind, int n_b, int b, const int* d_row_ptr
     const int cplx = kind == FK_COMPLEX ? 1 : 0;
     const int epp = fk::elems_per_packet(fk::kF64, cplx);
     const size_t esz = (size_t)fk::elem_bytes(fk::kF64, cplx);
-    // 16-byte packets: rows of ld elements must start on 16-byte boundaries
+    // 16-byte packets: rows of ld elements must start on 16-byte boundaries; H values are read as
+    // whole elements (double2 for FK_COMPLEX), row pointers and columns as 4-byte ints
     if (ld % epp != 0 || ((uintptr_t)d_R % 16) || ((uintptr_t)d_work % 16)) return FK_ERR_ARG;
+    if (((uintptr_t)d_hs_val % esz) || ((uintptr_t)d_row_ptr % 4) || ((uintptr_t)d_col_idx % 4)) return FK_ERR_ARG;
     unsigned char* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc != FK_OK) return rc;
@@ -114,10 +105,10 @@ extern "C" int fk_moments_noalloc(int kind, int n_b, int b, const int* d_row_ptr
     if (ctas < 1) ctas = 1;
 
     fk::SysDesc* sys = reinterpret_cast<fk::SysDesc*>(scratch + kSysOff);
-    const int* cta_sys = reinterpret_cast<const int*>(scratch + kCtaOff);
+    int* cta_sys = reinterpret_cast<int*>(scratch + kCtaOff);
     double* partials = reinterpret_cast<double*>(scratch + kPartialsOff);
     double* raw = reinterpret_cast<double*>(scratch + kRawOff);
-    k_noalloc_sys<<<1, 1, 0, st>>>(sys, n_b, (int)ctas);
+    k_noalloc_sys<<<(kMaxCtas + 255) / 256, 256, 0, st>>>(sys, cta_sys, n_b, (int)ctas);
     if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
 
     const size_t vec = (size_t)n_b * b * (size_t)ld;   // elements per vector

@@ -254,17 +254,20 @@ int  fk_batch_info(const fk_batch* bt, int* n_systems, long long* total_rows, si
  * routine is called.
  *   d_row_ptr[n_b+1], d_col_idx[nnzb] (each < 2^30), d_hs_val[nnzb*b*b]: the SCALED matrix
  *     Hs = (H - avg I)/mag as device BSR (column-major b x b blocks; interleaved (re, im) for
- *     FK_COMPLEX); the pattern is trusted, not checked.
+ *     FK_COMPLEX); the pattern is trusted, not checked. d_hs_val must be aligned to a whole
+ *     element (16 bytes for FK_COMPLEX, 8 for FK_REAL), d_row_ptr and d_col_idx to 4 bytes.
  *   d_R: device, row-major (n_b*b) x ld doubles (complex: pairs), zero in columns s..ld-1;
  *     ld a multiple of 2 for FK_REAL; 16-byte aligned.  d_work: device, 2 * (n_b*b) * ld
  *     elements for the two recursion vectors (overwritten).  mu: host, M doubles out.
  *   stream: a cudaStream_t or NULL (the legacy default stream); the call waits for it.
  * Limits: even M with 2 <= M <= 32768; larger M returns FK_ERR_UNSUPPORTED (the static
  * scratch holds 16384 steps); malformed arguments return FK_ERR_ARG.
- * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture. All calls share
- * the array and it keeps the last call's contents, so calls that overlap on the GPU (from
- * different streams or threads) race with each other: serialise them. */
+ * Every call looks up the array's device address on the current device (cudaGetSymbolAddress,
+ * which allocates nothing); the first lookup on a device loads the library's device code, so
+ * make the first call on each device before any stream capture. The launch tables in the array
+ * are rewritten on `stream` at the start of every call. All calls share the array and it keeps
+ * the last call's contents, so calls that overlap on the GPU (from different streams or
+ * threads) race with each other: serialise them. */
 int  fk_moments_noalloc(int kind, int n_b, int b, const int* d_row_ptr, const int* d_col_idx,
                         const double* d_hs_val, long long ld, int s, const double* d_R, double* d_work,
                         int M, double* mu, void* stream);
