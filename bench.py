@@ -8,18 +8,28 @@ zero-temperature Fermi-energy expansion. Synthetic seeded data: random unit
 spins, seeded unit-phase colour probes. Every vector (N x S x 16 B = 2 GiB) is
 far larger than the 129 MB L2, so no L2 flush is needed between steps.
 
+The headline line is the native-FP64 engine (--precision fp64, the reference's
+arithmetic). The same line carries "legs": the float-float (ds) and FP32-recursion
+engines on the same workload, each with its own rate, rooflines, end-to-end rate
+and its error against the FP64 engine at the full M (same H, R and c).
+
   value  device-resident throughput: H and R already on the GPU, solves enqueued
          back to back, timed with CUDA events on the engine's stream.
   e2e    the same metric through the public API with host buffers: every step
          uploads H and the colour probes' nonzeros (set_R_sparse) from pinned host
-         memory and reads back mu and D; e2e_dense_R does the same with the dense
-         n x S probe block (set_R, what the reference's transfer_R moves).
-  roofline        HBM roofline of the dominant kernel (the fused adjoint step):
-                  algorithmic bytes per launch / live CUDA-event launch time.
-  roofline_issue  (float-float) the same launch against the GPU's warp-instruction
-                  issue rate, from the ncu instruction count of the L=32 capture.
-  --impl reference: the reference's CPU engine restated (oracle port), all host
-         threads, each step a bounded sample (same workload, smaller M).
+         memory and reads back mu and D (--e2e-dense: also with the dense n x S R).
+  roofline           HBM roofline of the dominant kernel (the fused adjoint step):
+                     algorithmic bytes per launch / live CUDA-event launch time.
+  roofline_fp64_pipe (FP64) the same launch's algorithmic FP64 flops against the
+                     device's FP64 FMA rate measured in this run.
+  roofline_issue     (float-float) the launch against the GPU's warp-instruction issue
+                     rate, from the ncu instruction count of the L=32 capture.
+  cpu_baseline  the oracle port of the reference CPU engine on all host threads: one
+         moments + autodiff_matrix solve at M=8 and one at M=16 of the full workload,
+         the solve time extrapolated linearly in M to M=1000 (t = F + M c).
+  --impl reference: that CPU engine restated (oracle port), all host threads, each step
+         a M=8 solve of the full workload, the rate extrapolated to M=1000 as above; the
+         one-thread rate is measured on the L=32 lattice. Loads only the oracle library.
 Multi-GPU (torchrun): replicas only -- every rank solves its own copy; value is
 the sum over ranks divided by the slowest rank's time.
 """
@@ -46,13 +56,20 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="ds", choices=["ds", "fp64", "fp32"])
+    p.add_argument("--precision", default=None, choices=["ds", "fp64", "fp32"],
+                   help="engine of the headline value (default fp64, the reference's arithmetic; "
+                        "--workload square: fp32)")
+    p.add_argument("--legs", default="ds,fp32", help="other precisions timed on the same workload ('' for none)")
+    p.add_argument("--leg-steps", type=int, default=0, help="timed solves per leg (0: ds min(steps,3), fp32 min(steps,5))")
+    p.add_argument("--e2e-steps", type=int, default=1, help="timed end-to-end solves per engine (0: no e2e)")
+    p.add_argument("--e2e-dense", action="store_true", help="also time e2e with the dense n x S probe block")
     p.add_argument("--L", type=int, default=64)
     p.add_argument("--M", type=int, default=1000)
     p.add_argument("--S", type=int, default=256)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--cpu-M", type=int, default=8)
+    p.add_argument("--cpu-M", default="8,16", help="orders of the two CPU sample solves (extrapolated in M)")
+    p.add_argument("--cpu-L1", type=int, default=32, help="lattice of the one-thread CPU sample (reference arm)")
     p.add_argument("--workload", default="solve", choices=["solve", "precision", "batch", "serve", "cfg1", "square"])
     p.add_argument("--serve-requests", type=int, default=24)
     p.add_argument("--serve-max-sites", type=float, default=1e6)
@@ -138,13 +155,16 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------- workload
-def workload(args):
+def workload(args, coefficients=None, L=None):
+    """(H, es, R, c) of the cubic spin-lattice solve; numpy only, except the coefficients:
+    `coefficients(M, es)` when given (the reference arm passes the oracle's), else the
+    library's FP64 expansion_coefficients."""
     from fastkpm_gb300 import workloads as W
-    cfg = W.config2(L=args.L, S=args.S)
+    cfg = W.config2(L=L or args.L, S=args.S)
     H, es = cfg["H"], cfg["es"]
     R = W.phase_probes(cfg["groups"], cfg["realisations"], cfg["probe_seed"])
     R = R[:, :args.S] if R.shape[1] > args.S else R
-    c = W.fermi_coefficients(args.M, es, "fermi_energy")
+    c = coefficients(args.M, es) if coefficients else W.fermi_coefficients(args.M, es, "fermi_energy")
     return H, es, np.asfortranarray(R), c
 
 
@@ -156,25 +176,52 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def h_bytes(nnzb, b, sv, n_b):
+    return nnzb * (b * b * sv + 4) + 4 * (n_b + 1)
+
+
 def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
     """Algorithmic bytes of one adjoint launch (the kernel walks all S columns itself): read alpha_m,
     alpha_{m+1}, beta_{m+1}, beta_{m+2}, write alpha_{m-1}, beta_m (6 vectors), H once (entries +
     4-byte column index), row_ptr, and, when the D epilogue is fused, the D accumulator read + write
     (8 bytes per real: double or float-float)."""
-    vec = 6 * N * S * sv
-    h = nnzb * (b * b * sv + 4) + 4 * (N // b + 1)
     d = 2 * nnzb * b * b * 16 if fused else 0
-    return vec + h + d
+    return 6 * N * S * sv + h_bytes(nnzb, b, sv, N // b) + d
 
 
-# DRAM bytes per row of one fused DS adjoint launch (k_adjoint_pipe) from the ncu capture on the
-# cubic L=32 case (profiles/k_adjoint_step_ds_cubic32.md: 1.600 GB read + 0.530 GB written for
-# 65,536 rows); traffic grows in proportion to the rows, so the L=64 launch's traffic is this times N.
-ADJ_DS_TRAFFIC_PER_ROW = (1.600211e9 + 0.529769e9) / 65536
-# Warp instructions per row of the same launch (smsp__inst_executed.sum = 1,108,457,856 for 65,536
-# rows): the fused float-float adjoint is bound by instruction issue, not by DRAM. Issue peak of
-# the GPU: 152 SMs x 4 schedulers x 1 warp instruction per cycle at the maximum SM clock.
-ADJ_DS_WARP_INST_PER_ROW = 1108457856 / 65536
+def step_bytes_per_launch(N, S, nnzb, b, sv):
+    """Algorithmic bytes of one moments step: read x (gathered) and z, write y, H once."""
+    return 3 * N * S * sv + h_bytes(nnzb, b, sv, N // b)
+
+
+def block_classes(H):
+    """(hopping blocks: real multiples of the identity, general blocks) of a b=2 complex H."""
+    v = H.val.reshape(-1, 4)
+    ident = (v[:, 1] == 0) & (v[:, 2] == 0) & (v[:, 0] == v[:, 3]) & (v.imag == 0).all(axis=1)
+    return int(ident.sum()), int((~ident).sum())
+
+
+def adjoint_flops_per_launch(H, S):
+    """Algorithmic FP64 flops of one fused adjoint launch (complex b=2, H's pattern): per block and
+    column, both recursions (a hopping block t I2: 2 complex x real MACs of 4 flops each; a general
+    block: 4 complex MACs of 8 flops) and the epilogue's 4 complex MACs; per scalar row and column,
+    2 alpha_m+1 - alpha_m-1 style finishes (4 flops each) and beta's 3 coefficient terms (12 flops)."""
+    hop, gen = block_classes(H)
+    per_col = hop * (2 * 8 + 32) + gen * (2 * 32 + 32) + H.n_rows * 2 * 20
+    return float(per_col) * S
+
+
+def step_flops_per_launch(H, S):
+    """Algorithmic FP64 flops of one moments step: the block products, the finish and the two dots."""
+    hop, gen = block_classes(H)
+    return float(hop * 8 + gen * 32 + H.n_rows * 2 * 12) * S
+
+
+# DRAM bytes and warp instructions per row of one fused adjoint launch, from ncu captures on the
+# cubic L=32 case (profiles/): traffic grows in proportion to the rows, so the L=64 launch's traffic
+# is these times N. Keys: precision. A precision without a capture of the current kernel reports null.
+ADJ_TRAFFIC_PER_ROW = {"ds": (1.600211e9 + 0.529769e9) / 65536}
+ADJ_WARP_INST_PER_ROW = {"ds": 1108457856 / 65536}
 ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
 
 
@@ -193,9 +240,14 @@ def probe_entries(R):
     return R.shape[1], cols, vals
 
 
-def run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse):
+def run_e2e(prec, steps, wl, M, per_solve, ws, dist, dev, sparse):
     """moments + autodiff_matrix through the public API, every step uploading H and the probes
-    from pinned host memory and reading mu and D back; wall and device clocks, max over ranks."""
+    from pinned host memory and reading mu and D back; wall and device clocks, max over ranks.
+    One untimed solve first (allocation of the engine's buffers)."""
+    import fastkpm_gb300 as fk
+    from fastkpm_gb300 import _lib as Lb
+    H, es, R, c = wl
+    D = H.pattern_like(True)
     lib = Lb.load()
     hv = np.ascontiguousarray(H.val)
     if sparse:
@@ -207,7 +259,7 @@ def run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse):
         Rf = np.asfortranarray(R)
         probe_bufs = [Rf]
     pinned = all(lib.fk_host_register(b.ctypes.data, b.nbytes) == 0 for b in probe_bufs + [hv])
-    e2 = fk.Engine(True, args.precision, device=dev)
+    e2 = fk.Engine(True, prec, device=dev)
 
     def set_probes():
         if sparse:
@@ -224,7 +276,7 @@ def run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse):
     phases = np.zeros(4)   # wall ms per step: set_H, set_R, moments (+ mu read), autodiff (+ D read)
     t0 = time.perf_counter()
     e2.timer_start()
-    for _ in range(args.steps):
+    for _ in range(steps):
         tp = [time.perf_counter()]
         e2.set_H(H, es)
         tp.append(time.perf_counter())
@@ -244,28 +296,28 @@ def run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse):
     for b in probe_bufs + [hv]:
         lib.fk_host_unregister(b.ctypes.data)
     e2.close()
-    return {"value": per_solve * args.steps * ws / (e2_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "ms_per_step": e2_ms / args.steps, "host_buffers_pinned": pinned,
+    return {"value": per_solve * steps * ws / (e2_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": e2_ms / steps, "steps": steps, "host_buffers_pinned": pinned,
             "probes": "nonzeros (set_R_sparse)" if sparse else "dense n x S (set_R)",
-            "phases_ms_per_step": {k: float(v) / args.steps for k, v in
+            "phases_ms_per_step": {k: float(v) / steps for k, v in
                                    zip(["set_H", "set_R", "moments", "autodiff_matrix"], phases)}}
 
 
-# ---------------------------------------------------------------------------- arms
-def run_gb300(args, rank, ws, dist):
+# ---------------------------------------------------------------------------- one engine, timed
+def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps):
+    """W untimed and K timed solves of one engine precision, device-resident; kernel times from
+    CUDA events around every launch on the engine's stream; rooflines of the adjoint and step
+    kernels; the last solve's mu and D; optional end-to-end timing."""
     import fastkpm_gb300 as fk
     from fastkpm_gb300 import _lib as Lb
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    H, es, R, c = workload(args)
+    H, es, R, c = wl
     N, S, M = R.shape[0], R.shape[1], args.M
     D = H.pattern_like(True)
-    eng = fk.Engine(True, args.precision, device=dev)
+    eng = fk.Engine(True, prec, device=dev)
     eng.set_H(H, es)
     eng.set_R(R)
     per_solve = float(N) * M * S
-
-    # ---- device-resident throughput ----
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         eng.moments_async(M)
         eng.autodiff_matrix_async(c, D)
     eng.synchronize()
@@ -275,7 +327,7 @@ def run_gb300(args, rank, ws, dist):
     eng.synchronize()
     with ClockSampler(dev) as clk:
         eng.timer_start()
-        for _ in range(args.steps):
+        for _ in range(steps):
             eng.moments_async(M)
             eng.autodiff_matrix_async(c, D)
         ms = eng.timer_stop()
@@ -284,111 +336,161 @@ def run_gb300(args, rank, ws, dist):
     prof = {k: eng.profile(k) for k in range(4)}
     eng.set_profiling(0)
     ms_max = max_over_ranks(dist, ms)
-    value = replica_value(per_solve, args.steps, ws, ms_max)
     mu = eng.fetch_moments(M)
     eng.fetch_D(D)
+    fused = eng.get_option(Lb.FK_OPT_FUSE_D) != 0
+    eng.close()
 
-    # roofline of the dominant kernel (the adjoint step)
     n_adj, t_adj = prof[1]
     n_step, t_step = prof[0]
-    sv = 8 if args.precision == "fp32" else 16
-    fuse_opt = eng.get_option(Lb.FK_OPT_FUSE_D)
-    fused = fuse_opt != 0
-    bytes_adj = adjoint_bytes_per_launch(N, S, H.n_blocks(), 2, sv, fused)
-    avg_adj_ms = t_adj / max(n_adj, 1)
-    achieved = bytes_adj / (avg_adj_ms * 1e-3) / 1e9
+    sv = 8 if prec == "fp32" else 16
+    nnzb = H.n_blocks()
     peak, peak_kind = peaks()
-    traffic = ADJ_DS_TRAFFIC_PER_ROW * N if (args.precision == "ds" and S == 256 and fused) else None
-    issue = None
-    if traffic is not None:
-        clk_mhz = max(clk.summary().get("sm_mhz") or 2070.0, 1.0)
-        inst_rate = ADJ_DS_WARP_INST_PER_ROW * N / (avg_adj_ms * 1e-3)          # warp instructions / s
+    avg_adj_ms = t_adj / max(n_adj, 1)
+    avg_step_ms = t_step / max(n_step, 1)
+    bytes_adj = adjoint_bytes_per_launch(N, S, nnzb, 2, sv, fused)
+    bytes_step = step_bytes_per_launch(N, S, nnzb, 2, sv)
+    ach_adj = bytes_adj / (avg_adj_ms * 1e-3) / 1e9
+    ach_step = bytes_step / (avg_step_ms * 1e-3) / 1e9
+    traffic = ADJ_TRAFFIC_PER_ROW[prec] * N if (prec in ADJ_TRAFFIC_PER_ROW and S == 256 and fused) else None
+    clocks = clk.summary()
+    out = dict(prec=prec, value=replica_value(per_solve, steps, ws, ms_max), ms=ms_max, steps=steps, warmup=warmup,
+               clocks=clocks, launches=sum(v[0] for v in prof.values()), mu=mu, D=D.val.copy(), fused=fused,
+               N=N, S=S, M=M, nnzb=nnzb, n_adj=n_adj, n_step=n_step, avg_adj_ms=avg_adj_ms, avg_step_ms=avg_step_ms)
+    out["roofline"] = {"bound": "hbm", "achieved": ach_adj, "peak": peak, "unit": "GB/s", "frac": ach_adj / peak,
+                       "traffic": traffic,
+                       "kernel": "fused adjoint step (both recursions%s)" % (
+                           " + D epilogue" if fused else "; D outer product apart"),
+                       "traffic_source": ("ncu DRAM bytes of the L=32 launch scaled by rows (profiles/)"
+                                          if traffic else None),
+                       "peak_source": peak_kind, "bytes_per_launch": bytes_adj, "avg_launch_ms": avg_adj_ms,
+                       "launches": n_adj}
+    out["roofline_step"] = {"bound": "hbm", "achieved": ach_step, "peak": peak, "unit": "GB/s",
+                            "frac": ach_step / peak, "kernel": "Chebyshev step (moments)",
+                            "bytes_per_launch": bytes_step, "avg_launch_ms": avg_step_ms, "launches": n_step}
+    if prec == "fp64":
+        from fastkpm_gb300 import _lib as Lb2
+        import ctypes as C
+        rate = C.c_double(0.0)
+        st = Lb2.load().fk_device_fma_rate(dev, 1, C.byref(rate))
+        fl_adj = adjoint_flops_per_launch(H, S)
+        fl_step = step_flops_per_launch(H, S)
+        a_adj = fl_adj / (avg_adj_ms * 1e-3) / 1e12
+        a_step = fl_step / (avg_step_ms * 1e-3) / 1e12
+        pk = rate.value if st == 0 else None
+        out["roofline_fp64_pipe"] = {
+            "bound": "FP64 pipe (DFMA)", "unit": "TFLOP/s", "peak": pk,
+            "peak_source": "fk_device_fma_rate: independent DFMA chains timed on this GPU in this run",
+            "adjoint": {"achieved": a_adj, "frac": a_adj / pk if pk else None, "flops_per_launch": fl_adj},
+            "step": {"achieved": a_step, "frac": a_step / pk if pk else None, "flops_per_launch": fl_step}}
+    if prec in ADJ_WARP_INST_PER_ROW and S == 256 and fused:
+        clk_mhz = max(clocks.get("sm_mhz") or 2070.0, 1.0)
+        inst_rate = ADJ_WARP_INST_PER_ROW[prec] * N / (avg_adj_ms * 1e-3)
         peak_rate = ISSUE_PEAK_WARP_INST_PER_CYCLE * clk_mhz * 1e6
-        issue = {"bound": "instruction issue (FP32 pipe: float-float arithmetic)", "achieved": inst_rate / 1e12,
-                 "peak": peak_rate / 1e12, "unit": "T warp-instructions/s", "frac": inst_rate / peak_rate,
-                 "instructions": "ncu smsp__inst_executed.sum of the L=32 launch scaled by rows (profiles/)",
-                 "peak_clock_mhz": clk_mhz}
-    launches = sum(v[0] for v in prof.values())
-
-    # ---- end to end through the public API with pinned host buffers ----
-    # The probe block goes up as its nonzeros (set_R_sparse: colour probes have one entry per row
-    # and realisation, 21 MB here) for "e2e", and as the dense column-major n x S block (set_R,
-    # what the reference's transfer_R moves, 2.1 GB) for "e2e_dense_R"; H, mu and D as in both.
-    e2e = e2e_dense = None
-    if not args.no_e2e:
-        e2e = run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse=True)
-        e2e_dense = run_e2e(args, fk, Lb, H, es, R, c, D, M, per_solve, ws, dist, dev, sparse=False)
-
-    # ---- error vs the FP64 engine on the same workload (bounded: M = 40) ----
-    err = None
-    if args.precision != "fp64":
-        Mv = min(40, M)
-        cv = c[:Mv].copy()
-        ref = fk.Engine(True, "fp64", device=dev)
-        ref.set_H(H, es)
-        ref.set_R(R)
-        mu_r = ref.moments(Mv)
-        Dr = H.pattern_like(True)
-        ref.autodiff_matrix(cv, Dr)
-        ref.close()
-        eng.set_R(R)
-        mu_t = eng.moments(Mv)
-        Dt = H.pattern_like(True)
-        eng.autodiff_matrix(cv, Dt)
-        err = {"moments_max_rel_mu0": float(np.max(np.abs(mu_t - mu_r)) / abs(mu_r[0])),
-               "D_rel_fro": float(np.linalg.norm(Dt.val - Dr.val) / np.linalg.norm(Dr.val)),
-               "vs": "native FP64 GPU engine, same H and R, M=%d" % Mv}
-    eng.close()
-    return dict(value=value, ms=ms_max, clocks=clk.summary(), prof=prof, achieved=achieved, peak=peak,
-                peak_kind=peak_kind, traffic=traffic, launches=launches, e2e=e2e, e2e_dense=e2e_dense, issue=issue, err=err, N=N, S=S, M=M,
-                nnzb=H.n_blocks(), mu0=float(mu[0]), bytes_adj=bytes_adj, fused=fused, avg_adj_ms=avg_adj_ms,
-                avg_step_ms=t_step / max(n_step, 1), n_adj=n_adj, n_step=n_step)
+        out["roofline_issue"] = {"bound": "instruction issue (FP32 pipe: float-float arithmetic)",
+                                 "achieved": inst_rate / 1e12, "peak": peak_rate / 1e12,
+                                 "unit": "T warp-instructions/s", "frac": inst_rate / peak_rate,
+                                 "instructions": "ncu smsp__inst_executed.sum of the L=32 launch scaled by rows",
+                                 "peak_clock_mhz": clk_mhz}
+    if e2e_steps > 0:
+        out["e2e"] = run_e2e(prec, e2e_steps, wl, M, per_solve, ws, dist, dev, sparse=True)
+        if args.e2e_dense:
+            out["e2e_dense_R"] = run_e2e(prec, e2e_steps, wl, M, per_solve, ws, dist, dev, sparse=False)
+    return out
 
 
-def cpu_port_rate(args, M_sample, H=None, es=None, R=None):
-    """Oracle port of the reference's CPU engine on all host threads: one moments + autodiff solve
-    at order M_sample on the full workload; returns (probe-steps/s, seconds, threads)."""
-    from fastkpm_gb300 import workloads as W
+# ---------------------------------------------------------------------------- CPU samples
+def oracle_coefficients(M, es):
     from oracle import oracle as O
-    if H is None:
-        H, es, R, _ = workload(args)
-    c = W.fermi_coefficients(M_sample, es, "fermi_energy")
-    orc = O.OracleEngine(True, nthreads=0)
-    orc.set_H(H, es)
-    orc.set_R(R)
-    t0 = time.perf_counter()
-    orc.moments(M_sample)
-    orc.autodiff_matrix(c, H.pattern_like(True))
-    dt = time.perf_counter() - t0
+    return O.expansion_coefficients(M, 2 * M, "fermi_energy", 0.0, 0.0, es.lo, es.hi)
+
+
+def cpu_solve_times(H, es, R, Ms, nthreads=0, orc=None):
+    """Seconds of one moments(M) + autodiff_matrix(c_M, D) solve of the oracle port per M in Ms."""
+    from oracle import oracle as O
+    if orc is None:
+        orc = O.OracleEngine(True, nthreads=nthreads)
+        orc.set_H(H, es)
+        orc.set_R(R)
+    times = {}
+    for M in Ms:
+        c = oracle_coefficients(M, es)
+        t0 = time.perf_counter()
+        orc.moments(M)
+        orc.autodiff_matrix(c, H.pattern_like(True))
+        times[M] = time.perf_counter() - t0
+    return times, orc
+
+
+def extrapolate(t_lo, M_lo, t_hi, M_hi, M):
+    """Solve time at order M from two timed orders: t = F + M c (fixed per-solve work F, c per order)."""
+    c = (t_hi - t_lo) / (M_hi - M_lo)
+    F = t_lo - M_lo * c
+    return F + M * c, F, c
+
+
+def cpu_baseline(args, wl):
+    """The oracle port on all host threads: one solve at each of the two sample orders on the full
+    workload, extrapolated to the benchmark's M."""
+    H, es, R, _ = wl
+    Ms = [int(x) for x in args.cpu_M.split(",")]
+    times, orc = cpu_solve_times(H, es, R, Ms)
+    t_full, F, cM = extrapolate(times[Ms[0]], Ms[0], times[Ms[1]], Ms[1], args.M)
     N, S = R.shape
-    return float(N) * M_sample * S / dt, dt, orc.threads
+    return {"value": float(N) * args.M * S / t_full, "unit": UNIT, "cores": orc.threads, "kind": "port",
+            "sample": "one moments(M) + autodiff_matrix solve of the full workload at M = %d (%.1f s) and M = %d "
+                      "(%.1f s) on %d threads; solve time extrapolated linearly in M to M = %d (fixed %.2f s + "
+                      "%.3f s per order): the reference CPU engine restated" % (
+                          Ms[0], times[Ms[0]], Ms[1], times[Ms[1]], orc.threads, args.M, F, cM)}
 
 
 def run_reference(args, rank, ws, dist):
+    """The reference's CPU engine (oracle port) on all host threads. Each step is one solve of the
+    full workload at the lower sample order; one solve at the higher order (before the timed
+    steps) fixes the extrapolation to M. Loads the oracle library only."""
     if rank != 0:
         return
-    H, es, R, _ = workload(args)
-    Ms = args.cpu_M
+    import fastkpm_gb300
+    Ms = [int(x) for x in args.cpu_M.split(",")]
+    wl = workload(args, coefficients=oracle_coefficients)
+    H, es, R, _ = wl
+    N, S = R.shape
+    orc = None
     for _ in range(args.warmup):
-        cpu_port_rate(args, Ms, H, es, R)
-    rates, secs = [], []
-    threads = 1
+        _, orc = cpu_solve_times(H, es, R, [Ms[0]], orc=orc)
+    t_hi, orc = cpu_solve_times(H, es, R, [Ms[1]], orc=orc)
+    secs = []
     for _ in range(args.steps):
-        r, dt, threads = cpu_port_rate(args, Ms, H, es, R)
-        rates.append(r)
-        secs.append(dt)
-    value = float(np.sum([float(R.shape[0]) * Ms * R.shape[1]] * len(secs)) / np.sum(secs))
+        t, orc = cpu_solve_times(H, es, R, [Ms[0]], orc=orc)
+        secs.append(t[Ms[0]])
+    t_lo = float(np.mean(secs))
+    t_full, F, cM = extrapolate(t_lo, Ms[0], t_hi[Ms[1]], Ms[1], args.M)
+    value = float(N) * args.M * S / t_full
+    threads = orc.threads
+    del orc
+    # one thread, on the L = cpu-L1 lattice of the same family (the reference engine is single-threaded)
+    wl1 = workload(args, coefficients=oracle_coefficients, L=args.cpu_L1)
+    H1, es1, R1, _ = wl1
+    t1, _ = cpu_solve_times(H1, es1, R1, Ms, nthreads=1)
+    t1_full, _, _ = extrapolate(t1[Ms[0]], Ms[0], t1[Ms[1]], Ms[1], args.M)
+    rate1 = float(R1.shape[0]) * args.M * R1.shape[1] / t1_full
+    sample = ("each step one moments(%d) + autodiff_matrix solve of the full cubic L=%d, S=%d workload on %d "
+              "threads (mean %.2f s); one M=%d solve (%.2f s) before the timed steps; value = N*M*S of the M=%d "
+              "solve over its time extrapolated linearly in M (fixed %.2f s + %.3f s per order)"
+              % (Ms[0], args.L, S, threads, t_lo, Ms[1], t_hi[Ms[1]], args.M, F, cM))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": float(np.mean(secs) * 1e3), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": t_lo * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "cubic L=%d spin-block KPM solve (moments + autodiff_matrix), sample M=%d"
-                       % (args.L, Ms), "N": int(R.shape[0]), "S": int(R.shape[1]), "M": Ms, "b": 2,
-                       "nnzb": int(H.n_blocks())},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "one moments(%d) + autodiff_matrix solve of the full cubic L=%d, S=%d "
-                                       "workload per step (reference CPU engine restated, %d threads)"
-                                       % (Ms, args.L, R.shape[1], threads)},
+            "config": {"workload": "cubic L=%d spin-block KPM solve (moments + autodiff_matrix), M=%d extrapolated "
+                                   "from timed M=%d and M=%d solves" % (args.L, args.M, Ms[0], Ms[1]),
+                       "N": int(N), "S": int(S), "M": args.M, "sample_M": Ms, "b": 2, "nnzb": int(H.n_blocks())},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "rate_1_thread": {"value": rate1, "unit": UNIT, "cores": 1,
+                              "sample": "cubic L=%d (N=%d), S=%d: M=%d (%.1f s) and M=%d (%.1f s) solves, extrapolated "
+                                        "to M=%d" % (args.cpu_L1, R1.shape[0], R1.shape[1], Ms[0], t1[Ms[0]], Ms[1],
+                                                     t1[Ms[1]], args.M)},
+            "product_library_loaded": fastkpm_gb300._lib._lib is not None,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -672,7 +774,7 @@ def run_square(args):
     from fastkpm_gb300 import workloads as W
     L = args.L if args.L != 64 else 1448
     S = args.S if args.S != 256 else 32
-    prec = args.precision if args.precision != "ds" else "fp32"
+    prec = args.precision or "fp32"
     M = args.M
     H, es = W.square_lattice(L, -1.0, 1.0, 7)
     R = fk.probe_uncorrelated(H.n_rows, S, fk.RNG(7))
@@ -771,6 +873,27 @@ def run_cfg1(args):
     print(json.dumps(line), flush=True)
 
 
+def _leg_summary(r, ref):
+    """JSON of one engine run; errors against the reference engine's last solve (same H, R, c, M)."""
+    d = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / r["steps"], "steps": r["steps"],
+         "warmup": r["warmup"], "dtype": {"ds": "float-float (2 x FP32, ~48-bit significand, 8-bit exponent)",
+                                          "fp32": "f32 recursion and SpMM, float-float sums, D finished in f64",
+                                          "fp64": "f64"}[r["prec"]],
+         "roofline": r["roofline"], "roofline_step": r["roofline_step"], "clocks": r["clocks"],
+         "kernels": {"step_avg_ms": r["avg_step_ms"], "step_launches": r["n_step"],
+                     "adjoint_avg_ms": r["avg_adj_ms"], "adjoint_launches": r["n_adj"],
+                     "d_epilogue_fused": r["fused"]}}
+    for k in ("roofline_issue", "roofline_fp64_pipe", "e2e", "e2e_dense_R"):
+        if k in r:
+            d[k] = r[k]
+    if ref is not None and ref is not r:
+        d["err_vs_fp64"] = {"moments_max_rel_mu0": float(np.max(np.abs(r["mu"] - ref["mu"])) / abs(ref["mu"][0])),
+                            "D_rel_fro": float(np.linalg.norm(r["D"] - ref["D"]) / np.linalg.norm(ref["D"])),
+                            "vs": "native FP64 GPU engine, same H, R and c, M=%d" % r["M"]}
+        d["speedup_vs_fp64"] = (ref["ms"] / ref["steps"]) / (r["ms"] / r["steps"])
+    return d
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init()
@@ -782,44 +905,45 @@ def main():
             {"precision": run_precision, "batch": run_batch, "serve": run_serve, "cfg1": run_cfg1,
              "square": run_square}[args.workload](args)
         return
-    r = run_gb300(args, rank, ws, dist)
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    args.precision = args.precision or "fp64"
+    wl = workload(args)
+    e2e_steps = 0 if args.no_e2e else args.e2e_steps
+    head = run_leg(args, args.precision, args.steps, args.warmup, wl, ws, dist, dev, e2e_steps)
+    legs = {}
+    for prec in [p for p in args.legs.split(",") if p and p != args.precision]:
+        k = args.leg_steps or {"ds": min(args.steps, 3), "fp32": min(args.steps, 5), "fp64": min(args.steps, 2)}[prec]
+        legs[prec] = run_leg(args, prec, k, min(args.warmup, 2), wl, ws, dist, dev, e2e_steps)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        rate, dt, threads = cpu_port_rate(args, args.cpu_M)
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "one moments(%d) + autodiff_matrix solve of the full workload (%.1f s on %d threads), "
-                         "the reference CPU engine restated" % (args.cpu_M, dt, threads)}
+        cpu = cpu_baseline(args, wl)
     if rank != 0:
         return
-    dtype = {"ds": "f64 (double-single float-float storage and arithmetic)", "fp64": "f64",
-             "fp32": "f32 recursion, f64 accumulation"}[args.precision]
+    ref = head if args.precision == "fp64" else legs.get("fp64")
+    hs = _leg_summary(head, ref)
+    H = wl[0]
     line = {
-        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "ds": "float-float", "fp32": "f32"}[args.precision],
+        "data": "synthetic",
         "config": {"workload": "cubic L=%d Kondo-lattice spin-block KPM solve: moments(M) + autodiff_matrix(c, D) "
                                "on H's pattern" % args.L,
-                   "N": r["N"], "sites": r["N"] // 2, "b": 2, "nnzb": r["nnzb"], "M": r["M"], "S": r["S"],
+                   "N": head["N"], "sites": head["N"] // 2, "b": 2, "nnzb": head["nnzb"], "M": head["M"], "S": head["S"],
                    "precision": args.precision, "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 (2 GiB per vector), no flush"},
-        "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
-                     "frac": r["achieved"] / r["peak"], "traffic": r["traffic"],
-                     "kernel": "k_adjoint_step (reverse-mode step, both recursions%s)" % (
-                         " + fused D epilogue" if r["fused"] else "; D outer product in k_outer"),
-                     "traffic_source": "ncu capture of the L=32 case scaled by rows (profiles/)" if r["traffic"] else None,
-                     "peak_source": r["peak_kind"], "bytes_per_launch": r["bytes_adj"],
-                     "avg_launch_ms": r["avg_adj_ms"], "launches": r["n_adj"]},
+        "roofline": hs["roofline"],
+        "roofline_step": hs["roofline_step"],
         "cpu_baseline": cpu,
-        "roofline_issue": r["issue"],
-        "e2e": r["e2e"],
-        "e2e_dense_R": r["e2e_dense"],
-        "gpu_launches": r["launches"],
-        "clocks": r["clocks"],
-        "err_vs_fp64": r["err"],
-        "kernels": {"step_avg_ms": r["avg_step_ms"], "step_launches": r["n_step"],
-                    "adjoint_avg_ms": r["avg_adj_ms"], "adjoint_launches": r["n_adj"],
-                    "d_epilogue_fused": r["fused"]},
+        "e2e": hs.get("e2e"),
+        "gpu_launches": head["launches"],
+        "clocks": head["clocks"],
+        "kernels": hs["kernels"],
     }
+    for k in ("roofline_fp64_pipe", "roofline_issue", "e2e_dense_R", "err_vs_fp64"):
+        if k in hs:
+            line[k] = hs[k]
+    line["legs"] = {p: _leg_summary(r, ref) for p, r in legs.items()}
     print(json.dumps(line), flush=True)
 
 

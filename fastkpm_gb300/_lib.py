@@ -35,6 +35,7 @@ SIGNATURES = {
     "fk_status_string": (C.c_char_p, [_i]),
     "fk_device_count": (_i, [_ip]),
     "fk_device_memory": (_i, [_i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "fk_device_fma_rate": (_i, [_i, _i, _dp]),
     "fk_engine_create": (_i, [_i, _i, _i, C.POINTER(_p)]),
     "fk_engine_destroy": (_i, [_p]),
     "fk_engine_last_error": (C.c_char_p, [_p]),

@@ -64,6 +64,26 @@ struct ProfEvent { int kind; cudaEvent_t a, b; };
 
 int next_pow2(int v) { int p = 1; while (p < v) p <<= 1; return p; }
 
+// FMA pipe throughput probe: kFmaChains independent multiply-add chains per thread, no memory
+// traffic; the sum is stored only when it equals an impossible value, so nothing is optimised out.
+constexpr int kFmaChains = 8;
+constexpr int kFmaThreads = 256;
+template <class T>
+__global__ void __launch_bounds__(kFmaThreads) k_fma_rate(double* sink, int iters, T seed) {
+    T v[kFmaChains];
+#pragma unroll
+    for (int q = 0; q < kFmaChains; q++) v[q] = seed + (T)(threadIdx.x + q);
+    const T mul = (T)0.9999999, add = (T)1e-7;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int q = 0; q < kFmaChains; q++) v[q] = fma(v[q], mul, add);
+    }
+    T s = 0;
+#pragma unroll
+    for (int q = 0; q < kFmaChains; q++) s += v[q];
+    if (s == (T)-1.0) *sink = (double)s;
+}
+
 }  // namespace
 
 struct fk_engine {
@@ -1290,6 +1310,46 @@ int fk_device_count(int* count) {
     if (ce != cudaSuccess) { cudaGetLastError(); *count = 0; return FK_ERR_NODEV; }
     *count = c;
     return FK_OK;
+}
+
+int fk_device_fma_rate(int device, int fp64, double* tflops) {
+    if (!tflops) return FK_ERR_ARG;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) { cudaGetLastError(); return FK_ERR_NODEV; }
+    if (device < 0 || device >= count) return FK_ERR_ARG;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    double* sink = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    int rc = FK_OK;
+    const int blocks = sms * 8;
+    const int iters = fp64 ? 2048 : 65536;
+    float ms = 0.f;
+    if (cudaMalloc(&sink, sizeof(double)) != cudaSuccess || cudaEventCreate(&a) != cudaSuccess ||
+        cudaEventCreate(&b) != cudaSuccess) {
+        rc = FK_ERR_CUDA;
+    } else {
+        for (int rep = 0; rep < 2 && rc == FK_OK; rep++) {   // the first launch warms the clocks up
+            cudaEventRecord(a);
+            if (fp64) k_fma_rate<double><<<blocks, kFmaThreads>>>(sink, iters, 1.0);
+            else k_fma_rate<float><<<blocks, kFmaThreads>>>(sink, iters, 1.0f);
+            cudaEventRecord(b);
+            if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) rc = FK_ERR_CUDA;
+        }
+    }
+    if (rc == FK_OK) {
+        const double flops = 2.0 * kFmaChains * (double)iters * kFmaThreads * (double)blocks;
+        *tflops = flops / (ms * 1e-3) / 1e12;
+    }
+    cudaGetLastError();
+    if (sink) cudaFree(sink);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaSetDevice(prev);
+    return rc;
 }
 
 int fk_device_memory(int device, size_t* free_bytes, size_t* total_bytes) {

@@ -58,6 +58,10 @@ typedef struct fk_engine fk_engine;
 const char* fk_version(void);
 const char* fk_status_string(int status);
 int fk_device_count(int* count);
+/* Measured multiply-add throughput of `device` in TFLOP/s (2 flops per FMA), FP64 (fp64 != 0) or
+ * FP32: a few milliseconds of independent FMA chains with no memory traffic, timed with CUDA
+ * events. The denominator of the FP64 engine's compute roofline. No reference counterpart. */
+int fk_device_fma_rate(int device, int fp64, double* tflops);
 /* Free and total device memory of `device` in bytes (admission control of the serving loop). */
 int fk_device_memory(int device, size_t* free_bytes, size_t* total_bytes);
 
