@@ -304,16 +304,18 @@ def run_e2e(prec, steps, wl, M, per_solve, ws, dist, dev, sparse):
 
 
 # ---------------------------------------------------------------------------- one engine, timed
-def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps):
+def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=None):
     """W untimed and K timed solves of one engine precision, device-resident; kernel times from
     CUDA events around every launch on the engine's stream; rooflines of the adjoint and step
-    kernels; the last solve's mu and D; optional end-to-end timing."""
+    kernels; the last solve's mu and D; optional end-to-end timing. options: engine options."""
     import fastkpm_gb300 as fk
     from fastkpm_gb300 import _lib as Lb
     H, es, R, c = wl
     N, S, M = R.shape[0], R.shape[1], args.M
     D = H.pattern_like(True)
     eng = fk.Engine(True, prec, device=dev)
+    for k, v in (options or {}).items():
+        eng.set_option(k, v)
     eng.set_H(H, es)
     eng.set_R(R)
     per_solve = float(N) * M * S
@@ -339,6 +341,7 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps):
     mu = eng.fetch_moments(M)
     eng.fetch_D(D)
     fused = eng.get_option(Lb.FK_OPT_FUSE_D) != 0
+    acc64 = eng.get_option(Lb.FK_OPT_ACC64)
     eng.close()
 
     n_adj, t_adj = prof[1]
@@ -356,7 +359,8 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps):
     clocks = clk.summary()
     out = dict(prec=prec, value=replica_value(per_solve, steps, ws, ms_max), ms=ms_max, steps=steps, warmup=warmup,
                clocks=clocks, launches=sum(v[0] for v in prof.values()), mu=mu, D=D.val.copy(), fused=fused,
-               N=N, S=S, M=M, nnzb=nnzb, n_adj=n_adj, n_step=n_step, avg_adj_ms=avg_adj_ms, avg_step_ms=avg_step_ms)
+               N=N, S=S, M=M, nnzb=nnzb, n_adj=n_adj, n_step=n_step, avg_adj_ms=avg_adj_ms, avg_step_ms=avg_step_ms,
+               acc64=acc64)
     out["roofline"] = {"bound": "hbm", "achieved": ach_adj, "peak": peak, "unit": "GB/s", "frac": ach_adj / peak,
                        "traffic": traffic,
                        "kernel": "fused adjoint step (both recursions%s)" % (
@@ -877,7 +881,8 @@ def _leg_summary(r, ref):
     """JSON of one engine run; errors against the reference engine's last solve (same H, R, c, M)."""
     d = {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms"] / r["steps"], "steps": r["steps"],
          "warmup": r["warmup"], "dtype": {"ds": "float-float (2 x FP32, ~48-bit significand, 8-bit exponent)",
-                                          "fp32": "f32 recursion and SpMM, float-float sums, D finished in f64",
+                                          "fp32": "f32 recursion and SpMM, %s moment sums and D accumulator" % (
+                                              "f64" if r["acc64"] else "float-float"),
                                           "fp64": "f64"}[r["prec"]],
          "roofline": r["roofline"], "roofline_step": r["roofline_step"], "clocks": r["clocks"],
          "kernels": {"step_avg_ms": r["avg_step_ms"], "step_launches": r["n_step"],
@@ -914,6 +919,11 @@ def main():
     for prec in [p for p in args.legs.split(",") if p and p != args.precision]:
         k = args.leg_steps or {"ds": min(args.steps, 3), "fp32": min(args.steps, 5), "fp64": min(args.steps, 2)}[prec]
         legs[prec] = run_leg(args, prec, k, min(args.warmup, 2), wl, ws, dist, dev, e2e_steps)
+    if args.precision == "fp32" or "fp32" in legs:
+        # the FP32 engine with float-float accumulators (FK_OPT_ACC64 = 0): the cost of its FP64 sums
+        from fastkpm_gb300 import _lib as Lb
+        legs["fp32_float_float_sums"] = run_leg(args, "fp32", min(args.steps, 3), 1, wl, ws, dist, dev, 0,
+                                                {Lb.FK_OPT_ACC64: 0})
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(args, wl)

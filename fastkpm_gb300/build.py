@@ -19,7 +19,8 @@ LIB = os.path.join(OUT, "libfastkpm_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_UNITS = ["fk_inst_f64.cu", "fk_inst_f32.cu", "fk_inst_ds.cu", "fk_engine.cu", "fk_batch.cu", "fk_noalloc.cu"]
+CUDA_UNITS = ["fk_inst_f64.cu", "fk_inst_f32.cu", "fk_inst_f32a.cu", "fk_inst_ds.cu", "fk_engine.cu", "fk_batch.cu",
+              "fk_noalloc.cu"]
 CXX_UNITS = ["fk_host.cpp"]
 HEADERS = ["fk_sys.cuh", "fk_kernels.cuh", "fk_dispatch.h", "fk_inst.cuh", "fk_prep.h", "fk_staged.cuh", "fk_post.cuh"]
 

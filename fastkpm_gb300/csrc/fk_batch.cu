@@ -114,6 +114,7 @@ struct fk_batch {
     std::vector<double> h_raw;
     bool configured = false;
     int opt_graphs = 0;
+    int acc64 = 1;   // FK_OPT_ACC64 (FP32 batches): FP64 moment sums and D accumulator
     std::map<int, cudaGraphExec_t> graphs;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
 
@@ -149,14 +150,16 @@ namespace {
 cudaError_t batch_launch_step(fk_batch* bt, const fk::StepArgs& a, const fk::Launch& l) {
     switch (bt->prec) {
         case fk::kF64: return fk::launch_step_f64(bt->cplx, bt->b, bt->NP, a, l);
-        case fk::kF32: return fk::launch_step_f32(bt->cplx, bt->b, bt->NP, a, l);
+        case fk::kF32: return bt->acc64 ? fk::launch_step_f32a(bt->cplx, bt->b, bt->NP, a, l)
+                                        : fk::launch_step_f32(bt->cplx, bt->b, bt->NP, a, l);
         default: return fk::launch_step_ds(bt->cplx, bt->b, bt->NP, a, l);
     }
 }
 cudaError_t batch_occupancy(fk_batch* bt, int NP, size_t smem, int* n) {
     switch (bt->prec) {
         case fk::kF64: return fk::occupancy_f64(fk::kStep, bt->cplx, bt->b, NP, smem, n);
-        case fk::kF32: return fk::occupancy_f32(fk::kStep, bt->cplx, bt->b, NP, smem, n);
+        case fk::kF32: return bt->acc64 ? fk::occupancy_f32a(fk::kStep, bt->cplx, bt->b, NP, smem, n)
+                                        : fk::occupancy_f32(fk::kStep, bt->cplx, bt->b, NP, smem, n);
         default: return fk::occupancy_ds(fk::kStep, bt->cplx, bt->b, NP, smem, n);
     }
 }
@@ -320,14 +323,16 @@ int batch_run_moments(fk_batch* bt, int M) {
 cudaError_t batch_launch_adjoint(fk_batch* bt, const fk::AdjArgs& a, const fk::Launch& l) {
     switch (bt->prec) {
         case fk::kF64: return fk::launch_adjoint_f64(bt->cplx, bt->b, bt->NP, a, l);
-        case fk::kF32: return fk::launch_adjoint_f32(bt->cplx, bt->b, bt->NP, a, l);
+        case fk::kF32: return bt->acc64 ? fk::launch_adjoint_f32a(bt->cplx, bt->b, bt->NP, a, l)
+                                        : fk::launch_adjoint_f32(bt->cplx, bt->b, bt->NP, a, l);
         default: return fk::launch_adjoint_ds(bt->cplx, bt->b, bt->NP, a, l);
     }
 }
 cudaError_t batch_launch_outer(fk_batch* bt, const fk::OuterArgs& a, const fk::Launch& l) {
     switch (bt->prec) {
         case fk::kF64: return fk::launch_outer_f64(bt->cplx, bt->b, bt->NP, a, l);
-        case fk::kF32: return fk::launch_outer_f32(bt->cplx, bt->b, bt->NP, a, l);
+        case fk::kF32: return bt->acc64 ? fk::launch_outer_f32a(bt->cplx, bt->b, bt->NP, a, l)
+                                        : fk::launch_outer_f32(bt->cplx, bt->b, bt->NP, a, l);
         default: return fk::launch_outer_ds(bt->cplx, bt->b, bt->NP, a, l);
     }
 }
@@ -487,7 +492,7 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
     }
     rc = outer(A, Bv, 1.0);
     if (rc != FK_OK) return rc;
-    if (bt->prec != fk::kF64) {   // float-float accumulator -> double
+    if (bt->prec == fk::kDS || (bt->prec == fk::kF32 && !bt->acc64)) {   // float-float accumulator -> double
         const int g = (int)std::max<long long>(1, std::min<long long>(((long long)dn + 255) / 256, 152LL * 16));
         fk::k_ds_to_double<<<g, 256, 0, bt->stream>>>(bt->d_D.as<double>(), (long long)dn);
         BT_TRY(cudaGetLastError(), "accumulator conversion");
@@ -718,6 +723,12 @@ int fk_batch_set_option(fk_batch* bt, int option, int value) {
         case FK_OPT_CTAS_PER_SM: bt->opt.cap_per_sm = std::max(0, value); break;
         case FK_OPT_STAGE_H: bt->opt.stage = value == 2 ? -1 : (value ? 1 : 0); break;
         case FK_OPT_FUSE_D: return FK_OK;
+        case FK_OPT_ACC64:
+            if (value < 0 || value > 1) return bt->fail(FK_ERR_ARG, "ACC64 must be 0 or 1");
+            bt->acc64 = value;
+            bt->drop_graphs();
+            // the two kernel families may differ in occupancy: rebuild the launch tables for them
+            return bt->configured ? batch_configure(bt, bt->cur) : FK_OK;
         default: return bt->fail(FK_ERR_ARG, "unknown option %d", option);
     }
     if (!bt->n_sys) return FK_OK;
@@ -736,6 +747,7 @@ int fk_batch_get_option(const fk_batch* bt, int option, int* value) {
         case FK_OPT_NP: *value = bt->NP; return FK_OK;
         case FK_OPT_CTAS_PER_SM: *value = bt->cur.cap_per_sm; return FK_OK;
         case FK_OPT_STAGE_H: *value = bt->stage_cap > 0; return FK_OK;
+        case FK_OPT_ACC64: *value = bt->prec == fk::kF64 ? 1 : bt->prec == fk::kF32 ? bt->acc64 : 0; return FK_OK;
         default: return FK_ERR_ARG;
     }
 }

@@ -48,6 +48,7 @@ inline int elems_per_packet(int prec, int cplx) { return 16 / elem_bytes(prec, c
                                          long long ld, void* dst, cudaStream_t st);
 FK_DECLARE_PREC(f64)
 FK_DECLARE_PREC(f32)
+FK_DECLARE_PREC(f32a)   // FP32 systems with FP64 accumulators (fk_inst_f32a.cu)
 FK_DECLARE_PREC(ds)
 #undef FK_DECLARE_PREC
 

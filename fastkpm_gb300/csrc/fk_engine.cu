@@ -137,6 +137,7 @@ struct fk_engine {
     int opt_upload = 0;        // FK_OPT_UPLOAD: 0 read device-readable host R directly, 1 staging copies
     int opt_adj_split = 2;     // FK_OPT_ADJ_SPLIT: 0 one pass, 1 two passes, 2 (default) by configuration
     int opt_pipe = 2;          // FK_OPT_PIPE: 0 plain step, 1 double-buffered gathers (FP32), 2 (default) by configuration
+    int opt_acc64 = 1;         // FK_OPT_ACC64 (FP32 engines): 1 FP64 moment sums and D accumulator, 0 float-float
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
@@ -198,28 +199,32 @@ namespace {
 cudaError_t prec_launch_step(fk_engine* e, int NP, const fk::StepArgs& a, const fk::Launch& l) {
     switch (e->prec) {
         case fk::kF64: return fk::launch_step_f64(e->cplx, e->b, NP, a, l);
-        case fk::kF32: return fk::launch_step_f32(e->cplx, e->b, NP, a, l);
+        case fk::kF32: return e->opt_acc64 ? fk::launch_step_f32a(e->cplx, e->b, NP, a, l)
+                                           : fk::launch_step_f32(e->cplx, e->b, NP, a, l);
         default: return fk::launch_step_ds(e->cplx, e->b, NP, a, l);
     }
 }
 cudaError_t prec_launch_adjoint(fk_engine* e, int NP, const fk::AdjArgs& a, const fk::Launch& l) {
     switch (e->prec) {
         case fk::kF64: return fk::launch_adjoint_f64(e->cplx, e->b, NP, a, l);
-        case fk::kF32: return fk::launch_adjoint_f32(e->cplx, e->b, NP, a, l);
+        case fk::kF32: return e->opt_acc64 ? fk::launch_adjoint_f32a(e->cplx, e->b, NP, a, l)
+                                           : fk::launch_adjoint_f32(e->cplx, e->b, NP, a, l);
         default: return fk::launch_adjoint_ds(e->cplx, e->b, NP, a, l);
     }
 }
 cudaError_t prec_launch_outer(fk_engine* e, int NP, const fk::OuterArgs& a, const fk::Launch& l) {
     switch (e->prec) {
         case fk::kF64: return fk::launch_outer_f64(e->cplx, e->b, NP, a, l);
-        case fk::kF32: return fk::launch_outer_f32(e->cplx, e->b, NP, a, l);
+        case fk::kF32: return e->opt_acc64 ? fk::launch_outer_f32a(e->cplx, e->b, NP, a, l)
+                                           : fk::launch_outer_f32(e->cplx, e->b, NP, a, l);
         default: return fk::launch_outer_ds(e->cplx, e->b, NP, a, l);
     }
 }
 cudaError_t prec_occupancy(fk_engine* e, int kind, int NP, size_t smem, int* n) {
     switch (e->prec) {
         case fk::kF64: return fk::occupancy_f64(kind, e->cplx, e->b, NP, smem, n);
-        case fk::kF32: return fk::occupancy_f32(kind, e->cplx, e->b, NP, smem, n);
+        case fk::kF32: return e->opt_acc64 ? fk::occupancy_f32a(kind, e->cplx, e->b, NP, smem, n)
+                                           : fk::occupancy_f32(kind, e->cplx, e->b, NP, smem, n);
         default: return fk::occupancy_ds(kind, e->cplx, e->b, NP, smem, n);
     }
 }
@@ -286,7 +291,7 @@ std::vector<long long> graph_signature(const fk_engine* e) {
                             &e->d_partials, &e->d_raw, &e->d_coef})
         addr(b->p);
     for (long long v : {(long long)e->n_b, (long long)e->b, (long long)e->nnzb, (long long)e->n, (long long)e->s, e->ld,
-                        (long long)e->P, (long long)e->d_nnzb})
+                        (long long)e->P, (long long)e->d_nnzb, (long long)e->opt_acc64})
         s.push_back(v);
     long long mag_bits;
     const double mag = (e->es_hi - e->es_lo) / 2.0;
@@ -568,7 +573,10 @@ int run_step(fk_engine* e, const void* x, const void* z, void* y, bool two, bool
             cudaError_t ce;
             switch (e->prec) {
                 case fk::kF64: ce = fk::launch_step_staged_f64(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l); break;
-                case fk::kF32: ce = fk::launch_step_staged_f32(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l); break;
+                case fk::kF32:
+                    ce = e->opt_acc64 ? fk::launch_step_staged_f32a(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l)
+                                      : fk::launch_step_staged_f32(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l);
+                    break;
                 default: ce = fk::launch_step_staged_ds(e->cplx, e->b, c.NP, e->opt_tma == 1, a, tb, l); break;
             }
             FK_TRY(ce, "staged step kernel launch");
@@ -696,9 +704,10 @@ int set_D_pattern(fk_engine* e, int d_n_b, int d_nnzb, const int* rp, const int*
     return FK_OK;
 }
 
-// FP32 and DS engines accumulate D as float-float pairs; turn them into doubles in place.
+// DS engines, and FP32 engines without FK_OPT_ACC64, accumulate D as float-float pairs; turn them
+// into doubles in place.
 int finish_D_accumulator(fk_engine* e, size_t n_reals) {
-    if (e->prec == fk::kF64 || n_reals == 0) return FK_OK;
+    if (e->prec == fk::kF64 || (e->prec == fk::kF32 && e->opt_acc64) || n_reals == 0) return FK_OK;
     const int grid = (int)std::max<long long>(1, std::min<long long>(((long long)n_reals + 255) / 256, 152LL * 16));
     ProfScope ps(e, fk::kHelper);
     fk::k_ds_to_double<<<grid, 256, 0, e->stream>>>(e->dd_acc.as<double>(), (long long)n_reals);
@@ -1485,6 +1494,11 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             e->opt_pipe = value;
             drop_graphs(e);
             return configure(e);
+        case FK_OPT_ACC64:
+            if (value < 0 || value > 1) return e->fail(FK_ERR_ARG, "ACC64 must be 0 or 1");
+            e->opt_acc64 = value;   // the kept recursion state stays valid: every D call starts its accumulator anew
+            drop_graphs(e);
+            return configure(e);
         case FK_OPT_ADJ_SPLIT:
             if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "ADJ_SPLIT must be 0, 1 or 2");
             e->opt_adj_split = value;
@@ -1531,6 +1545,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_PRIORITY: *value = e->opt_priority; return FK_OK;
         case FK_OPT_ADJ_SPLIT: *value = e->opt_adj_split; return FK_OK;
         case FK_OPT_PIPE: *value = e->cfg[fk::kStep].valid ? (int)e->cfg[fk::kStep].pipe : e->opt_pipe; return FK_OK;
+        case FK_OPT_ACC64: *value = e->prec == fk::kF64 ? 1 : e->prec == fk::kF32 ? e->opt_acc64 : 0; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }

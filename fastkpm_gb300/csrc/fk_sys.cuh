@@ -242,6 +242,26 @@ struct SysF32C {
     __device__ static double2 to_double2(E x) { return make_double2((double)x.x, (double)x.y); }
 };
 
+// FP32 storage and arithmetic with FP64 accumulators: each thread's moment sums are doubles
+// (one DADD per column chunk), and the D accumulator holds one double per real, updated by a
+// DFMA from the chunk's FP32 lane reduction. Everything else is the FP32 system's.
+struct SysF32RA : SysF32R {
+    typedef double Dot;
+    __device__ static Dot dot_zero() { return 0.0; }
+    __device__ static void dot_add(Dot& d, RowDot r) { d += (double)r; }
+    __device__ static Dot dot_shfl_add(Dot d, int off) { return d + __shfl_xor_sync(0xffffffffu, d, off); }
+    __device__ static double dot_get(Dot d) { return d; }
+    static constexpr bool DACC_DS = false;
+};
+struct SysF32CA : SysF32C {
+    typedef double Dot;
+    __device__ static Dot dot_zero() { return 0.0; }
+    __device__ static void dot_add(Dot& d, RowDot r) { d += (double)r; }
+    __device__ static Dot dot_shfl_add(Dot d, int off) { return d + __shfl_xor_sync(0xffffffffu, d, off); }
+    __device__ static double dot_get(Dot d) { return d; }
+    static constexpr bool DACC_DS = false;
+};
+
 // Double-single real: E = (hi, lo)
 struct SysDSR {
     typedef float2 E; typedef float2 H; typedef float2 Hr; typedef float2 Acc;

@@ -185,3 +185,27 @@ def test_batch_autodiff_keeps_h_pattern_without_diagonal(gpu):
         eng.autodiff_matrix(cs[k], D)
         assert np.array_equal(Ds[k].col_idx, H.col_idx)
         assert np.max(np.abs(Ds[k].val - D.val)) <= 1e-12 * max(1.0, np.max(np.abs(D.val))), k
+
+
+@pytest.mark.parametrize("acc64", [1, 0])
+def test_batch_fp32_accumulator_forms(gpu, acc64):
+    # FP64 (default) and float-float accumulators of the FP32 batch: moments and D against the oracle
+    systems = make_systems(4, 32, 17)
+    M = 40
+    bt = fk.Batch(False, "fp32")
+    for H, es, R in systems:
+        bt.add(H, es, R)
+    bt.commit()
+    bt.set_option(L.FK_OPT_ACC64, acc64)
+    assert bt.get_option(L.FK_OPT_ACC64) == acc64
+    mu = bt.moments(M)
+    cs = np.stack([W.fermi_coefficients(M, es, "fermi_energy") for _, es, _ in systems])
+    Ds = bt.autodiff_matrix(M, cs)
+    for k, (H, es, R) in enumerate(systems):
+        o = O.OracleEngine(False, nthreads=2)
+        o.set_H(H, es)
+        o.set_R(R)
+        ref = o.moments(M)
+        assert np.max(np.abs(mu[k] - ref)) / ref[0] <= 1e-5, k
+        D_ref = o.autodiff_matrix(cs[k], H.pattern_like(False))
+        assert rel_err(Ds[k].val, D_ref) <= 1e-4, k

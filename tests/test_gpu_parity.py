@@ -507,3 +507,30 @@ def test_probe_split_additivity_full_size(gpu, prec):
     assert abs(parts_mu[0][0] - np.vdot(R, R).real) / parts_mu[0][0] < 1e-12
     assert mu_err(parts_mu[1] + parts_mu[2], parts_mu[0]) < 1e-12
     assert rel_err(parts_D[1] + parts_D[2], parts_D[0]) < 1e-11
+
+
+@pytest.mark.parametrize("acc64", [1, 0])
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("kind", ["autodiff", "stoch"])
+def test_fp32_accumulator_forms_against_oracle(gpu, acc64, cplx, kind):
+    # FP32 recursion with FP64 moment sums and D accumulator (FK_OPT_ACC64 = 1, the default) and
+    # with float-float ones (0): both within the FP32 tolerances of the oracle
+    H, es, R = small_complex_case(4, 32, 41) if cplx else small_real_case(12, 32, 41)
+    M = 60
+    c = W.fermi_coefficients(M, es, "fermi_energy" if kind == "autodiff" else "fermi_density", 0.0, 0.2)
+    mu, mu_ref, D, D_ref = run_pair(H, es, R, cplx, "fp32", M, c, kind, {L.FK_OPT_ACC64: acc64})
+    assert mu_err(mu, mu_ref) <= TOL_MU["fp32"]
+    assert rel_err(D, D_ref) <= TOL_D["fp32"]
+
+
+def test_acc64_option_reads_back(gpu):
+    for prec, want in [("fp64", 1), ("ds", 0), ("fp32", 1)]:
+        eng = fk.Engine(True, prec)
+        assert eng.get_option(L.FK_OPT_ACC64) == want
+        eng.close()
+    eng = fk.Engine(False, "fp32")
+    eng.set_option(L.FK_OPT_ACC64, 0)
+    assert eng.get_option(L.FK_OPT_ACC64) == 0
+    with pytest.raises(L.FkError):
+        eng.set_option(L.FK_OPT_ACC64, 2)
+    eng.close()
