@@ -80,6 +80,7 @@ SIGNATURES = {
     "fk_batch_set_option": (_i, [_p, _i, _i]),
     "fk_batch_get_option": (_i, [_p, _i, _ip]),
     "fk_batch_autotune": (_i, [_p, _i, _ip, _ip, _ip, _ip, _dp]),
+    "fk_batch_profile_moments": (_i, [_p, _i, _dp, _ip]),
     "fk_batch_timer_start": (_i, [_p]),
     "fk_batch_timer_stop": (_i, [_p, _dp]),
     "fk_batch_info": (_i, [_p, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_size_t)]),

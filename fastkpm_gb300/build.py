@@ -22,7 +22,8 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_UNITS = ["fk_inst_f64.cu", "fk_inst_f32.cu", "fk_inst_f32a.cu", "fk_inst_ds.cu", "fk_engine.cu", "fk_batch.cu",
               "fk_noalloc.cu"]
 CXX_UNITS = ["fk_host.cpp"]
-HEADERS = ["fk_sys.cuh", "fk_kernels.cuh", "fk_dispatch.h", "fk_inst.cuh", "fk_prep.h", "fk_staged.cuh", "fk_post.cuh"]
+HEADERS = ["fk_sys.cuh", "fk_kernels.cuh", "fk_dispatch.h", "fk_inst.cuh", "fk_prep.h", "fk_staged.cuh", "fk_post.cuh",
+           "fk_gram.cuh"]
 
 
 def _nvcc():
@@ -86,7 +87,7 @@ def build(force=False, verbose=False, ptxas_verbose=False):
                         print(log)
     if force or jobs or _newer(LIB, objs):
         tmp = LIB + ".tmp"
-        _compile([nvcc] + GENCODE + ["-shared", "-o", tmp] + objs + ["-lcublas", "-lpthread"])
+        _compile([nvcc] + GENCODE + ["-shared", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB)
     return LIB
 

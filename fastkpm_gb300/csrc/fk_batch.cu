@@ -115,6 +115,7 @@ struct fk_batch {
     bool configured = false;
     int opt_graphs = 0;
     int acc64 = 1;   // FK_OPT_ACC64 (FP32 batches): FP64 moment sums and D accumulator
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* prof = nullptr;   // events around each step launch
     std::map<int, cudaGraphExec_t> graphs;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
 
@@ -288,7 +289,17 @@ int batch_enqueue_moments(fk_batch* bt, int M) {
             a.partials = part + per_step * m + (size_t)sl * bt->grid * 2;
             a.stage_cap = bt->stage_cap;
             a.pipe = 0;
+            cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+            if (bt->prof) {
+                BT_TRY(cudaEventCreate(&ev0), "profile event");
+                BT_TRY(cudaEventCreate(&ev1), "profile event");
+                BT_TRY(cudaEventRecord(ev0, bt->stream), "profile event");
+            }
             BT_TRY(batch_launch_step(bt, a, fk::Launch{bt->grid, bt->smem, bt->stream}), "batched step launch");
+            if (bt->prof) {
+                BT_TRY(cudaEventRecord(ev1, bt->stream), "profile event");
+                bt->prof->push_back({ev0, ev1});
+            }
         }
     }
     const int warps = nsteps * bt->n_sys;
@@ -801,6 +812,34 @@ int fk_batch_autotune(fk_batch* bt, int trial_steps, int* lanes, int* np_out, in
     if (cap_out) *cap_out = best.cap_per_sm;
     if (stage_out) *stage_out = best.stage;
     if (ms_out) *ms_out = best_ms;
+    return FK_OK;
+}
+
+int fk_batch_profile_moments(fk_batch* bt, int M, double* kernel_ms, int* launches) {
+    if (!bt || !kernel_ms || !launches) return FK_ERR_ARG;
+    if (!bt->configured) return bt->fail(FK_ERR_STATE, "batch_profile_moments: commit the batch first");
+    if (M < 2 || M % 2 != 0) return bt->fail(FK_ERR_ARG, "M must be even and >= 2");
+    cudaSetDevice(bt->device);
+    int rc = batch_ensure_partials(bt, M / 2);
+    if (rc != FK_OK) return rc;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    bt->prof = &ev;
+    rc = batch_enqueue_moments(bt, M);
+    bt->prof = nullptr;
+    double total = 0.0;
+    cudaError_t ce = cudaStreamSynchronize(bt->stream);
+    for (auto& p : ev) {
+        float f = 0.f;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&f, p.first, p.second);
+        total += f;
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    if (rc != FK_OK) return rc;
+    if (ce != cudaSuccess) return bt->cuda_fail(ce, "batch_profile_moments");
+    bt->mom_M = M;
+    *kernel_ms = total;
+    *launches = (int)ev.size();
     return FK_OK;
 }
 

@@ -9,7 +9,6 @@
 //   vectors rotate. stoch_matrix: two rotating vectors plus xi. autodiff: the
 //   two moment vectors (alpha) plus two beta vectors, all updated in place by
 //   the fused adjoint kernel. No allocation happens inside any recursion.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,6 +23,7 @@
 
 #include "../../include/fastkpm_gb300.h"
 #include "fk_dispatch.h"
+#include "fk_gram.cuh"
 #include "fk_post.cuh"
 #include "fk_prep.h"
 
@@ -143,11 +143,11 @@ struct fk_engine {
     int post_M = 0, post_Mq = 0;
 
     // second-order moments (moments2_v1): operators j1, j2 in the engine's format, the two
-    // double panels of Chebyshev vectors, a scratch vector, the M x M result; cuBLAS reduces
+    // double panels of Chebyshev vectors, a scratch vector, the M x M result, and the split
+    // partial tiles of the FP64 products (fk_gram.cuh) that reduce the panels
     struct Op { DevBuf row_ptr, colc, hval; };
     Op d_j[2];
-    DevBuf d_panel[2], d_tmp, d_mu2, d_R2;
-    cublasHandle_t blas = nullptr;
+    DevBuf d_panel[2], d_tmp, d_mu2, d_R2, d_gram;
     std::vector<double> h_raw;
 
     KCfg cfg[fk::kNumKinds];
@@ -1057,8 +1057,36 @@ int m2_step(fk_engine* e, const M2Mat& A, const void* x, const void* z, void* y,
     return FK_OK;
 }
 
-int blas_fail(fk_engine* e, cublasStatus_t st, const char* what) {
-    return e->fail(st == CUBLAS_STATUS_ALLOC_FAILED ? FK_ERR_OOM : FK_ERR_CUDA, "%s: cuBLAS status %d", what, (int)st);
+// C[i + j ldc] = (accumulate ? C : 0) + sum_k opA(i, k) opB(k, j) in FP64 on the engine's stream
+// (fk_gram.cuh): opA(i, k) = A[i a_si + k a_sk] (conjugated when conj_a), opB(k, j) = B[k b_sk +
+// j b_sj] (conjugated when conj_b). The contraction is split over enough CTAs to fill the GPU.
+int gram(fk_engine* e, int m, int n, long long kdim, const double* A, long long a_si, long long a_sk, bool conj_a,
+         const double* B, long long b_sk, long long b_sj, bool conj_b, double* C, long long ldc, bool accumulate,
+         const char* what) {
+    const size_t elt = e->cplx ? 16 : 8;
+    const long long tiles = (long long)((m + fk::kGramTile - 1) / fk::kGramTile) * ((n + fk::kGramTile - 1) / fk::kGramTile);
+    const long long want = std::max<long long>(1, (4LL * e->num_sms + tiles - 1) / tiles);   // ~4 CTAs per SM
+    long long splits = std::min<long long>(want, std::max<long long>(1, kdim / (4 * fk::kGramDepth)));
+    // keep the workspace of partial tiles within 256 MB
+    const long long cap = std::max<long long>(1, (256LL << 20) / std::max<long long>(1, (long long)m * n * (long long)elt));
+    splits = std::max<long long>(1, std::min<long long>({splits, cap, 65535LL}));
+    long long per = (kdim + splits - 1) / splits;
+    per = (per + fk::kGramDepth - 1) / fk::kGramDepth * fk::kGramDepth;
+    splits = std::max<long long>(1, (kdim + per - 1) / per);
+    FK_TRY(e->d_gram.ensure((size_t)splits * m * n * elt), "alloc product workspace");
+    fk::GramArgs g{m, n, kdim, per, A, a_si, a_sk, conj_a ? 1 : 0, B, b_sk, b_sj, conj_b ? 1 : 0, e->d_gram.as<double>()};
+    const dim3 grid((m + fk::kGramTile - 1) / fk::kGramTile, (n + fk::kGramTile - 1) / fk::kGramTile, (unsigned)splits);
+    const int rg = (int)std::max<long long>(1, std::min<long long>(((long long)m * n + 255) / 256, 152LL * 8));
+    ProfScope ps(e, fk::kHelper);
+    if (e->cplx) {
+        fk::k_gram_partial<true><<<grid, fk::kGramThreads, 0, e->stream>>>(g);
+        fk::k_gram_reduce<true><<<rg, 256, 0, e->stream>>>(e->d_gram.as<double>(), (int)splits, m, n, C, ldc, accumulate);
+    } else {
+        fk::k_gram_partial<false><<<grid, fk::kGramThreads, 0, e->stream>>>(g);
+        fk::k_gram_reduce<false><<<rg, 256, 0, e->stream>>>(e->d_gram.as<double>(), (int)splits, m, n, C, ldc, accumulate);
+    }
+    FK_TRY(cudaGetLastError(), what);
+    return FK_OK;
 }
 
 // Upload operator q (j1 or j2) in the engine's format: H's block rows, unscaled (energy scale
@@ -1121,12 +1149,6 @@ int moments2_v1(fk_engine* e, int M, const int* nnzb, const int* const* rp, cons
     FK_TRY(e->d_tmp.ensure(e->vec_bytes()), "alloc scratch vector");
     FK_TRY(e->d_mu2.ensure((size_t)M * M * elt), "alloc moments");
     FK_TRY(cudaMemsetAsync(e->d_mu2.p, 0, (size_t)M * M * elt, e->stream), "clear moments");
-    if (!e->blas) {
-        const cublasStatus_t st = cublasCreate(&e->blas);
-        if (st != CUBLAS_STATUS_SUCCESS) { e->blas = nullptr; return blas_fail(e, st, "cublasCreate"); }
-    }
-    cublasStatus_t bst = cublasSetStream(e->blas, e->stream);
-    if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "cublasSetStream");
     const M2Mat hs{e->d_row_ptr.as<int>(), e->d_colc.as<unsigned>(), e->d_hval.p};
     const M2Mat j1{e->d_j[0].row_ptr.as<int>(), e->d_j[0].colc.as<unsigned>(), e->d_j[0].hval.p};
     const M2Mat j2{e->d_j[1].row_ptr.as<int>(), e->d_j[1].colc.as<unsigned>(), e->d_j[1].hval.p};
@@ -1177,20 +1199,12 @@ int moments2_v1(fk_engine* e, int M, const int* nnzb, const int* const* rp, cons
                     FK_TRY(prec_export(e, e->d_tmp.p, c0, w, reinterpret_cast<double*>(PB + (size_t)q * L * elt)),
                            "export panel");
                 }
-                // mu[a0 .. a0+Ka, b0 .. b0+Kb] += A^H B   (mu column-major M x M on the device)
-                if (e->cplx) {
-                    const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0);
-                    bst = cublasZgemm(e->blas, CUBLAS_OP_C, CUBLAS_OP_N, Ka, Kb, (int)L, &one,
-                                      reinterpret_cast<const cuDoubleComplex*>(PA), (int)L,
-                                      reinterpret_cast<const cuDoubleComplex*>(PB), (int)L, &one,
-                                      e->d_mu2.as<cuDoubleComplex>() + a0 + (size_t)b0 * M, M);
-                } else {
-                    const double one = 1.0;
-                    bst = cublasDgemm(e->blas, CUBLAS_OP_T, CUBLAS_OP_N, Ka, Kb, (int)L, &one, reinterpret_cast<const double*>(PA),
-                                      (int)L, reinterpret_cast<const double*>(PB), (int)L, &one,
-                                      e->d_mu2.as<double>() + a0 + (size_t)b0 * M, M);
-                }
-                if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "moments2 GEMM");
+                // mu[a0 .. a0+Ka, b0 .. b0+Kb] += A^H B   (mu column-major M x M on the device):
+                // mu[a, b] += sum_l conj(PA[l + a L]) PB[l + b L]
+                rc = gram(e, Ka, Kb, L, reinterpret_cast<const double*>(PA), L, 1, true,
+                          reinterpret_cast<const double*>(PB), 1, L, false,
+                          e->d_mu2.as<double>() + (a0 + (size_t)b0 * M) * (elt / 8), M, true, "moments2 product");
+                if (rc != FK_OK) return rc;
             }
         }
     }
@@ -1417,7 +1431,6 @@ int fk_engine_destroy(fk_engine* e) {
         cudaStreamDestroy(e->copy_stream);
         for (int q = 0; q < 2; q++) { cudaEventDestroy(e->ev_copied[q]); cudaEventDestroy(e->ev_consumed[q]); }
     }
-    if (e->blas) cublasDestroy(e->blas);
     for (auto& op : e->d_j) { op.row_ptr.release(); op.colc.release(); op.hval.release(); }
     for (auto& pb : e->d_panel) pb.release();
     e->d_tmp.release();
@@ -1804,12 +1817,6 @@ int moments2_v2(fk_engine* e, int M, const int* nnzb, const int* const* rp, cons
     char* Ep = At + (size_t)M * ld2 * elt;
     FK_TRY(prec_export(e, e->d_R.p, 0, (int)ld, Rp), "export R");
     FK_TRY(prec_export(e, R2, 0, (int)ld, R2p), "export R2");
-    if (!e->blas) {
-        const cublasStatus_t st = cublasCreate(&e->blas);
-        if (st != CUBLAS_STATUS_SUCCESS) { e->blas = nullptr; return blas_fail(e, st, "cublasCreate"); }
-    }
-    cublasStatus_t bst = cublasSetStream(e->blas, e->stream);
-    if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "cublasSetStream");
     const M2Mat hs{e->d_row_ptr.as<int>(), e->d_colc.as<unsigned>(), e->d_hval.p};
     const M2Mat j1{e->d_j[0].row_ptr.as<int>(), e->d_j[0].colc.as<unsigned>(), e->d_j[0].hval.p};
     const M2Mat j2{e->d_j[1].row_ptr.as<int>(), e->d_j[1].colc.as<unsigned>(), e->d_j[1].hval.p};
@@ -1829,33 +1836,17 @@ int moments2_v2(fk_engine* e, int M, const int* nnzb, const int* const* rp, cons
             cur = y;
             FK_TRY(prec_export(e, cur, 0, n_ld, Xp), "export panel");
             char* dst = (side == 0 ? At : Ep) + (size_t)m * ld2 * elt;
-            // panels are column-major ld x n (leading dimension ld)
-            if (e->cplx) {
-                const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-                const cuDoubleComplex* a = reinterpret_cast<const cuDoubleComplex*>(side == 0 ? Xp : R2p);
-                const cuDoubleComplex* b = reinterpret_cast<const cuDoubleComplex*>(side == 0 ? Rp : Xp);
-                bst = cublasZgemm(e->blas, CUBLAS_OP_N, CUBLAS_OP_C, n_ld, n_ld, e->n, &one, a, n_ld, b, n_ld, &zero,
-                                  reinterpret_cast<cuDoubleComplex*>(dst), n_ld);
-            } else {
-                const double one = 1.0, zero = 0.0;
-                bst = cublasDgemm(e->blas, CUBLAS_OP_N, CUBLAS_OP_T, n_ld, n_ld, e->n, &one, side == 0 ? Xp : R2p, n_ld,
-                                  side == 0 ? Rp : Xp, n_ld, &zero, reinterpret_cast<double*>(dst), n_ld);
-            }
-            if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "moments2_v2 projection");
+            // panels are column-major ld x n (leading dimension ld):
+            // dst[p + q ld] = sum_i a[p + i ld] conj(b[q + i ld])
+            rc = gram(e, n_ld, n_ld, e->n, side == 0 ? Xp : R2p, 1, ld, false, side == 0 ? Rp : Xp, ld, 1, true,
+                      reinterpret_cast<double*>(dst), ld, false, "moments2_v2 projection");
+            if (rc != FK_OK) return rc;
         }
     }
     // mu^T (column-major M x M) = mu row-major: (E^H At)(m2, m1) = sum_q conj(E[q, m2]) At[q, m1]
-    if (e->cplx) {
-        const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-        bst = cublasZgemm(e->blas, CUBLAS_OP_C, CUBLAS_OP_N, M, M, (int)ld2, &one, reinterpret_cast<const cuDoubleComplex*>(Ep),
-                          (int)ld2, reinterpret_cast<const cuDoubleComplex*>(At), (int)ld2, &zero,
-                          e->d_mu2.as<cuDoubleComplex>(), M);
-    } else {
-        const double one = 1.0, zero = 0.0;
-        bst = cublasDgemm(e->blas, CUBLAS_OP_T, CUBLAS_OP_N, M, M, (int)ld2, &one, reinterpret_cast<const double*>(Ep),
-                          (int)ld2, reinterpret_cast<const double*>(At), (int)ld2, &zero, e->d_mu2.as<double>(), M);
-    }
-    if (bst != CUBLAS_STATUS_SUCCESS) return blas_fail(e, bst, "moments2_v2 trace GEMM");
+    rc = gram(e, M, M, ld2, reinterpret_cast<const double*>(Ep), ld2, 1, true, reinterpret_cast<const double*>(At), 1, ld2,
+              false, e->d_mu2.as<double>(), M, false, "moments2_v2 trace product");
+    if (rc != FK_OK) return rc;
     std::vector<double> h((size_t)M * M * (e->cplx ? 2 : 1));
     FK_TRY(cudaMemcpyAsync(h.data(), e->d_mu2.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream),
            "copy moments");

@@ -576,6 +576,13 @@ class Batch:
         return dict(lanes_per_row=g.value, packets_per_lane=npk.value, ctas_per_sm=cap.value, stage_h=st.value,
                     ms_per_step=ms.value)
 
+    def profile_moments(self, M):
+        """moments(M) once with direct launches, each step launch timed by CUDA events on the batch's
+        stream: (sum of the launch times in ms, number of launches)."""
+        ms, n = C.c_double(0), C.c_int(0)
+        self._check(self.lib.fk_batch_profile_moments(self.h, M, C.byref(ms), C.byref(n)), "batch_profile_moments")
+        return ms.value, n.value
+
     def timer_start(self):
         self._check(self.lib.fk_batch_timer_start(self.h), "batch_timer_start")
 

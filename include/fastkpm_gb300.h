@@ -165,7 +165,8 @@ int  fk_engine_expansion_coefficients(fk_engine* e, int M, int Mq, int f_kind, d
  * mu[m1][m2] = sum_k <T_m1(Hs) r_k, j2 T_m2(Hs) j1 r_k> ~ tr(j1 T_m1(Hs) j2 T_m2(Hs)) over the
  * probe columns r_k of R. j1, j2: BSR operators with H's block rows and block size (values as
  * for set_H, not scaled). mu[2*(m1*M + m2) + {0,1}] = (re, im), M even. Chebyshev vectors in
- * the engine's precision, reduction in FP64 (cuBLAS GEMMs over double panels).
+ * the engine's precision, reduction in FP64 over double panels (this library's split-contraction
+ * product kernels).
  * R_chunk_ncols > 0: probe columns per pass (default all); a_chunk_ncols >= 3: Chebyshev orders
  * per panel (default: as many as fit 60% of free device memory). Overwrites the recursion state
  * that moments() leaves for autodiff_matrix(). */
@@ -177,7 +178,8 @@ int  fk_engine_moments2_v1(fk_engine* e, int M, int j1_nnzb, const int* j1_row_p
  * engine exits there, src/engine_cusparse.cpp:904-908): with a second probe block R2 (column-
  * major n x s like R; NULL: R2 = R), A_i = R^dag T_i(Hs) j2 R2 and B_i = R2^dag T_i(Hs) j1 R,
  * mu[m1][m2] = tr(A_m1 B_m2); mu[2*(m1*M + m2) + {0,1}] = (re, im). Projections and the
- * trace are FP64 GEMMs (cuBLAS); holds 2 M ld^2 projected values on the device. Overwrites
+ * trace are FP64 products in this library's kernels; holds 2 M ld^2 projected values on the
+ * device. Overwrites
  * the recursion state that moments() leaves for autodiff_matrix(). */
 int  fk_engine_moments2_v2(fk_engine* e, int M, int j1_nnzb, const int* j1_row_ptr, const int* j1_col_idx,
                            const double* j1_val, int j2_nnzb, const int* j2_row_ptr, const int* j2_col_idx,
@@ -246,6 +248,11 @@ int  fk_batch_get_option(const fk_batch* bt, int option, int* value);
  * shape for later batches in this process). Returns the chosen mapping and its step time. */
 int  fk_batch_autotune(fk_batch* bt, int trial_steps, int* lanes_per_row, int* packets_per_lane,
                        int* ctas_per_sm, int* stage_h, double* ms_per_step);
+/* moments(M) of the batch once with direct launches, each step launch bracketed by CUDA events on
+ * the batch's stream: *kernel_ms = the sum of the launch times, *launches = their number. Set
+ * against the time of the same moments(M) replayed from a CUDA graph, it gives the share of the
+ * graph's time spent between kernels. Leaves the moments state like fk_batch_moments. */
+int  fk_batch_profile_moments(fk_batch* bt, int M, double* kernel_ms, int* launches);
 int  fk_batch_timer_start(fk_batch* bt);
 int  fk_batch_timer_stop(fk_batch* bt, double* ms);
 int  fk_batch_info(const fk_batch* bt, int* n_systems, long long* total_rows, size_t* device_bytes);

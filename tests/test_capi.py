@@ -73,3 +73,13 @@ int main() {
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.strip() in ("gpu", "nogpu")
+
+
+def test_library_uses_no_blas(built_lib):
+    # every product on the path, the second-order moments' FP64 products included, is a kernel of
+    # this library: the shared object links no BLAS and references no BLAS symbol
+    from fastkpm_gb300 import _lib
+    deps = subprocess.run(["ldd", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "cublas" not in deps.lower()
+    syms = subprocess.run(["nm", "-D", "--undefined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "cublas" not in syms.lower()

@@ -209,3 +209,19 @@ def test_batch_fp32_accumulator_forms(gpu, acc64):
         assert np.max(np.abs(mu[k] - ref)) / ref[0] <= 1e-5, k
         D_ref = o.autodiff_matrix(cs[k], H.pattern_like(False))
         assert rel_err(Ds[k].val, D_ref) <= 1e-4, k
+
+
+def test_batch_profile_moments(gpu):
+    # the per-launch timing run gives the same moments as the plain and graph-replayed runs
+    systems = make_systems(4, 32, 23)
+    M = 30
+    bt = fk.Batch(False, "fp32")
+    for H, es, R in systems:
+        bt.add(H, es, R)
+    bt.commit()
+    a = bt.moments(M)
+    ms, n = bt.profile_moments(M)
+    assert n == M // 2 and ms > 0
+    bt.set_option(L.FK_OPT_GRAPHS, 1)
+    b = bt.moments(M)
+    assert np.array_equal(a, b)
