@@ -6,9 +6,11 @@
 #include <complex>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <type_traits>
 
 #include "../../include/fastkpm.h"
@@ -580,15 +582,120 @@ public:
     }
 };
 
+// Probe columns split over several devices (the reference's Engine_Threaded,
+// src/engine_cusparse.cpp:1043-1168): every worker engine holds H and a contiguous slice of
+// R's columns; moments and D are sums over probe columns, so the workers' results are added
+// on the host in worker order (deterministic). set_R_* fill this engine's R exactly as one
+// engine would (one draw of the master generator per column, the same columns the
+// reference's per-worker generators produce), and transfer_R hands each worker its slice.
+// Solves are enqueued on every worker's stream first and collected afterwards, so the
+// devices run concurrently without a host thread per device; set_H, whose host preparation
+// is the heavy part, runs one thread per worker. moments2_v2 couples all probe columns
+// (traces over s x s products) and is not split: more than one worker throws.
+template <typename T>
+class Engine_Split : public Engine<T> {
+    std::vector<std::shared_ptr<Engine_GB300<T>>> w_;
+    std::vector<int> active_;   // workers that hold at least one probe column
+    std::vector<double> buf_;
+
+    static void check(fk_engine* e, int rc, const char* what) { if (rc != FK_OK) raise(e, rc, what); }
+    template <class F>
+    void parallel(F&& fn) {
+        std::vector<std::thread> ts;
+        std::vector<std::exception_ptr> errs(w_.size());
+        for (size_t t = 0; t < w_.size(); t++)
+            ts.emplace_back([&, t] { try { fn(t); } catch (...) { errs[t] = std::current_exception(); } });
+        for (auto& th : ts) th.join();
+        for (auto& e : errs) if (e) std::rethrow_exception(e);
+    }
+    template <class Enqueue>
+    void d_sum(SpMatBsr<T>& D, Enqueue&& enqueue, const char* what) {
+        if (active_.empty()) throw std::logic_error(std::string(what) + ": no probe block (call set_R_* first)");
+        for (int t : active_) enqueue(w_[t]->handle());
+        const size_t nv = D.val.size() * (is_cx<T>() ? 2 : 1);
+        std::vector<double> acc(nv, 0.0), part(nv);
+        for (int t : active_) {
+            check(w_[t]->handle(), fk_engine_fetch_D(w_[t]->handle(), part.data()), what);
+            for (size_t q = 0; q < nv; q++) acc[q] += part[q];
+        }
+        from_doubles(acc.data(), D.val.size(), D.val.data());
+    }
+
+public:
+    Engine_Split(const Vec<int>& devices, Precision p) {
+        for (int d : devices) w_.push_back(std::make_shared<Engine_GB300<T>>(d, p));
+    }
+    int workers() const { return (int)w_.size(); }
+
+    EnergyScale energy_scale(SpMatBsr<T> const& H, double extend, int iters) override {
+        return w_[0]->energy_scale(H, extend, iters);
+    }
+    void transfer_R() override {
+        if (this->R.n_cols == 0) throw std::invalid_argument("transfer_R: cannot handle an empty R matrix");
+        const int s = this->R.n_cols, n = this->R.n_rows, nw = (int)w_.size();
+        active_.clear();
+        for (int t = 0; t < nw; t++) {
+            const int j1 = t * s / nw, j2 = (t + 1) * s / nw;   // the reference's contiguous column ranges
+            if (j2 == j1) continue;
+            Mat<T>& Rt = w_[t]->R;
+            Rt.set_size(n, j2 - j1);
+            std::copy(this->R.colptr(j1), this->R.colptr(j1) + (size_t)n * (j2 - j1), Rt.memptr());
+            w_[t]->transfer_R();
+            active_.push_back(t);
+        }
+    }
+    void set_H(SpMatBsr<T> const& H, EnergyScale const& es) override {
+        parallel([&](size_t t) { w_[t]->set_H(H, es); });
+    }
+    Vec<double> moments(int M) override {
+        if (active_.empty()) throw std::logic_error("moments: no probe block (call set_R_* first)");
+        for (int t : active_) check(w_[t]->handle(), fk_engine_moments_async(w_[t]->handle(), M), "moments");
+        Vec<double> mu(M, 0.0), part(M);
+        for (int t : active_) {
+            check(w_[t]->handle(), fk_engine_fetch_moments(w_[t]->handle(), part.data()), "moments");
+            for (int m = 0; m < M; m++) mu[m] += part[m];
+        }
+        return mu;
+    }
+    Vec<Vec<cx_double>> moments2_v1(int M, SpMatBsr<T> const& j1op, SpMatBsr<T> const& j2op, int a_chunk_ncols,
+                                    int R_chunk_ncols) override {
+        Vec<Vec<cx_double>> mu(M, Vec<cx_double>(M, cx_double(0.0, 0.0)));
+        for (int t : active_) {
+            auto part = w_[t]->moments2_v1(M, j1op, j2op, a_chunk_ncols, R_chunk_ncols);
+            for (int m1 = 0; m1 < M; m1++)
+                for (int m2 = 0; m2 < M; m2++) mu[m1][m2] += part[m1][m2];
+        }
+        return mu;
+    }
+    Vec<Vec<cx_double>> moments2_v2(int M, SpMatBsr<T> const& j1op, SpMatBsr<T> const& j2op, int a, int r) override {
+        if (w_.size() > 1)
+            throw std::logic_error("moments2_v2 couples all probe columns and is not split over devices: use one device");
+        w_[0]->R2 = this->R2;
+        return w_[0]->moments2_v2(M, j1op, j2op, a, r);
+    }
+    void stoch_matrix(Vec<double> const& c, SpMatBsr<T>& D) override {
+        d_sum(D, [&](fk_engine* e) {
+            check(e, fk_engine_stoch_matrix_async(e, (int)c.size(), c.data(), D.n_rows, D.n_blocks(), D.row_ptr.data(),
+                                                  D.col_idx.data()), "stoch_matrix");
+        }, "stoch_matrix");
+    }
+    void autodiff_matrix(Vec<double> const& c, SpMatBsr<T>& D) override {
+        d_sum(D, [&](fk_engine* e) {
+            check(e, fk_engine_autodiff_matrix_async(e, (int)c.size(), c.data(), D.n_rows, D.n_blocks(),
+                                                     D.row_ptr.data(), D.col_idx.data()), "autodiff_matrix");
+        }, "autodiff_matrix");
+    }
+};
+
 template <typename T>
 std::shared_ptr<Engine<T>> mk_engine_gb300(int device, Precision precision) {
     return std::make_shared<Engine_GB300<T>>(device, precision);
 }
 template <typename T>
 std::shared_ptr<Engine<T>> mk_engine_cuSPARSE(Vec<int> devices) {
-    const int d = devices.empty() ? 0 : devices[0];
     const bool single = std::is_same<T, float>::value || std::is_same<T, cx_float>::value;
-    return mk_engine_gb300<T>(d, default_precision(single));
+    if (devices.size() > 1) return std::make_shared<Engine_Split<T>>(devices, default_precision(single));
+    return mk_engine_gb300<T>(devices.empty() ? 0 : devices[0], default_precision(single));
 }
 template <typename T>
 std::shared_ptr<Engine<T>> mk_engine() {

@@ -13,7 +13,10 @@
 //     no CUDA device is usable; it never falls back to a CPU engine.
 //     mk_engine_cpu<T>() and mk_engine_mpi<T>() throw: neither is part of this
 //     build. mk_engine_cuSPARSE<T>(devices) returns the GB300 engine on
-//     devices[0] (device 0 when empty).
+//     devices[0] (device 0 when empty); with two or more entries it splits the
+//     probe columns over one engine per listed device, like the reference's
+//     threaded engine, and sums moments and D on the host in device order
+//     (moments2_v2 is not split: it throws with more than one device).
 //   * moments2_v1 and moments2_v2 run on the GPU (the reference's GPU engine exits
 //     in moments2_v2); moments2_v2 takes R2 = R when R2 is empty.
 //   * Errors throw std::runtime_error instead of assert/abort/exit.
