@@ -71,8 +71,15 @@ def parse():
     p.add_argument("--cpu-M", default="8,16", help="orders of the two CPU sample solves (extrapolated in M)")
     p.add_argument("--cpu-L1", type=int, default=32, help="lattice of the one-thread CPU sample (reference arm)")
     p.add_argument("--workload", default="solve", choices=["solve", "precision", "batch", "serve", "cfg1", "square"])
+    p.add_argument("--batch-systems", type=int, default=64, help="systems of the batch workload")
+    p.add_argument("--batch-M", type=int, default=500, help="Chebyshev order of the batch workload")
+    p.add_argument("--batch-only", action="store_true", help="batch workload: batched moments only (no FP64 "
+                   "comparison, no full solve); a short run to profile the batched step kernel")
     p.add_argument("--serve-requests", type=int, default=24)
     p.add_argument("--serve-max-sites", type=float, default=1e6)
+    p.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrival rate of the request stream (1/s)")
+    p.add_argument("--serve-pack-bytes", type=float, default=256 << 20,
+                   help="footprint bound of requests that share batched launches (0: no packing)")
     return p.parse_args()
 
 
@@ -564,8 +571,8 @@ def run_batch(args):
     import fastkpm_gb300 as fk
     from fastkpm_gb300 import _lib as Lb
     from fastkpm_gb300 import workloads as W
-    systems = W.config4()
-    M = 500
+    systems = W.config4(n_systems=args.batch_systems)
+    M = args.batch_M
     Rs = [fk.probe_uncorrelated(s["H"].n_rows, s["S"], fk.RNG(s["probe_seed"])) for s in systems]
     total_rows = sum(s["H"].n_rows for s in systems)
     S = systems[0]["S"]
@@ -573,6 +580,18 @@ def run_batch(args):
     for s, R in zip(systems, Rs):
         bt.add(s["H"], s["es"], R)
     bt.commit()
+    if args.batch_only:
+        # the batched step in both accumulator forms (FK_OPT_ACC64 0 then 1), fixed mapping, direct launches
+        for acc in (0, 1):
+            bt.set_option(Lb.FK_OPT_ACC64, acc)
+            for _ in range(max(args.warmup, 1)):
+                bt.moments(M)
+            bt.timer_start()
+            for _ in range(args.steps):
+                bt.moments(M)
+            print(json.dumps({"workload": "batch moments only", "acc64": acc, "ms": bt.timer_stop() / args.steps}),
+                  flush=True)
+        return
     tune = bt.autotune(8)
     bt.set_option(Lb.FK_OPT_GRAPHS, 1)
     for _ in range(max(args.warmup, 1)):
@@ -589,6 +608,15 @@ def run_batch(args):
             "gap_fraction": max(0.0, 1.0 - kern_ms / ms_b),
             "how": "sum of per-launch CUDA-event times of moments(M) with direct launches vs the CUDA-graph "
                    "replay time of the same moments(M)"}
+    # the same batch with FP64 per-thread moment sums (FK_OPT_ACC64 = 1; the batch default is 0)
+    bt.set_option(Lb.FK_OPT_ACC64, 1)
+    for _ in range(max(args.warmup, 1)):
+        mu_a = bt.moments(M)
+    bt.timer_start()
+    for _ in range(args.steps):
+        mu_a = bt.moments(M)
+    acc64_line = {"ms": bt.timer_stop() / args.steps, "what": "batched moments with FP64 per-thread sums (FK_OPT_ACC64 1)"}
+    bt.set_option(Lb.FK_OPT_ACC64, 0)
     # sequential plain FP64 solves (moments only, the batched output)
     eng = fk.Engine(False, "fp64")
     t_seq = 0.0
@@ -601,6 +629,8 @@ def run_batch(args):
         mu = eng.moments(M)
         t_seq += eng.timer_stop()
         err = max(err, _mu_err(mu_b[k], mu))
+        acc64_line["moments_max_rel_mu0_vs_fp64"] = max(acc64_line.get("moments_max_rel_mu0_vs_fp64", 0.0),
+                                                        _mu_err(mu_a[k], mu))
     # full solve (moments + autodiff_matrix with each system's own Fermi-energy coefficients):
     # batched FP32 vs sequential plain FP64, wall clock around the synchronous calls
     cs = np.stack([W.fermi_coefficients(M, s["es"], "fermi_energy") for s in systems])
@@ -641,28 +671,29 @@ def run_batch(args):
     peak, kind = peaks()
     line = {"metric": METRIC, "value": per / (ms_b / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 recursion, f64 accumulation", "data": "synthetic",
-            "config": {"workload": "64 square lattices L~U{32..256}, W~U[0,4], b=1 real, M=500, S=32: "
-                                   "batched moments, CUDA graph, autotuned", "total_rows": total_rows, "M": M, "S": S,
+            "vs_baseline": None, "dtype": "f32 recursion; float-float per-thread sums, f64 across CTAs (FK_OPT_ACC64 0)",
+            "data": "synthetic",
+            "config": {"workload": "%d square lattices L~U{32..256}, W~U[0,4], b=1 real, M=%d, S=%d: batched moments, "
+                                   "CUDA graph, autotuned" % (len(systems), M, S), "total_rows": total_rows, "M": M, "S": S,
                        "systems": len(systems)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "kernel": "k_cheb_step (batched)", "peak_source": kind},
             "sequential_fp64_ms": t_seq, "speedup_vs_sequential_fp64": t_seq / ms_b,
-            "moments_max_rel_mu0_vs_fp64": err, "solve": solve, "autotune": tune, "graph_gaps": gaps,
+            "moments_max_rel_mu0_vs_fp64": err, "solve": solve, "autotune": tune, "graph_gaps": gaps, "acc64": acc64_line,
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
 
-def serve_requests(n_req, seed, max_sites):
+def serve_requests(n_req, seed, max_sites, rate=4.0):
     """Mixed-size KPM solve requests: cubic or square lattice (50/50), sites log-uniform over
     10^3 .. max_sites, b=1 real or b=2 complex spin-exchange (50/50), M in {200,500,1000,2000},
-    S in {32,64,128} by colour probing; Poisson arrival offsets (rate 4/s)."""
+    S in {32,64,128} by colour probing; Poisson arrival offsets (`rate` per second)."""
     from fastkpm_gb300 import workloads as W
     rng = np.random.default_rng(seed)
     reqs = []
     t = 0.0
     for k in range(n_req):
-        t += rng.exponential(0.25)
+        t += rng.exponential(1.0 / rate)
         cubic = rng.random() < 0.5
         spin = rng.random() < 0.5
         sites = 10 ** rng.uniform(3, np.log10(max_sites))
@@ -721,8 +752,9 @@ def run_serve(args):
     plain FP64 engine; each request's result checked against its FP64 solve."""
     import fastkpm_gb300 as fk
     from fastkpm_gb300.serve import Request, Server
-    reqs = serve_requests(args.serve_requests, 5, args.serve_max_sites)
-    srv = Server(max_slots=8, memory_budget=int(120e9))
+    reqs = serve_requests(args.serve_requests, 5, args.serve_max_sites, args.serve_rate)
+    srv = Server(max_slots=8, memory_budget=int(120e9), pack_bytes=int(args.serve_pack_bytes),
+                 pack_max=16 if args.serve_pack_bytes > 0 else 1)
     t0 = time.perf_counter()
     tickets = []
     for r in reqs:
@@ -760,10 +792,12 @@ def run_serve(args):
     line = {"metric": METRIC, "value": st["probe_steps_per_s"], "unit": UNIT, "n_gpus": 1, "steps": len(reqs),
             "warmup": 0, "ms_per_step": st["wall_s"] * 1e3 / max(len(reqs), 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 recursion, f64 accumulation", "data": "synthetic",
-            "config": {"workload": "Poisson stream of %d mixed KPM solves (moments + autodiff D), sites 1e3..%g"
-                                   % (len(reqs), args.serve_max_sites), "slots": 8},
+            "config": {"workload": "Poisson stream of %d mixed KPM solves (moments + autodiff D), sites 1e3..%g, "
+                                   "%g arrivals/s" % (len(reqs), args.serve_max_sites, args.serve_rate), "slots": 8},
             "latency_p50_s": st["p50_s"], "latency_p99_s": st["p99_s"], "completed": st["completed"],
             "rejected": st["rejected"], "max_concurrent": st["max_concurrent"],
+            "packs": {"batches": st["packs"], "requests": st["packed_requests"], "pack_bytes": int(args.serve_pack_bytes),
+                      "what": "requests solved together by one batch (one launch per Chebyshev step)"},
             "serial_fp64_probe_steps_per_s": work / t_ser, "speedup_vs_serial_fp64": (work / t_ser and
                                                                                   st["probe_steps_per_s"] / (work / t_ser)),
             "moments_max_rel_mu0_vs_fp64": worst, "serial_fp64_requests": n_ser}
@@ -774,6 +808,9 @@ def run_serve(args):
                                 % (st["busy_s"], st["wall_s"]),
                         "bytes": "sum of each solve's algorithmic bytes (forward steps + fused reverse steps)",
                         "peak_source": kind}
+    gbs_wall = st["algorithmic_bytes"] / max(st["wall_s"], 1e-9) / 1e9
+    line["roofline_wall"] = {"bound": "hbm", "achieved": gbs_wall, "peak": peak, "unit": "GB/s", "frac": gbs_wall / peak,
+                             "over": "wall time from the first arrival to the last completion (%.2f s)" % st["wall_s"]}
     print(json.dumps(line), flush=True)
 
 

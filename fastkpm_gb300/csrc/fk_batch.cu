@@ -114,7 +114,11 @@ struct fk_batch {
     std::vector<double> h_raw;
     bool configured = false;
     int opt_graphs = 0;
-    int acc64 = 1;   // FK_OPT_ACC64 (FP32 batches): FP64 moment sums and D accumulator
+    // FK_OPT_ACC64 (FP32 batches): 0 (default) float-float per-thread sums, 1 FP64. Measured on the
+    // 64 square lattices (b=1, S=32, M=500): 37.8 ms per batch with float-float sums, 45.8 ms with FP64
+    // ones (the narrow-row step's per-row FP64 conversions and adds keep this GPU's FP64 pipe 44% busy
+    // and double its short-scoreboard stalls); the moments' error against FP64 is 3.0e-7 either way.
+    int acc64 = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* prof = nullptr;   // events around each step launch
     std::map<int, cudaGraphExec_t> graphs;
     cudaEvent_t t0 = nullptr, t1 = nullptr;

@@ -7,10 +7,20 @@ its own GB300 engine and CUDA stream, so admitted solves of different sizes
 run concurrently on the device, and a request that arrives while others are
 running starts as soon as a slot and its memory are free. Probe and recursion
 state stay on the device for the whole solve (moments -> autodiff_matrix).
-Every kernel's per-system reduction order depends only on that system, so a
-request's result is the same alone and in any mix. Solves whose algorithmic traffic is
-below `urgent_bytes` run on a high-priority CUDA stream, so that short requests are not
-queued behind the CTAs of long ones.
+
+Small autodiff solves share launches: a request whose footprint is at most
+`pack_bytes` has a pack key (value kind, block size, probe count, order,
+precision); when one is admitted while queued requests have the same key, up to
+`pack_max` of them are admitted together as one pack, solved by a Batch: every
+Chebyshev step of every system in the pack is one launch, and the reverse
+recursion and D of all of them too. A request admitted with no partner runs on
+an engine of its own (creating a batch for one request costs more than it
+saves). Every kernel's per-system reduction order depends only on that system,
+so a request's result in a pack of any composition is bit-identical to its
+result as a pack of one, and on its own engine the same as alone; the two paths
+agree within the FP32 tolerance. Solves whose algorithmic traffic is below `urgent_bytes` run on
+a high-priority CUDA stream, so that short requests are not queued behind the
+CTAs of long ones.
 
     srv = Server(max_slots=8, memory_budget=100 << 30)
     t = srv.submit(Request(H, es, R, M, c))
@@ -23,7 +33,7 @@ import time
 import numpy as np
 
 from . import _lib as L
-from .engine import Engine
+from .engine import Batch, Engine
 
 
 class Request:
@@ -58,6 +68,7 @@ class Request:
         self.arrival = time.perf_counter() if arrival is None else arrival
         self.admitted = None
         self.finished = None
+        self.pack_size = 1   # requests in the batch that solved this one (1: its own engine)
         self.mu = None
         self.D = None
         self.error = None
@@ -69,6 +80,25 @@ class Request:
 
     def probe_steps(self):
         return float(self.n_rows) * self.M * self.s
+
+    def pack_key(self, max_bytes):
+        """Requests with equal keys can share one batched launch per Chebyshev step: autodiff solves
+        of the same value kind, block size, probe count, order and precision, each of footprint at
+        most max_bytes. None: the request runs on an engine of its own."""
+        if self.kind != "autodiff" or self.footprint() > max_bytes:
+            return None
+        return (self.complex_values, self.H.b_len, self.s, self.M, self.precision)
+
+    def dense_R(self):
+        """The probe block as a column-major n x s array (expanded from its nonzeros if needed)."""
+        if self.R is not None:
+            return self.R
+        s, cols, vals = self.R_entries
+        R = np.zeros((self.n_rows, s), np.complex128 if self.complex_values else np.float64, order="F")
+        rows = np.arange(self.n_rows)
+        for q in range(cols.shape[1]):
+            R[rows, cols[:, q]] += vals[:, q]   # one entry per row in each slice q
+        return R
 
     def algorithmic_bytes(self):
         """HBM bytes the solve must move at least: M/2 forward steps (read x, z, write y, H once)
@@ -103,6 +133,21 @@ class Request:
         return vec + h + d + stage + scratch
 
 
+def pack_group(req, queue, pack_bytes, pack_max):
+    """req and, when it is packable, the requests of `queue` (in order) with its pack key, at most
+    pack_max in all: the requests solved together by one batch."""
+    group = [req]
+    key = req.pack_key(pack_bytes)
+    if key is None:
+        return group
+    for other in queue:
+        if len(group) >= pack_max:
+            break
+        if other is not req and other.pack_key(pack_bytes) == key:
+            group.append(other)
+    return group
+
+
 class _Slot:
     def __init__(self, server, idx):
         self.server = server
@@ -124,15 +169,45 @@ class _Slot:
             self.engines[key] = e
         return e
 
+    def _run_pack(self, reqs):
+        """Solve a pack of same-key requests with one Batch: moments and autodiff_matrix of all of
+        them, one launch per Chebyshev step."""
+        r0 = reqs[0]
+        bt = Batch(r0.complex_values, r0.precision, device=self.server.device)
+        try:
+            for r in reqs:
+                bt.add(r.H, r.es, r.dense_R())
+            bt.commit()
+            mu = bt.moments(r0.M)
+            Ds = bt.autodiff_matrix(r0.M, np.stack([r.c for r in reqs]))
+            for k, r in enumerate(reqs):
+                r.mu = mu[k].copy()
+                r.D = Ds[k].val.copy()
+        finally:
+            bt.close()
+
     def _run(self):
         while True:
             self.wake.wait()
             self.wake.clear()
-            req = self.req
-            if req is None:
+            reqs = self.req
+            if reqs is None:
                 if self.server._stopping:
                     return
                 continue
+            if len(reqs) > 1:
+                try:
+                    self._run_pack(reqs)
+                except Exception as ex:   # the pack fails, the server keeps serving
+                    for r in reqs:
+                        r.error = ex
+                t = time.perf_counter()
+                for r in reqs:
+                    r.finished = t
+                self.req = None
+                self.server._slot_done(self, reqs)
+                continue
+            req = reqs[0]
             try:
                 eng = self.engine(req)
                 # short solves run on an urgent stream so their launches are not queued behind
@@ -156,13 +231,15 @@ class _Slot:
                 req.error = ex
             req.finished = time.perf_counter()
             self.req = None
-            self.server._slot_done(self, req)
+            self.server._slot_done(self, [req])
 
 
 class Server:
     def __init__(self, device=0, max_slots=8, memory_budget=None, lookahead=64, max_bypass=16,
-                 urgent_bytes=100e9):
+                 urgent_bytes=100e9, pack_bytes=256 << 20, pack_max=16):
         self.device = device
+        self.pack_bytes = int(pack_bytes) if pack_max > 1 else -1   # footprint bound of packable requests
+        self.pack_max = max(1, int(pack_max))
         self.urgent_bytes = float(urgent_bytes)   # solves moving less than this get the urgent stream
         if memory_budget is None:
             memory_budget = int(0.8 * self.device_free(device))
@@ -176,6 +253,7 @@ class Server:
         self._reserved = {}           # slot idx -> bytes reserved by its request
         self.completed = []
         self.rejected = []
+        self.packs = []               # sizes of the packs solved by a Batch
         self.max_concurrent = 0
         self._head_bypassed = 0
         self._dispatcher = threading.Thread(target=self._dispatch, name="fkpm-dispatch", daemon=True)
@@ -237,9 +315,12 @@ class Server:
     def _used(self):
         return sum(self._reserved.values())
 
-    def _need(self, slot, req):
-        """Bytes this slot would hold with req admitted (engine buffers only grow)."""
-        return max(slot.capacity(), req.footprint())
+    def _need(self, slot, group):
+        """Bytes this slot would hold with the requests admitted (engine buffers only grow; a pack's
+        batch holds about the sum of its requests' footprints while it runs)."""
+        if len(group) > 1:
+            return slot.capacity() + sum(r.footprint() for r in group)
+        return max(slot.capacity(), group[0].footprint())
 
     def _dispatch(self):
         with self._lock:
@@ -252,13 +333,24 @@ class Server:
                         if qi > 0 and self._head_bypassed >= self.max_bypass:
                             break
                         slot = min(free_slots, key=lambda s: abs(s.capacity() - req.footprint()))
-                        need = self._need(slot, req)
+                        group = pack_group(req, list(self._queue)[:self.lookahead], self.pack_bytes, self.pack_max)
+                        need = self._need(slot, group)
+                        while len(group) > 1 and self._used() - self._reserved.get(slot.idx, 0) + need > self.budget:
+                            group.pop()
+                            need = self._need(slot, group)
                         if self._used() - self._reserved.get(slot.idx, 0) + need <= self.budget:
-                            self._queue.remove(req)
+                            for r in group:
+                                self._queue.remove(r)
                             self._head_bypassed = self._head_bypassed + 1 if qi > 0 else 0
                             self._reserved[slot.idx] = need
-                            req.admitted = time.perf_counter()
-                            slot.req = req
+                            t_adm = time.perf_counter()
+                            for r in group:
+                                r.admitted = t_adm
+                            if len(group) > 1:
+                                self.packs.append(len(group))
+                            for r in group:
+                                r.pack_size = len(group)
+                            slot.req = group
                             slot.wake.set()
                             admitted = True
                             busy = sum(1 for s in self._slots if s.req is not None)
@@ -267,14 +359,15 @@ class Server:
                 if not admitted:
                     self._lock.wait(0.05)
 
-    def _slot_done(self, slot, req):
+    def _slot_done(self, slot, reqs):
         with self._lock:
             self._reserved[slot.idx] = slot.capacity()
-            if req.error is None:
-                self.completed.append(req)
-            else:
-                self.rejected.append(req)
-            req.done.set()
+            for req in reqs:
+                if req.error is None:
+                    self.completed.append(req)
+                else:
+                    self.rejected.append(req)
+                req.done.set()
             self._lock.notify_all()
 
     def stats(self):
@@ -294,4 +387,5 @@ class Server:
         return {"busy_s": busy, "algorithmic_bytes": sum(r.algorithmic_bytes() for r in self.completed),"completed": len(self.completed), "rejected": len(self.rejected),
                 "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                 "probe_steps_per_s": work / max(t1 - t0, 1e-9), "wall_s": t1 - t0,
-                "max_concurrent": self.max_concurrent, "budget_bytes": self.budget}
+                "max_concurrent": self.max_concurrent, "budget_bytes": self.budget,
+                "packs": len(self.packs), "packed_requests": int(sum(self.packs))}

@@ -98,8 +98,9 @@ int  fk_engine_synchronize(fk_engine* e);
                                 * clamped to the device's range); FK_ERR_STATE on a caller-set stream   */
 #define FK_OPT_ACC64      13   /* FP32 engines: 1 (default) each thread's moment sums and the D accumulator across
                                 * the reverse recursion are FP64 (doubles, DADD / DFMA); 0 float-float pairs on
-                                * the FP32 pipe, D converted to double once at the end. Reads back 1 for FP64
-                                * engines and 0 for float-float (DS) engines                                  */
+                                * the FP32 pipe, D converted to double once at the end. Batches (fk_batch_*)
+                                * default to 0: there the FP64 additions cost 21% (narrow rows). Reads back 1
+                                * for FP64 engines and 0 for float-float (DS) engines                         */
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 

@@ -59,3 +59,20 @@ def test_request_with_probe_entries():
     import pytest
     with pytest.raises(ValueError):
         Request(H, es, np.ones((H.n_rows, 4)), 10, np.zeros(10), R_entries=(s, cols, vals))
+
+
+def test_pack_group_takes_same_key_requests_in_order():
+    from fastkpm_gb300.serve import pack_group
+    H8, es8 = W.square_lattice(8, -1.0, 1.0, seed=1)
+    H6, es6 = W.square_lattice(6, -1.0, 1.0, seed=2)
+
+    def req(H, es, S=8, M=10, kind="autodiff"):
+        return Request(H, es, np.ones((H.n_rows, S)), M, np.zeros(M), kind, "fp32")
+    a, b, c, d, e = req(H8, es8), req(H6, es6), req(H8, es8, S=16), req(H8, es8, M=12), req(H6, es6, kind="stoch")
+    f, g = req(H6, es6), req(H8, es8)
+    queue = [a, b, c, d, e, f, g]
+    assert pack_group(a, queue, 1 << 30, 16) == [a, b, f, g]        # same kind, b, S, M, precision
+    assert pack_group(a, queue, 1 << 30, 3) == [a, b, f]            # at most pack_max
+    assert pack_group(e, queue, 1 << 30, 16) == [e]                 # stoch solves are not packed
+    assert pack_group(a, queue, a.footprint() - 1, 16) == [a]       # above the footprint bound: alone
+    assert a.pack_key(1 << 30) != c.pack_key(1 << 30) != d.pack_key(1 << 30)
