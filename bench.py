@@ -225,10 +225,13 @@ def step_flops_per_launch(H, S):
 
 
 # DRAM bytes and warp instructions per row of one fused adjoint launch, from ncu captures on the
-# cubic L=32 case (profiles/): traffic grows in proportion to the rows, so the L=64 launch's traffic
-# is these times N. Keys: precision. A precision without a capture of the current kernel reports null.
-ADJ_TRAFFIC_PER_ROW = {"ds": (1.600211e9 + 0.529769e9) / 65536}
-ADJ_WARP_INST_PER_ROW = {"ds": 1108457856 / 65536}
+# cubic L=32 case (65,536 rows; profiles/k_adjoint_*_cubic32.md): traffic grows in proportion to the
+# rows, so the L=64 launch's traffic is these times N. Keys: (precision, FP64 accumulators). An
+# engine form without a capture of its current kernel reports null.
+ADJ_TRAFFIC_PER_ROW = {("fp64", 1): (1.838671e9 + 0.646393e9) / 65536,
+                       ("fp32", 1): (0.577651e9 + 0.248572e9) / 65536,
+                       ("ds", 0): (1.570807e9 + 0.529550e9) / 65536}
+ADJ_WARP_INST_PER_ROW = {("ds", 0): 1108457856 / 65536}
 ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
 
 
@@ -362,7 +365,8 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=Non
     bytes_step = step_bytes_per_launch(N, S, nnzb, 2, sv)
     ach_adj = bytes_adj / (avg_adj_ms * 1e-3) / 1e9
     ach_step = bytes_step / (avg_step_ms * 1e-3) / 1e9
-    traffic = ADJ_TRAFFIC_PER_ROW[prec] * N if (prec in ADJ_TRAFFIC_PER_ROW and S == 256 and fused) else None
+    key = (prec, acc64)
+    traffic = ADJ_TRAFFIC_PER_ROW[key] * N if (key in ADJ_TRAFFIC_PER_ROW and S == 256 and fused) else None
     clocks = clk.summary()
     out = dict(prec=prec, value=replica_value(per_solve, steps, ws, ms_max), ms=ms_max, steps=steps, warmup=warmup,
                clocks=clocks, launches=sum(v[0] for v in prof.values()), mu=mu, D=D.val.copy(), fused=fused,
@@ -394,9 +398,9 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=Non
             "peak_source": "fk_device_fma_rate: independent DFMA chains timed on this GPU in this run",
             "adjoint": {"achieved": a_adj, "frac": a_adj / pk if pk else None, "flops_per_launch": fl_adj},
             "step": {"achieved": a_step, "frac": a_step / pk if pk else None, "flops_per_launch": fl_step}}
-    if prec in ADJ_WARP_INST_PER_ROW and S == 256 and fused:
+    if key in ADJ_WARP_INST_PER_ROW and S == 256 and fused:
         clk_mhz = max(clocks.get("sm_mhz") or 2070.0, 1.0)
-        inst_rate = ADJ_WARP_INST_PER_ROW[prec] * N / (avg_adj_ms * 1e-3)
+        inst_rate = ADJ_WARP_INST_PER_ROW[key] * N / (avg_adj_ms * 1e-3)
         peak_rate = ISSUE_PEAK_WARP_INST_PER_CYCLE * clk_mhz * 1e6
         out["roofline_issue"] = {"bound": "instruction issue (FP32 pipe: float-float arithmetic)",
                                  "achieved": inst_rate / 1e12, "peak": peak_rate / 1e12,
