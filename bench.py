@@ -78,6 +78,7 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=24)
     p.add_argument("--serve-max-sites", type=float, default=1e6)
     p.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrival rate of the request stream (1/s)")
+    p.add_argument("--serve-cta-waves", type=int, default=8, help="FK_OPT_CTA_WAVES of the serving engines")
     p.add_argument("--serve-pack-bytes", type=float, default=256 << 20,
                    help="footprint bound of requests that share batched launches (0: no packing)")
     return p.parse_args()
@@ -758,7 +759,7 @@ def run_serve(args):
     from fastkpm_gb300.serve import Request, Server
     reqs = serve_requests(args.serve_requests, 5, args.serve_max_sites, args.serve_rate)
     srv = Server(max_slots=8, memory_budget=int(120e9), pack_bytes=int(args.serve_pack_bytes),
-                 pack_max=16 if args.serve_pack_bytes > 0 else 1)
+                 pack_max=16 if args.serve_pack_bytes > 0 else 1, cta_waves=args.serve_cta_waves)
     t0 = time.perf_counter()
     tickets = []
     for r in reqs:
@@ -797,14 +798,19 @@ def run_serve(args):
             "warmup": 0, "ms_per_step": st["wall_s"] * 1e3 / max(len(reqs), 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 recursion, f64 accumulation", "data": "synthetic",
             "config": {"workload": "Poisson stream of %d mixed KPM solves (moments + autodiff D), sites 1e3..%g, "
-                                   "%g arrivals/s" % (len(reqs), args.serve_max_sites, args.serve_rate), "slots": 8},
-            "latency_p50_s": st["p50_s"], "latency_p99_s": st["p99_s"], "completed": st["completed"],
+                                   "%g arrivals/s" % (len(reqs), args.serve_max_sites, args.serve_rate), "slots": 8,
+                       "cta_waves": args.serve_cta_waves},
+            "latency_p50_s": st["p50_s"], "latency_p99_s": st["p99_s"], "queue_wait_p50_s": st["queue_p50_s"],
+            "service_p50_s": st["service_p50_s"], "completed": st["completed"],
             "rejected": st["rejected"], "max_concurrent": st["max_concurrent"],
             "packs": {"batches": st["packs"], "requests": st["packed_requests"], "pack_bytes": int(args.serve_pack_bytes),
                       "what": "requests solved together by one batch (one launch per Chebyshev step)"},
             "serial_fp64_probe_steps_per_s": work / t_ser, "speedup_vs_serial_fp64": (work / t_ser and
                                                                                   st["probe_steps_per_s"] / (work / t_ser)),
-            "moments_max_rel_mu0_vs_fp64": worst, "serial_fp64_requests": n_ser}
+            "moments_max_rel_mu0_vs_fp64": worst, "serial_fp64_requests": n_ser,
+            "requests": {"columns": ["rows", "M", "S", "queue_s", "service_s"],
+                         "rows": [[t.n_rows, t.M, t.s, round(t.admitted - t.arrival, 4), round(t.finished - t.admitted, 4)]
+                                  for t in tickets if t.error is None and t.admitted is not None]}}
     peak, kind = peaks()
     gbs = st["algorithmic_bytes"] / max(st["busy_s"], 1e-9) / 1e9
     line["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,

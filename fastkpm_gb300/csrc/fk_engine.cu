@@ -138,6 +138,7 @@ struct fk_engine {
     int opt_adj_split = 2;     // FK_OPT_ADJ_SPLIT: 0 one pass, 1 two passes, 2 (default) by configuration
     int opt_pipe = 2;          // FK_OPT_PIPE: 0 plain step, 1 double-buffered gathers (FP32), 2 (default) by configuration
     int opt_acc64 = 1;         // FK_OPT_ACC64 (FP32 engines): 1 FP64 moment sums and D accumulator, 0 float-float
+    int opt_waves = 1;         // FK_OPT_CTA_WAVES: grids of this many times the resident CTAs (shorter-lived CTAs)
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
@@ -517,7 +518,7 @@ int configure(fk_engine* e) {
         FK_TRY(prec_occupancy(e, okind, c.NP, c.smem, &occ), "occupancy query");
         if (occ < 1) return e->fail(FK_ERR_UNSUPPORTED, "kernel kind %d does not fit on an SM", kind);
         if (e->opt_ctas_per_sm > 0) occ = std::min(occ, e->opt_ctas_per_sm);
-        c.ctas = (int)std::max<long long>(1, std::min<long long>(tiles, (long long)occ * e->num_sms));
+        c.ctas = (int)std::max<long long>(1, std::min<long long>(tiles, (long long)occ * e->num_sms * e->opt_waves));
         SysDesc sd{0, e->n_b, 0, c.ctas};
         FK_TRY(c.sys.ensure(sizeof(SysDesc)), "alloc sys table");
         FK_TRY(cudaMemcpy(c.sys.p, &sd, sizeof sd, cudaMemcpyHostToDevice), "upload sys table");
@@ -1507,6 +1508,11 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             e->opt_pipe = value;
             drop_graphs(e);
             return configure(e);
+        case FK_OPT_CTA_WAVES:
+            if (value < 1 || value > 64) return e->fail(FK_ERR_ARG, "CTA_WAVES must be 1 .. 64");
+            e->opt_waves = value;
+            drop_graphs(e);
+            return configure(e);
         case FK_OPT_ACC64:
             if (value < 0 || value > 1) return e->fail(FK_ERR_ARG, "ACC64 must be 0 or 1");
             e->opt_acc64 = value;   // the kept recursion state stays valid: every D call starts its accumulator anew
@@ -1559,6 +1565,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_ADJ_SPLIT: *value = e->opt_adj_split; return FK_OK;
         case FK_OPT_PIPE: *value = e->cfg[fk::kStep].valid ? (int)e->cfg[fk::kStep].pipe : e->opt_pipe; return FK_OK;
         case FK_OPT_ACC64: *value = e->prec == fk::kF64 ? 1 : e->prec == fk::kF32 ? e->opt_acc64 : 0; return FK_OK;
+        case FK_OPT_CTA_WAVES: *value = e->opt_waves; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }

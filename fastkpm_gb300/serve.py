@@ -36,6 +36,10 @@ from . import _lib as L
 from .engine import Batch, Engine
 
 
+# FK_OPT_CTA_WAVES of the slots' engines: grids of 8 resident-CTA waves (see Server)
+DEFAULT_CTA_WAVES = 8
+
+
 class Request:
     """One KPM solve: moments(M), then autodiff_matrix(c, D) ("autodiff") or
     stoch_matrix(c, D) ("stoch") on H's pattern. The probe block is R (dense, n x s) or, for
@@ -166,6 +170,9 @@ class _Slot:
         e = self.engines.get(key)
         if e is None:
             e = Engine(req.complex_values, req.precision, device=self.server.device)
+            # grids of several CTA waves: a long solve's CTAs are short-lived, so the launches of a short
+            # solve on the urgent stream find free SMs within a fraction of a long launch
+            e.set_option(L.FK_OPT_CTA_WAVES, self.server.cta_waves)
             self.engines[key] = e
         return e
 
@@ -236,8 +243,9 @@ class _Slot:
 
 class Server:
     def __init__(self, device=0, max_slots=8, memory_budget=None, lookahead=64, max_bypass=16,
-                 urgent_bytes=100e9, pack_bytes=256 << 20, pack_max=16):
+                 urgent_bytes=100e9, pack_bytes=256 << 20, pack_max=16, cta_waves=DEFAULT_CTA_WAVES):
         self.device = device
+        self.cta_waves = int(cta_waves)   # FK_OPT_CTA_WAVES of the slots' engines
         self.pack_bytes = int(pack_bytes) if pack_max > 1 else -1   # footprint bound of packable requests
         self.pack_max = max(1, int(pack_max))
         self.urgent_bytes = float(urgent_bytes)   # solves moving less than this get the urgent stream
@@ -386,6 +394,8 @@ class Server:
                 end = f
         return {"busy_s": busy, "algorithmic_bytes": sum(r.algorithmic_bytes() for r in self.completed),"completed": len(self.completed), "rejected": len(self.rejected),
                 "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "queue_p50_s": float(np.median([r.admitted - r.arrival for r in self.completed])) if self.completed else 0.0,
+                "service_p50_s": float(np.median([r.finished - r.admitted for r in self.completed])) if self.completed else 0.0,
                 "probe_steps_per_s": work / max(t1 - t0, 1e-9), "wall_s": t1 - t0,
                 "max_concurrent": self.max_concurrent, "budget_bytes": self.budget,
                 "packs": len(self.packs), "packed_requests": int(sum(self.packs))}

@@ -101,6 +101,11 @@ int  fk_engine_synchronize(fk_engine* e);
                                 * the FP32 pipe, D converted to double once at the end. Batches (fk_batch_*)
                                 * default to 0: there the FP64 additions cost 21% (narrow rows). Reads back 1
                                 * for FP64 engines and 0 for float-float (DS) engines                         */
+#define FK_OPT_CTA_WAVES  14   /* launch grids of this many times the CTAs an SM set holds at once (1 .. 64; 1 the
+                                * default: every CTA walks its share of tiles for the whole launch). Larger values
+                                * make each CTA shorter-lived, so that launches of a higher-priority stream on the
+                                * same GPU start sooner (the serving loop's short solves); moment sums are then
+                                * added over more CTA partials (last-bit differences, deterministic)          */
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 

@@ -103,6 +103,7 @@ def test_identity_probes_exact_traces(gpu, prec):
     {L.FK_OPT_NP: 1},
     {L.FK_OPT_NP: 2},
     {L.FK_OPT_CTAS_PER_SM: 1},
+    {L.FK_OPT_CTA_WAVES: 8},
 ])
 def test_launch_options_do_not_change_results(gpu, opts):
     # S = 80 complex -> 80 packets per row: exercises column slices when NP is capped

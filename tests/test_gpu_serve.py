@@ -13,7 +13,7 @@ import pytest
 import fastkpm_gb300 as fk
 from fastkpm_gb300 import _lib as L
 from fastkpm_gb300 import workloads as W
-from fastkpm_gb300.serve import Request, Server
+from fastkpm_gb300.serve import DEFAULT_CTA_WAVES, Request, Server
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -49,6 +49,7 @@ def solo(H, es, R, M, c, precision, packable=False):
         bt.close()
         return mu, D
     eng = fk.Engine(cplx, precision)
+    eng.set_option(L.FK_OPT_CTA_WAVES, DEFAULT_CTA_WAVES)   # as the server's slot engines
     eng.set_H(H, es)
     eng.set_R(R)
     mu = eng.moments(M)
