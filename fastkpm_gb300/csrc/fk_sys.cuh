@@ -4,8 +4,10 @@
 // sums are stored and combined. Three precisions x {real, complex}:
 //
 //   F64  native IEEE double storage and DFMA arithmetic.
-//   F32  float storage and arithmetic; moment sums promoted to a float-float
-//        accumulator per block row; D sums finished in FP64.
+//   F32  float storage and arithmetic; per-row partial sums in float, accumulated
+//        in FP64 (SysF32RA / SysF32CA, the engine default) or in float-float
+//        pairs (SysF32R / SysF32C), the moment sums and the D accumulator alike;
+//        D finished in FP64.
 //   DS   "double-single": every real number is an unevaluated sum hi + lo of
 //        two floats (about 48 significant bits), stored in 8 bytes like a
 //        double, and all arithmetic runs on the FP32 pipe with error-free
@@ -76,7 +78,10 @@ struct SysF64R {
     __device__ static void mac(Acc& a, H h, E x) { a = fma(h, x, a); }
     __device__ static void mac_re(Acc& a, Hr h, E x) { a = fma(h, x, a); }
     // y = alpha * acc + beta * z, alpha in {1, 2}, beta in {0, -1}
+    // 2 a - z as one fma: 2 a is exact, so fma(2, a, -z) = round(2 a - z), the same value as
+    // (2 a) - z with one FP64-pipe instruction instead of two (the flags are kernel arguments)
     __device__ static E fin(Acc a, bool two, bool has_z, E z) {
+        if (two && has_z) return fma(2.0, a, -z);
         double v = two ? 2.0 * a : a;
         return has_z ? v - z : v;
     }
@@ -116,6 +121,7 @@ struct SysF64C {
     }
     __device__ static void mac_re(Acc& a, Hr h, E x) { a.x = fma(h, x.x, a.x); a.y = fma(h, x.y, a.y); }
     __device__ static E fin(Acc a, bool two, bool has_z, E z) {
+        if (two && has_z) return make_double2(fma(2.0, a.x, -z.x), fma(2.0, a.y, -z.y));   // exact as above
         double vr = two ? 2.0 * a.x : a.x, vi = two ? 2.0 * a.y : a.y;
         return has_z ? make_double2(vr - z.x, vi - z.y) : make_double2(vr, vi);
     }
@@ -160,6 +166,7 @@ struct SysF32R {
     __device__ static void mac(Acc& a, H h, E x) { a = fmaf(h, x, a); }
     __device__ static void mac_re(Acc& a, Hr h, E x) { a = fmaf(h, x, a); }
     __device__ static E fin(Acc a, bool two, bool has_z, E z) {
+        if (two && has_z) return fmaf(2.f, a, -z);   // 2 a exact: the same value as (2 a) - z
         float v = two ? 2.f * a : a;
         return has_z ? v - z : v;
     }
@@ -204,6 +211,7 @@ struct SysF32C {
     }
     __device__ static void mac_re(Acc& a, Hr h, E x) { a.x = fmaf(h, x.x, a.x); a.y = fmaf(h, x.y, a.y); }
     __device__ static E fin(Acc a, bool two, bool has_z, E z) {
+        if (two && has_z) return make_float2(fmaf(2.f, a.x, -z.x), fmaf(2.f, a.y, -z.y));   // exact as above
         float vr = two ? 2.f * a.x : a.x, vi = two ? 2.f * a.y : a.y;
         return has_z ? make_float2(vr - z.x, vi - z.y) : make_float2(vr, vi);
     }
