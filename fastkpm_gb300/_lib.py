@@ -22,6 +22,7 @@ FK_OPT_ADJ_SPLIT = 11
 FK_OPT_PIPE = 12
 FK_OPT_ACC64 = 13
 FK_OPT_CTA_WAVES = 14
+FK_OPT_WARP_ROWS = 15
 
 PRECISIONS = {"fp64": FK_PREC_FP64, "fp32": FK_PREC_FP32, "ds": FK_PREC_DS}
 

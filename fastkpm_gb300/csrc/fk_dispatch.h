@@ -11,7 +11,7 @@ namespace fk {
 
 enum Prec { kF64 = 0, kF32 = 1, kDS = 2 };
 enum KernelKind { kStep = 0, kAdjoint = 1, kOuter = 2, kHelper = 3, kNumKinds = 4, kStepStaged = 5, kStepStagedAsync = 6,
-                  kAdjointSplit = 7, kStepPipe = 8, kAdjointPipe = 9 };
+                  kAdjointSplit = 7, kStepPipe = 8, kAdjointPipe = 9, kAdjointWarp = 10 };
 
 struct Launch {
     int grid;

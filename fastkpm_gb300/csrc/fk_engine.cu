@@ -57,6 +57,7 @@ struct KCfg {
     bool staged = false;   // step kind only: TMA-staged gathers (k_cheb_step_staged)
     bool split = false;    // adjoint kind only: two passes over the blocks (k_adjoint_split)
     bool pipe = false;     // step kind only: double-buffered gathers (k_cheb_step_pipe, FP32)
+    bool warp = false;     // adjoint kind: the warp-per-row kernel (k_adjoint_warp)
     int umax = 0;          // largest per-tile gather list
 };
 
@@ -139,6 +140,7 @@ struct fk_engine {
     int opt_pipe = 2;          // FK_OPT_PIPE: 0 plain step, 1 double-buffered gathers (FP32), 2 (default) by configuration
     int opt_acc64 = 1;         // FK_OPT_ACC64 (FP32 engines): 1 FP64 moment sums and D accumulator, 0 float-float
     int opt_waves = 1;         // FK_OPT_CTA_WAVES: grids of this many times the resident CTAs (shorter-lived CTAs)
+    int opt_warp = 1;          // FK_OPT_WARP_ROWS: warp-per-row kernels where a warp serves each block row
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
@@ -505,14 +507,22 @@ int configure(fk_engine* e) {
         c.pipe = (kind == fk::kStep && !e->opt_tma && use_pipe(e, fk::kStep, NP)) ||
                  (kind == fk::kAdjoint && use_pipe(e, fk::kAdjoint, NP));
         c.split = kind == fk::kAdjoint && !c.pipe && use_adjoint_split(e, NP);
+        // the warp-per-row kernel (FP32) keeps a row's block columns one per lane: rows of at most
+        // 32 blocks. Float-float keeps k_adjoint_pipe: its blocks' code is ~4x longer, and the warp
+        // kernel's unrolled, class-specialised copies measured slower (cubic L=64, S=256: 10.54 vs
+        // 9.75 ms; FP32 1.85 vs 2.14 ms)
+        c.warp = kind == fk::kAdjoint && c.pipe && e->opt_warp && e->prec == fk::kF32 && Gp == 32 &&
+                 P % (32 * NP) == 0 && fk::max_row_blocks(e->h_row_ptr.data(), e->n_b) <= 32;
         if (c.split) c.smem += 2 * (size_t)fk::kThreads * e->b * NP * 16;   // kept alpha_{m+1}, alpha_{m-1}
-        if (c.pipe) c.smem = stage_smem + (kind == fk::kStep ? fk::pipe_smem_bytes(e->b, NP) : fk::adj_pipe_smem_bytes(e->b, NP));
+        if (c.pipe) c.smem = stage_smem + (kind == fk::kStep ? fk::pipe_smem_bytes(e->b, NP)
+                                           : c.warp ? fk::adj_warp_smem_bytes(e->b, NP) : fk::adj_pipe_smem_bytes(e->b, NP));
         if (kind == fk::kStep && e->opt_tma) {
             int rc = configure_staged(e, c, Gp, nk_max, per_blk);
             if (rc != FK_OK) return rc;
         }
         int occ = 0;
         const int okind = c.split ? (int)fk::kAdjointSplit
+                        : c.warp ? (int)fk::kAdjointWarp
                         : c.pipe ? (kind == fk::kStep ? (int)fk::kStepPipe : (int)fk::kAdjointPipe)
                         : !c.staged ? kind : (e->opt_tma == 1 ? (int)fk::kStepStaged : (int)fk::kStepStagedAsync);
         FK_TRY(prec_occupancy(e, okind, c.NP, c.smem, &occ), "occupancy query");
@@ -613,6 +623,7 @@ int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp,
         a.stage_cap = c.stage_cap;
         a.split = c.split ? 1 : 0;
         a.pipe = c.pipe ? 1 : 0;
+        a.warp = c.warp ? 1 : 0;
         ProfScope ps(e, fk::kAdjoint);
         FK_TRY(prec_launch_adjoint(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "adjoint kernel launch");
     }
@@ -1518,6 +1529,11 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             e->opt_acc64 = value;   // the kept recursion state stays valid: every D call starts its accumulator anew
             drop_graphs(e);
             return configure(e);
+        case FK_OPT_WARP_ROWS:
+            if (value < 0 || value > 1) return e->fail(FK_ERR_ARG, "WARP_ROWS must be 0 or 1");
+            e->opt_warp = value;
+            drop_graphs(e);
+            return configure(e);
         case FK_OPT_ADJ_SPLIT:
             if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "ADJ_SPLIT must be 0, 1 or 2");
             e->opt_adj_split = value;
@@ -1566,6 +1582,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_PIPE: *value = e->cfg[fk::kStep].valid ? (int)e->cfg[fk::kStep].pipe : e->opt_pipe; return FK_OK;
         case FK_OPT_ACC64: *value = e->prec == fk::kF64 ? 1 : e->prec == fk::kF32 ? e->opt_acc64 : 0; return FK_OK;
         case FK_OPT_CTA_WAVES: *value = e->opt_waves; return FK_OK;
+        case FK_OPT_WARP_ROWS: *value = e->cfg[fk::kAdjoint].valid ? (int)e->cfg[fk::kAdjoint].warp : e->opt_warp; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }

@@ -67,8 +67,21 @@ cudaError_t adj_pipe_launch(const AdjArgs& a, const Launch& l) {
     return cudaGetLastError();
 }
 template <class S, int B, int NP>
+cudaError_t adj_warp_launch(const AdjArgs& a, const Launch& l) {
+    if (l.smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)k_adjoint_warp<S, B, NP>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)l.smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_adjoint_warp<S, B, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+    return cudaGetLastError();
+}
+template <class S, int B, int NP>
 cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
     const bool whole = whole_chunks(a.P, a.Gp, NP);
+    if constexpr (S::PREC == 1) {   // FP32: rows served by a whole warp
+        if (a.pipe && a.warp && whole && a.Gp == 32 && a.Dacc) return adj_warp_launch<S, B, NP>(a, l);
+    }
     if constexpr (S::PREC != 0) {   // double-buffered gathers: FP32 and float-float systems
         if (a.pipe) return whole ? adj_pipe_launch<S, B, NP, true>(a, l) : adj_pipe_launch<S, B, NP, false>(a, l);
     }
@@ -85,6 +98,9 @@ cudaError_t outer_one(const OuterArgs& a, const Launch& l) {
 }
 template <class S, int B, int NP>
 const void* pipe_fn(int kind) {
+    if constexpr (S::PREC == 1) {
+        if (kind == kAdjointWarp) return (const void*)k_adjoint_warp<S, B, NP>;
+    }
     if constexpr (S::PREC != 0)
         return kind == kStepPipe ? (const void*)k_cheb_step_pipe<S, B, NP, true> : (const void*)k_adjoint_pipe<S, B, NP, true>;
     else return nullptr;
@@ -92,10 +108,10 @@ const void* pipe_fn(int kind) {
 template <class S, int B, int NP>
 cudaError_t occ_one(int kind, size_t smem, int* n) {
     if constexpr (S::PREC == 0) {
-        if (kind == kStepPipe || kind == kAdjointPipe) return cudaErrorInvalidValue;
+        if (kind == kStepPipe || kind == kAdjointPipe || kind == kAdjointWarp) return cudaErrorInvalidValue;
     }
     const void* f = kind == kStep ? (const void*)k_cheb_step<S, B, NP>
-                  : (kind == kStepPipe || kind == kAdjointPipe) ? pipe_fn<S, B, NP>(kind)
+                  : (kind == kStepPipe || kind == kAdjointPipe || kind == kAdjointWarp) ? pipe_fn<S, B, NP>(kind)
                   : kind == kAdjoint ? (const void*)k_adjoint_step<S, B, NP>
                   : kind == kAdjointSplit ? (const void*)k_adjoint_split<S, B, NP, true>
                   : kind == kStepStaged ? (const void*)k_cheb_step_staged<S, B, NP, true>

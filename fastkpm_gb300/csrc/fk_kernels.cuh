@@ -76,6 +76,7 @@ struct AdjArgs {
     int stage_cap;
     int split;            // run k_adjoint_split (two passes over the blocks) instead of k_adjoint_step
     int pipe;             // FP32 systems: run k_adjoint_pipe (double-buffered gathers)
+    int warp = 0;         // with pipe, Gp == 32, whole chunks and the fused epilogue: run k_adjoint_warp
 };
 
 struct OuterArgs {
@@ -433,14 +434,13 @@ __device__ __forceinline__ float2 bits_float2(double d) {
     return make_float2(__int_as_float((int)(unsigned)(u & 0xffffffffull)), __int_as_float((int)(unsigned)(u >> 32)));
 }
 
-// Reduce a block's per-lane D partials over the row group and add them to Dacc[k];
-// `pre` is the d_prefetch of the lane's first entry. FP64 systems accumulate in
+// Add a block's reduced D values (the entries [o.first, o.first + o.count) held by this lane)
+// to Dacc[k]; `pre` is the d_prefetch of the lane's first entry. FP64 systems accumulate in
 // double; FP32 and DS systems keep the accumulator as float-float pairs (same 8 bytes
 // per real) on the FP32 pipe and convert it to double once at the end (k_ds_to_double).
 template <class S, int B>
-__device__ __forceinline__ void flush_block(typename S::OAcc (&of)[B * B], int Gp, int g, bool has, size_t k,
-                                            double scale, float2 scale_ds, double* Dacc, const Owner& o, double2 pre) {
-    group_sum_transposed<S, B * B>(of, Gp, g);
+__device__ __forceinline__ void d_write(const typename S::OAcc (&of)[B * B], bool has, size_t k, double scale,
+                                        float2 scale_ds, double* Dacc, const Owner& o, double2 pre) {
     if (has && o.writer) {
 #pragma unroll
         for (int t = 0; t < B * B; t++) {
@@ -466,6 +466,14 @@ __device__ __forceinline__ void flush_block(typename S::OAcc (&of)[B * B], int G
             }
         }
     }
+}
+
+// Reduce a block's per-lane D partials over the row group and add them to Dacc[k].
+template <class S, int B>
+__device__ __forceinline__ void flush_block(typename S::OAcc (&of)[B * B], int Gp, int g, bool has, size_t k,
+                                            double scale, float2 scale_ds, double* Dacc, const Owner& o, double2 pre) {
+    group_sum_transposed<S, B * B>(of, Gp, g);
+    d_write<S, B>(of, has, k, scale, scale_ds, Dacc, o, pre);
 }
 
 // Float-float accumulator -> double, in place (both are 8 bytes per real).

@@ -233,6 +233,12 @@ inline bool append_tile_tables(const int* rp, const int* col, int n_b, int Gp, i
 }
 
 // Largest number of H blocks one tile of kThreads (row, lane) items touches.
+// Most blocks in one block row.
+inline int max_row_blocks(const int* row_ptr, int n_b) {
+    int m = 0;
+    for (int i = 0; i < n_b; i++) m = row_ptr[i + 1] - row_ptr[i] > m ? row_ptr[i + 1] - row_ptr[i] : m;
+    return m;
+}
 inline int max_tile_blocks(const int* row_ptr, int n_b, int Gp) {
     const long long items = (long long)n_b * Gp;
     const long long tiles = (items + kThreads - 1) / kThreads;

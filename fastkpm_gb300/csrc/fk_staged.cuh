@@ -689,4 +689,291 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
     }
 }
 
+// ---------------------------------------------------------------------------------
+// The FP32 reverse step for block rows served by a whole warp (Gp == 32) whose column chunks
+// are all whole: the shape of wide probe blocks (b=2 complex, S >= 128). Same
+// recursions, epilogue and double-buffered gathers as k_adjoint_pipe; the fixed shape lets it
+// drop per-block work that the general kernel spends on lanes of differing rows:
+//  * lane and packet offsets are compile-time (packet q of a lane sits 32 packets after q-1),
+//    and row addresses are one 32 x 32 -> 64-bit multiply-add each;
+//  * every lane of a warp walks the same row, so there is no per-block "row has block kk" test,
+//    no zero fill of missing blocks and no warp-wide maximum of the row lengths; the row's block
+//    columns are read once, one per lane (rows of at most 32 blocks), and passed by shuffles;
+//  * the block loop is unrolled by two, so the shared-memory buffers alternate at compile time;
+//    in FP32 the next block's H entries travel with its packets (a cp.async by the warp's first
+//    lanes into a per-warp shared slot of each buffer) instead of in registers;
+//  * b=2: a lane whose bit 4 is set (sw = 1) holds every block index swapped -- gathered rows
+//    b j + (bj ^ sw), own rows b i + (bi ^ sw), accumulators and H entries permuted to match --
+//    so the two D entries it sends at the first transposed reduction level are exactly the two
+//    its partner (lane ^ 16, the other swap) keeps, and that level needs no selects.
+// It runs with the fused D epilogue only (D's pattern is H's). Results equal k_adjoint_pipe's up to
+// the order of the two bj terms of a general block in the swapped lanes (FP32/float-float
+// rounding), and the same lanes write the same D entries.
+// ---------------------------------------------------------------------------------
+template <int V>
+struct BufTag { static constexpr int value = V; };
+
+__device__ __forceinline__ const uint4* row_at(const void* base, unsigned row, unsigned row_bytes) {
+    return reinterpret_cast<const uint4*>(static_cast<const char*>(base) + (unsigned long long)row * row_bytes);
+}
+
+// Shared memory of k_adjoint_warp after the H stage: the pipe kernel's slots, then two per-warp H
+// blocks (FP32) of up to 32 bytes each.
+__host__ __device__ inline size_t adj_warp_smem_bytes(int B, int NP) {
+    return adj_pipe_smem_bytes(B, NP) + (size_t)(kThreads / 32) * 2 * 32;
+}
+// cp.async of N = 4, 8 or 16 bytes (N < 16 goes through L1: the .cg form moves 16 bytes only)
+template <int N>
+__device__ __forceinline__ void cp_async_n(void* dst, const void* src) {
+    if constexpr (N == 16) cp_async16(dst, src);
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(N) : "memory");
+}
+
+template <class S, int B, int NP>
+__global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_warp(AdjArgs a) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    typedef typename S::OAcc OAcc;
+    constexpr int EPP = S::EPP;
+    constexpr int EPT = NP * EPP;
+    constexpr int G = 32;            // lanes per block row
+    constexpr int W = G * NP;        // packets per column chunk
+    constexpr bool kHAhead = S::PREC == 1;     // FP32: H entries copied a block ahead (not staged per tile)
+    constexpr int kHBytes = B * B * (int)sizeof(H);
+    static_assert(!kHAhead || kHBytes <= 32, "per-warp H slot holds 32 bytes");
+    constexpr bool kOwnAsync = S::PREC == 1;   // FP32: own rows copied at the start of each chunk
+    extern __shared__ __align__(16) unsigned char smem[];
+    H* s_h = reinterpret_cast<H*>(smem);
+    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
+    uint4* sbuf = reinterpret_cast<uint4*>(smem + ((sizeof(H) * B * B + sizeof(unsigned)) * (size_t)a.stage_cap + 15) / 16 * 16);
+    uint4* const mine = sbuf + threadIdx.x;
+    // thread-minor slots (same layout as k_adjoint_pipe): (buffer, vector v, bj, q) and own (v, bi, q)
+    auto slot = [&](int buf, int v, int bj, int q) -> uint4* { return mine + (((buf * 2 + v) * B + bj) * NP + q) * kThreads; };
+    auto own_slot = [&](int v, int bi, int q) -> uint4* { return mine + ((4 * B + v * B + bi) * NP + q) * kThreads; };
+    // per-warp H block of buffer `buf` (FP32)
+    H* const wh = reinterpret_cast<H*>(sbuf + (size_t)6 * B * NP * kThreads) + (threadIdx.x >> 5) * 2 * (32 / sizeof(H));
+    auto h_slot = [&](int buf) -> H* { return wh + buf * (32 / sizeof(H)); };
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int nch = a.P / W;
+    const long long items = (long long)sd.n_b * G;
+    const unsigned rb = (unsigned)(a.ld * (long long)sizeof(E));   // bytes per scalar row
+    const int lane = threadIdx.x & 31;
+    const int sw = B == 2 ? (lane >> 4) & 1 : 0;   // block-index swap of this lane
+    const int hx = sw * 3;                          // H entry (bi, bj) -> (bi ^ sw, bj ^ sw), column-major b=2
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef cA = S::coef(a.coef[sidx * a.cstride + 0]);
+    const typename S::Coef cAp = S::coef(a.coef[sidx * a.cstride + 1]);
+    const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
+    const float2 dscale_ds = ds_from_double(a.dscale);   // a.Dacc is never null here (fused epilogue only)
+    const Owner own = transposed_owner<B * B>(G, lane);
+
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const Tile tl = tile_range(a.row_ptr, sd, t0, items, G, a.stage_cap);
+        if (tl.staged) {
+            __syncthreads();
+            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
+            __syncthreads();
+        }
+        const long long t = t0 + threadIdx.x;
+        if (t >= items) continue;   // items is a multiple of 32: whole warps leave together
+        const int i = sd.row_base + (int)(t >> 5);
+        const int kb = a.row_ptr[i];
+        const int nrow = a.row_ptr[i + 1] - kb;   // at most 32 (checked by the host)
+        // the row's block columns | classes, lane kk holding block kb + kk
+        const unsigned ccl = lane < nrow ? __ldg(a.colc + kb + lane) : 0u;
+        for (int c = 0; c < nch; c++) {
+            const unsigned coff = (unsigned)(c * W + lane) * 16u;   // this lane's first packet of the chunk
+            const char* Ac = static_cast<const char*>(a.A) + coff;
+            const char* Bc = static_cast<const char*>(a.Bv) + coff;
+            char* Apc = static_cast<char*>(a.Ap) + coff;
+            char* Bpc = static_cast<char*>(a.Bp) + coff;
+            E Ai[B][EPT];   // alpha_m of the own rows, in this lane's (swapped) order
+#pragma unroll
+            for (int r = 0; r < B; r++) {
+                const uint4* src = row_at(Ac, (unsigned)(B * i + (r ^ sw)), rb);
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    Packet<E, EPP> pk;
+                    pk.u = __ldg(src + q * G);
+#pragma unroll
+                    for (int e = 0; e < EPP; e++) Ai[r][q * EPP + e] = pk.e[e];
+                }
+            }
+            typename S::Acc accA[B][EPT], accB[B][EPT];
+#pragma unroll
+            for (int r = 0; r < B; r++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) { accA[r][e] = S::zero(); accB[r][e] = S::zero(); }
+            if constexpr (kOwnAsync) {
+#pragma unroll
+                for (int r = 0; r < B; r++) {
+                    const uint4* rap = row_at(Apc, (unsigned)(B * i + (r ^ sw)), rb);
+                    const uint4* rbp = row_at(Bpc, (unsigned)(B * i + (r ^ sw)), rb);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        cp_async16(own_slot(0, r, q), rap + q * G);
+                        cp_async16(own_slot(1, r, q), rbp + q * G);
+                    }
+                }
+            }
+            unsigned ccb[2] = {0u, 0u};   // block column | class of the block in each buffer
+            // copies of block k's alpha_m / beta_{m+1} packets (and, FP32, its H entries) into buffer BF
+            auto issue = [&](int k, auto tag) {
+                constexpr int BF = decltype(tag)::value;
+                const unsigned cc = __shfl_sync(0xffffffffu, ccl, k - kb);
+                ccb[BF] = cc;
+                if constexpr (kHAhead) {
+                    constexpr int kPieces = kHBytes >= 16 ? kHBytes / 16 : 1;
+                    constexpr int kPiece = kHBytes >= 16 ? 16 : kHBytes;
+                    if (lane < kPieces)
+                        cp_async_n<kPiece>(reinterpret_cast<char*>(h_slot(BF)) + lane * kPiece,
+                                           reinterpret_cast<const char*>(hval + (size_t)k * B * B) + lane * kPiece);
+                }
+                const unsigned j = cc & kColMask;
+#pragma unroll
+                for (int bj = 0; bj < B; bj++) {
+                    const uint4* ra = row_at(Ac, B * j + (unsigned)(bj ^ sw), rb);
+                    const uint4* rbv = row_at(Bc, B * j + (unsigned)(bj ^ sw), rb);
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        cp_async16(slot(BF, 0, bj, q), ra + q * G);
+                        cp_async16(slot(BF, 1, bj, q), rbv + q * G);
+                    }
+                }
+            };
+            // one block's multiply-adds and epilogue products; IDENT: the block is a real multiple of
+            // the identity (class 2, read from its (0,0) entry), else general (real systems, or complex
+            // with class 0 or 1: a class-1 block's zero imaginary parts make the complex product exact)
+            auto body = [&](auto itag, auto btag, const H* hm, OAcc (&of)[B * B]) {
+                constexpr bool IDENT = decltype(itag)::value != 0;
+                constexpr int BF = decltype(btag)::value;
+                typename S::Hr hd;
+                H hr[B * B];
+                if constexpr (IDENT) hd = S::hreal(hm[0]);
+                else {
+#pragma unroll
+                    for (int q = 0; q < B * B; q++) hr[q] = hm[q ^ hx];   // this lane's order
+                }
+#pragma unroll
+                for (int rj = 0; rj < B; rj++) {
+                    E av[EPT], bv[EPT];
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        Packet<E, EPP> pa, pb;
+                        pa.u = *slot(BF, 0, rj, q);
+                        pb.u = *slot(BF, 1, rj, q);
+#pragma unroll
+                        for (int e = 0; e < EPP; e++) { av[q * EPP + e] = pa.e[e]; bv[q * EPP + e] = pb.e[e]; }
+                    }
+                    if constexpr (IDENT) {
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) { S::mac_re(accA[rj][e], hd, av[e]); S::mac_re(accB[rj][e], hd, bv[e]); }
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < B; r++) {
+                            const H h = hr[rj * B + r];
+                            if constexpr (S::CPLX) {
+#pragma unroll
+                                for (int e = 0; e < EPT; e++) { S::mac(accA[r][e], h, av[e]); S::mac(accB[r][e], h, bv[e]); }
+                            } else {
+#pragma unroll
+                                for (int e = 0; e < EPT; e++) { S::mac_re(accA[r][e], S::hreal(h), av[e]); S::mac_re(accB[r][e], S::hreal(h), bv[e]); }
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < B; r++)
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) S::oa_mac(of[rj * B + r], Ai[r][e], bv[e]);
+                }
+            };
+            auto block = [&](int kk, auto tag) {
+                constexpr int BF = decltype(tag)::value;
+                const int k = kb + kk;
+                if constexpr (kHAhead) __syncwarp();   // every lane is done with buffer BF ^ 1's H entries
+                if (kk + 1 < nrow) issue(k + 1, BufTag<BF ^ 1>());
+                cp_async_commit();
+                cp_async_wait<1>();   // this thread's copies of block k have landed
+                if constexpr (kHAhead) __syncwarp();   // ... and the H entries the warp's first lanes copied
+                const unsigned cc = ccb[BF];
+                const H* hm = kHAhead ? h_slot(BF) : (tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B);
+                const double2 dpre = d_prefetch<S, B>(a.Dacc, (size_t)k, own, own.writer);
+                OAcc of[B * B];
+#pragma unroll
+                for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
+                if ((cc >> 30) == 2u) body(BufTag<1>(), BufTag<BF>(), hm, of);
+                else body(BufTag<0>(), BufTag<BF>(), hm, of);
+                {
+                    // of[rj * B + r] holds D entry (bj = rj ^ sw, bi = r ^ sw)
+                    if constexpr (B == 2) {
+                        // lane ^ 16 has the other swap: its (1,1) and (1,0) slots are this lane's (0,0), (0,1)
+                        of[0] = S::oa_add(of[0], S::oa_shfl(of[3], 16));
+                        of[1] = S::oa_add(of[1], S::oa_shfl(of[2], 16));
+                        // now of[0] = (bj sw, bi sw), of[1] = (bj sw, bi sw ^ 1); lane bit 3 picks bi
+                        const bool k0 = ((lane >> 3) & 1) == sw;
+                        const OAcc keep = k0 ? of[0] : of[1];
+                        const OAcc send = k0 ? of[1] : of[0];
+                        of[0] = S::oa_add(keep, S::oa_shfl(send, 8));
+#pragma unroll
+                        for (int off = 4; off > 0; off >>= 1) of[0] = S::oa_add(of[0], S::oa_shfl(of[0], off));
+                    } else {
+                        group_sum_transposed<S, B * B>(of, G, lane);
+                    }
+                    d_write<S, B>(of, true, (size_t)k, a.dscale, dscale_ds, a.Dacc, own, dpre);
+                }
+            };
+            if constexpr (kHAhead) __syncwarp();   // the previous chunk's last block is done with its H slot
+            if (nrow > 0) issue(kb, BufTag<0>());
+            cp_async_commit();
+            int kk = 0;
+#pragma unroll 1
+            for (; kk + 2 <= nrow; kk += 2) {
+                block(kk, BufTag<0>());
+                block(kk + 1, BufTag<1>());
+            }
+            if (kk < nrow) block(kk, BufTag<0>());
+            cp_async_wait<0>();
+#pragma unroll
+            for (int r = 0; r < B; r++) {
+                E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
+                uint4* rap = const_cast<uint4*>(row_at(Apc, (unsigned)(B * i + (r ^ sw)), rb));
+                uint4* rbp = const_cast<uint4*>(row_at(Bpc, (unsigned)(B * i + (r ^ sw)), rb));
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    Packet<E, EPP> pa, pb;
+                    if constexpr (kOwnAsync) {
+                        pa.u = *own_slot(0, r, q);
+                        pb.u = *own_slot(1, r, q);
+                    } else {
+                        pa.u = rap[q * G];
+                        pb.u = rbp[q * G];
+                    }
+#pragma unroll
+                    for (int e = 0; e < EPP; e++) { apv[q * EPP + e] = pa.e[e]; bpv[q * EPP + e] = pb.e[e]; }
+                }
+#pragma unroll
+                for (int e = 0; e < EPT; e++) {
+                    an[e] = S::fin(accA[r][e], true, true, apv[e]);
+                    typename S::Acc tb = S::from(S::fin(accB[r][e], true, true, bpv[e]));
+                    S::axpy(tb, cA, Ai[r][e]);
+                    S::axpy(tb, cAp, apv[e]);
+                    S::axpy(tb, cAn, an[e]);
+                    bn[e] = S::to(tb);
+                }
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    Packet<E, EPP> pa, pb;
+#pragma unroll
+                    for (int e = 0; e < EPP; e++) { pa.e[e] = an[q * EPP + e]; pb.e[e] = bn[q * EPP + e]; }
+                    rap[q * G] = pa.u;
+                    rbp[q * G] = pb.u;
+                }
+            }
+        }
+    }
+}
+
 }  // namespace fk

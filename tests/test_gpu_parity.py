@@ -186,6 +186,7 @@ def test_two_pass_adjoint_equals_one_pass(gpu, prec, S):
 def test_pipelined_step_equals_plain(gpu, prec, cplx, S):
     # k_cheb_step_pipe and k_adjoint_pipe (gathers double-buffered through shared memory) do the
     # plain kernels' arithmetic in the same order: identical moments and D, whole and ragged chunks
+    # (the warp-per-row reverse step, which rows of 32 lanes would otherwise take, has its own test)
     if cplx:
         H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=13)
         R = fk.probe_uncorrelated(H.n_rows * H.b_len, S, fk.RNG(13), complex_values=True)
@@ -195,7 +196,7 @@ def test_pipelined_step_equals_plain(gpu, prec, cplx, S):
     c = W.fermi_coefficients(M, es, "fermi_energy")
     for kind in ("autodiff", "stoch"):
         plain = run_pair(H, es, R, cplx, prec, M, c, kind, {L.FK_OPT_PIPE: 0})
-        piped = run_pair(H, es, R, cplx, prec, M, c, kind, {L.FK_OPT_PIPE: 1})
+        piped = run_pair(H, es, R, cplx, prec, M, c, kind, {L.FK_OPT_PIPE: 1, L.FK_OPT_WARP_ROWS: 0})
         assert np.array_equal(plain[0], piped[0]) and np.array_equal(plain[2], piped[2])
         assert mu_err(piped[0], piped[1]) <= TOL_MU[prec]
 
@@ -535,3 +536,30 @@ def test_acc64_option_reads_back(gpu):
     with pytest.raises(L.FkError):
         eng.set_option(L.FK_OPT_ACC64, 2)
     eng.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32"])
+@pytest.mark.parametrize("opts", [{L.FK_OPT_ACC64: 1}, {L.FK_OPT_ACC64: 0}, {L.FK_OPT_FUSE_D: 0}])
+def test_warp_row_adjoint_against_general(gpu, prec, opts):
+    # b=2 complex rows with S=256 columns are served by a whole warp (32 lanes, whole chunks):
+    # the FP32 reverse step runs k_adjoint_warp by default (FK_OPT_WARP_ROWS 1) and k_adjoint_pipe
+    # with the option off. Same moments (the forward step is shared); D within the engine's
+    # tolerance of the oracle, and within FP32 rounding (1e-5, Frobenius) of the general kernel
+    H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=17)
+    R = fk.probe_uncorrelated(H.n_rows * H.b_len, 256, fk.RNG(17), complex_values=True)
+    M = 24
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    warp = run_pair(H, es, R, True, prec, M, c, "autodiff", dict(opts))
+    general = run_pair(H, es, R, True, prec, M, c, "autodiff", {**opts, L.FK_OPT_WARP_ROWS: 0})
+    assert np.array_equal(warp[0], general[0])
+    assert mu_err(warp[0], warp[1]) <= TOL_MU[prec]
+    assert rel_err(warp[2], warp[3]) <= TOL_D[prec]
+    assert rel_err(warp[2], general[2]) <= 1e-5
+    for p, want in [("fp32", 1), ("ds", 0), ("fp64", 0)]:   # float-float and FP64 keep their kernels
+        eng = fk.Engine(True, p)
+        eng.set_H(H, es)
+        eng.set_R(R)
+        assert eng.get_option(L.FK_OPT_WARP_ROWS) == want
+        eng.set_option(L.FK_OPT_WARP_ROWS, 0)
+        assert eng.get_option(L.FK_OPT_WARP_ROWS) == 0
+        eng.close()
