@@ -691,42 +691,66 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
 
 // ---------------------------------------------------------------------------------
 // The FP32 reverse step for block rows served by a whole warp (Gp == 32) whose column chunks
-// are all whole: the shape of wide probe blocks (b=2 complex, S >= 128). Same
-// recursions, epilogue and double-buffered gathers as k_adjoint_pipe; the fixed shape lets it
-// drop per-block work that the general kernel spends on lanes of differing rows:
-//  * lane and packet offsets are compile-time (packet q of a lane sits 32 packets after q-1),
-//    and row addresses are one 32 x 32 -> 64-bit multiply-add each;
-//  * every lane of a warp walks the same row, so there is no per-block "row has block kk" test,
-//    no zero fill of missing blocks and no warp-wide maximum of the row lengths; the row's block
-//    columns are read once, one per lane (rows of at most 32 blocks), and passed by shuffles;
-//  * the block loop is unrolled by two, so the shared-memory buffers alternate at compile time;
-//    in FP32 the next block's H entries travel with its packets (a cp.async by the warp's first
-//    lanes into a per-warp shared slot of each buffer) instead of in registers;
+// are all whole: the shape of wide probe blocks (b=2 complex, S >= 128). Same recursions and
+// fused D epilogue as k_adjoint_pipe, organised around the fixed shape:
+//  * a warp walks one row as a stream of units, chunk by chunk: A (the own alpha_m rows of the
+//    chunk), K (one H block: its alpha_m / beta_{m+1} rows, H entries and D entries) for each of
+//    the row's blocks, then O (the own alpha_{m+1} / beta_{m+2} rows: the chunk's final update);
+//  * every unit's data arrives by cp.async in a ring of three shared-memory slots, issued two units
+//    ahead, so two units' copies are in flight while one is computed, also across chunk ends
+//    (the general kernel keeps one block ahead and drains at every chunk end);
+//  * lane and packet offsets are compile-time (packet q of a lane sits 32 packets after q-1), row
+//    addresses are one 32 x 32 -> 64-bit multiply-add; the row's block columns are read once, one
+//    per lane (rows of at most 32 blocks, checked by the host), and passed by shuffles;
+//  * every lane of a warp walks the same row: no per-block "row has block kk" test, no zero fill;
+//    one class branch and one read of the H entries per block;
 //  * b=2: a lane whose bit 4 is set (sw = 1) holds every block index swapped -- gathered rows
 //    b j + (bj ^ sw), own rows b i + (bi ^ sw), accumulators and H entries permuted to match --
 //    so the two D entries it sends at the first transposed reduction level are exactly the two
 //    its partner (lane ^ 16, the other swap) keeps, and that level needs no selects.
 // It runs with the fused D epilogue only (D's pattern is H's). Results equal k_adjoint_pipe's up to
-// the order of the two bj terms of a general block in the swapped lanes (FP32/float-float
-// rounding), and the same lanes write the same D entries.
+// the order of the two bj terms of a general block in the swapped lanes (FP32 rounding), and the
+// same lanes write the same D entries.
 // ---------------------------------------------------------------------------------
 template <int V>
 struct BufTag { static constexpr int value = V; };
 
-__device__ __forceinline__ const uint4* row_at(const void* base, unsigned row, unsigned row_bytes) {
-    return reinterpret_cast<const uint4*>(static_cast<const char*>(base) + (unsigned long long)row * row_bytes);
-}
+constexpr int kRing = 3;          // shared-memory slots of the unit stream
+constexpr int kWarpSlotBytes = 96;   // per warp and slot: H block (32 B) + the 4 writer lanes' D entries (16 B each)
 
-// Shared memory of k_adjoint_warp after the H stage: the pipe kernel's slots, then two per-warp H
-// blocks (FP32) of up to 32 bytes each.
+// Shared memory of k_adjoint_warp after the H stage: kRing slots of 2 vectors x B rows x NP packets
+// per thread, then the per-warp H / D slots.
 __host__ __device__ inline size_t adj_warp_smem_bytes(int B, int NP) {
-    return adj_pipe_smem_bytes(B, NP) + (size_t)(kThreads / 32) * 2 * 32;
+    return (size_t)kRing * 2 * B * NP * kThreads * 16 + (size_t)(kThreads / 32) * kRing * kWarpSlotBytes;
 }
 // cp.async of N = 4, 8 or 16 bytes (N < 16 goes through L1: the .cg form moves 16 bytes only)
 template <int N>
 __device__ __forceinline__ void cp_async_n(void* dst, const void* src) {
     if constexpr (N == 16) cp_async16(dst, src);
     else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(N) : "memory");
+}
+// 16-byte cp.async with compile-time offsets on both addresses (folded into the instruction)
+template <int DOFF, int SOFF>
+__device__ __forceinline__ void cp_async16_at(unsigned dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0+%2], [%1+%3], 16;" ::"r"(dst), "l"(src), "n"(DOFF), "n"(SOFF) : "memory");
+}
+// 16-byte cp.async issued only where `on` holds: a predicated instruction, no branch
+__device__ __forceinline__ void cp_async16_if(unsigned dst, const void* src, bool on) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %2, 0;\n\t@p cp.async.cg.shared.global [%0], [%1], 16;\n\t}\n"
+        ::"r"(dst), "l"(src), "r"((int)on)
+        : "memory");
+}
+// compile-time loop: f(BufTag<I>()) for I in [I0, N)
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (I < N) {
+        f(BufTag<I>());
+        static_for<I + 1, N>(f);
+    }
+}
+__device__ __forceinline__ const uint4* row_at(const void* base, unsigned row, unsigned row_bytes) {
+    return reinterpret_cast<const uint4*>(static_cast<const char*>(base) + (unsigned long long)row * row_bytes);
 }
 
 template <class S, int B, int NP>
@@ -738,21 +762,27 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
     constexpr int EPT = NP * EPP;
     constexpr int G = 32;            // lanes per block row
     constexpr int W = G * NP;        // packets per column chunk
-    constexpr bool kHAhead = S::PREC == 1;     // FP32: H entries copied a block ahead (not staged per tile)
     constexpr int kHBytes = B * B * (int)sizeof(H);
-    static_assert(!kHAhead || kHBytes <= 32, "per-warp H slot holds 32 bytes");
-    constexpr bool kOwnAsync = S::PREC == 1;   // FP32: own rows copied at the start of each chunk
+    constexpr int kDBytes = S::CPLX ? 16 : 8;   // one D entry of the accumulator (8 bytes per real)
+    static_assert(kHBytes <= 32 && B * B * kDBytes <= 64, "per-warp slot sizes");
     extern __shared__ __align__(16) unsigned char smem[];
-    H* s_h = reinterpret_cast<H*>(smem);
-    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
     uint4* sbuf = reinterpret_cast<uint4*>(smem + ((sizeof(H) * B * B + sizeof(unsigned)) * (size_t)a.stage_cap + 15) / 16 * 16);
     uint4* const mine = sbuf + threadIdx.x;
-    // thread-minor slots (same layout as k_adjoint_pipe): (buffer, vector v, bj, q) and own (v, bi, q)
-    auto slot = [&](int buf, int v, int bj, int q) -> uint4* { return mine + (((buf * 2 + v) * B + bj) * NP + q) * kThreads; };
-    auto own_slot = [&](int v, int bi, int q) -> uint4* { return mine + ((4 * B + v * B + bi) * NP + q) * kThreads; };
-    // per-warp H block of buffer `buf` (FP32)
-    H* const wh = reinterpret_cast<H*>(sbuf + (size_t)6 * B * NP * kThreads) + (threadIdx.x >> 5) * 2 * (32 / sizeof(H));
-    auto h_slot = [&](int buf) -> H* { return wh + buf * (32 / sizeof(H)); };
+    // thread-minor ring slots: (slot, vector v, row r, packet q)
+    auto slot = [&](int sl, int v, int r, int q) -> uint4* { return mine + (((sl * 2 + v) * B + r) * NP + q) * kThreads; };
+    unsigned char* const wbase = reinterpret_cast<unsigned char*>(sbuf + (size_t)kRing * 2 * B * NP * kThreads) +
+                                 (threadIdx.x >> 5) * kRing * kWarpSlotBytes;
+    // the same places as 32-bit shared addresses, and the strides of the ring slots (bytes)
+    const unsigned s_mine = smem_addr(mine), s_warp = smem_addr(wbase);
+    constexpr int kQStride = kThreads * 16, kRowStride = NP * kQStride, kVecStride = B * kRowStride;
+    constexpr unsigned kSlotStride = 2u * kVecStride;
+    // complex b=2: the H block is kHP whole 16-byte pieces and a D entry is 16 bytes, so one predicated
+    // copy per lane fetches both (lanes 0-1 H, lanes 2-5 the four D entries)
+    constexpr int kHP = kHBytes / 16;
+    constexpr bool kFast = kHBytes % 16 == 0 && kDBytes == 16 && kHP + B * B <= 32;
+    // complex b=2 (FP32: OAcc is a float pair): the last reduction levels split real and imaginary parts
+    constexpr bool kCompSplit = kFast && B == 2 && sizeof(OAcc) == 8;
+    auto h_slot = [&](int sl) -> const H* { return reinterpret_cast<const H*>(wbase + sl * kWarpSlotBytes); };
 
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
@@ -771,208 +801,240 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
     const Owner own = transposed_owner<B * B>(G, lane);
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
-        const Tile tl = tile_range(a.row_ptr, sd, t0, items, G, a.stage_cap);
-        if (tl.staged) {
-            __syncthreads();
-            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
-            __syncthreads();
-        }
         const long long t = t0 + threadIdx.x;
-        if (t >= items) continue;   // items is a multiple of 32: whole warps leave together
+        if (t >= items) continue;   // items is a multiple of 32: whole warps leave together (no CTA barrier here)
         const int i = sd.row_base + (int)(t >> 5);
         const int kb = a.row_ptr[i];
-        const int nrow = a.row_ptr[i + 1] - kb;   // at most 32 (checked by the host)
-        // the row's block columns | classes, lane kk holding block kb + kk
-        const unsigned ccl = lane < nrow ? __ldg(a.colc + kb + lane) : 0u;
-        for (int c = 0; c < nch; c++) {
-            const unsigned coff = (unsigned)(c * W + lane) * 16u;   // this lane's first packet of the chunk
-            const char* Ac = static_cast<const char*>(a.A) + coff;
-            const char* Bc = static_cast<const char*>(a.Bv) + coff;
-            char* Apc = static_cast<char*>(a.Ap) + coff;
-            char* Bpc = static_cast<char*>(a.Bp) + coff;
-            E Ai[B][EPT];   // alpha_m of the own rows, in this lane's (swapped) order
-#pragma unroll
-            for (int r = 0; r < B; r++) {
-                const uint4* src = row_at(Ac, (unsigned)(B * i + (r ^ sw)), rb);
-#pragma unroll
-                for (int q = 0; q < NP; q++) {
-                    Packet<E, EPP> pk;
-                    pk.u = __ldg(src + q * G);
-#pragma unroll
-                    for (int e = 0; e < EPP; e++) Ai[r][q * EPP + e] = pk.e[e];
-                }
-            }
-            typename S::Acc accA[B][EPT], accB[B][EPT];
-#pragma unroll
-            for (int r = 0; r < B; r++)
-#pragma unroll
-                for (int e = 0; e < EPT; e++) { accA[r][e] = S::zero(); accB[r][e] = S::zero(); }
-            if constexpr (kOwnAsync) {
-#pragma unroll
-                for (int r = 0; r < B; r++) {
-                    const uint4* rap = row_at(Apc, (unsigned)(B * i + (r ^ sw)), rb);
-                    const uint4* rbp = row_at(Bpc, (unsigned)(B * i + (r ^ sw)), rb);
-#pragma unroll
-                    for (int q = 0; q < NP; q++) {
-                        cp_async16(own_slot(0, r, q), rap + q * G);
-                        cp_async16(own_slot(1, r, q), rbp + q * G);
-                    }
-                }
-            }
-            unsigned ccb[2] = {0u, 0u};   // block column | class of the block in each buffer
-            // copies of block k's alpha_m / beta_{m+1} packets (and, FP32, its H entries) into buffer BF
-            auto issue = [&](int k, auto tag) {
-                constexpr int BF = decltype(tag)::value;
-                const unsigned cc = __shfl_sync(0xffffffffu, ccl, k - kb);
-                ccb[BF] = cc;
-                if constexpr (kHAhead) {
+        const int nrow = a.row_ptr[i + 1] - kb;   // at most 32
+        const unsigned ccl = lane < nrow ? __ldg(a.colc + kb + lane) : 0u;   // lane kk: block kb + kk
+        const int per = nrow + 2;                  // units per chunk: A, K x nrow, O
+        const int U = nch * per;
+
+        // ---- issue: put unit (ic, ir) in flight into ring slot sl (one commit group per unit)
+        auto issue = [&](int ic, int ir, int sl) {
+            const unsigned coff = (unsigned)(ic * W + lane) * 16u;
+            const unsigned sdst = s_mine + (unsigned)sl * kSlotStride;   // this thread's part of slot sl
+            // the B x NP packets of vector V (slot part) from the rows b r0 + (r ^ sw) of `base`
+            auto rows = [&](auto vt, const void* base, unsigned r0) {
+                constexpr int V = decltype(vt)::value;
+                static_for<0, B>([&](auto rt) {
+                    constexpr int R = decltype(rt)::value;
+                    const uint4* src = row_at(static_cast<const char*>(base) + coff, (unsigned)(B * r0 + (R ^ sw)), rb);
+                    static_for<0, NP>([&](auto qt) {
+                        constexpr int Q = decltype(qt)::value;
+                        cp_async16_at<V * kVecStride + R * kRowStride + Q * kQStride, Q * G * 16>(sdst, src);
+                    });
+                });
+            };
+            if (ir == 0) {                 // A: alpha_m own rows
+                rows(BufTag<0>(), a.A, (unsigned)i);
+            } else if (ir == per - 1) {    // O: alpha_{m+1}, beta_{m+2} own rows
+                rows(BufTag<0>(), a.Ap, (unsigned)i);
+                rows(BufTag<1>(), a.Bp, (unsigned)i);
+            } else {                       // K: block kb + kk
+                const int kk = ir - 1;
+                const int k = kb + kk;
+                const unsigned cc = __shfl_sync(0xffffffffu, ccl, kk);
+                const unsigned j = cc & kColMask;
+                const unsigned ws = s_warp + (unsigned)sl * kWarpSlotBytes;
+                if constexpr (kFast) {
+                    // lanes 0 .. kHP-1: the H block's 16-byte pieces; lanes kHP .. kHP+B*B-1: the D
+                    // entries of the block (one per writer lane, read back by it)
+                    const bool hl = lane < kHP;
+                    const int dl = lane - kHP;
+                    const bool dlane = dl >= 0 && dl < B * B;
+                    const char* src = hl ? reinterpret_cast<const char*>(hval + (size_t)k * B * B) + lane * 16
+                                         : reinterpret_cast<const char*>(a.Dacc + ((size_t)k * B * B + (dlane ? dl : 0)) * 2);
+                    cp_async16_if(hl ? ws + lane * 16 : ws + 32 + dl * 16, src, hl || dlane);
+                } else {
                     constexpr int kPieces = kHBytes >= 16 ? kHBytes / 16 : 1;
                     constexpr int kPiece = kHBytes >= 16 ? 16 : kHBytes;
+                    unsigned char* wsp = wbase + sl * kWarpSlotBytes;
                     if (lane < kPieces)
-                        cp_async_n<kPiece>(reinterpret_cast<char*>(h_slot(BF)) + lane * kPiece,
-                                           reinterpret_cast<const char*>(hval + (size_t)k * B * B) + lane * kPiece);
+                        cp_async_n<kPiece>(wsp + lane * kPiece, reinterpret_cast<const char*>(hval + (size_t)k * B * B) + lane * kPiece);
+                    if (own.writer)   // the D entry this lane will update
+                        cp_async_n<kDBytes>(wsp + 32 + own.first * kDBytes,
+                                            a.Dacc + ((size_t)k * B * B + own.first) * (S::CPLX ? 2 : 1));
                 }
-                const unsigned j = cc & kColMask;
+                rows(BufTag<0>(), a.A, j);
+                rows(BufTag<1>(), a.Bv, j);
+            }
+            cp_async_commit();
+        };
+
+        E Ai[B][EPT];   // alpha_m of the own rows (this lane's order), for the current chunk
+        typename S::Acc accA[B][EPT], accB[B][EPT];
+        // one block's multiply-adds and epilogue products from ring slot sl; IDENT: a real multiple
+        // of the identity (class 2, read from its (0,0) entry), else general (real systems, or complex
+        // with class 0 or 1: a class-1 block's zero imaginary parts make the complex product exact)
+        auto body = [&](auto itag, int sl, OAcc (&of)[B * B]) {
+            constexpr bool IDENT = decltype(itag)::value != 0;
+            const H* hm = h_slot(sl);
+            typename S::Hr hd;
+            H hr[B * B];
+            if constexpr (IDENT) hd = S::hreal(hm[0]);
+            else {
 #pragma unroll
-                for (int bj = 0; bj < B; bj++) {
-                    const uint4* ra = row_at(Ac, B * j + (unsigned)(bj ^ sw), rb);
-                    const uint4* rbv = row_at(Bc, B * j + (unsigned)(bj ^ sw), rb);
+                for (int q = 0; q < B * B; q++) hr[q] = hm[q ^ hx];   // this lane's order
+            }
 #pragma unroll
-                    for (int q = 0; q < NP; q++) {
-                        cp_async16(slot(BF, 0, bj, q), ra + q * G);
-                        cp_async16(slot(BF, 1, bj, q), rbv + q * G);
-                    }
+            for (int rj = 0; rj < B; rj++) {
+                E av[EPT], bv[EPT];
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    Packet<E, EPP> pa, pb;
+                    pa.u = *slot(sl, 0, rj, q);
+                    pb.u = *slot(sl, 1, rj, q);
+#pragma unroll
+                    for (int e = 0; e < EPP; e++) { av[q * EPP + e] = pa.e[e]; bv[q * EPP + e] = pb.e[e]; }
                 }
-            };
-            // one block's multiply-adds and epilogue products; IDENT: the block is a real multiple of
-            // the identity (class 2, read from its (0,0) entry), else general (real systems, or complex
-            // with class 0 or 1: a class-1 block's zero imaginary parts make the complex product exact)
-            auto body = [&](auto itag, auto btag, const H* hm, OAcc (&of)[B * B]) {
-                constexpr bool IDENT = decltype(itag)::value != 0;
-                constexpr int BF = decltype(btag)::value;
-                typename S::Hr hd;
-                H hr[B * B];
-                if constexpr (IDENT) hd = S::hreal(hm[0]);
-                else {
+                if constexpr (IDENT) {
 #pragma unroll
-                    for (int q = 0; q < B * B; q++) hr[q] = hm[q ^ hx];   // this lane's order
-                }
+                    for (int e = 0; e < EPT; e++) { S::mac_re(accA[rj][e], hd, av[e]); S::mac_re(accB[rj][e], hd, bv[e]); }
+                } else {
 #pragma unroll
-                for (int rj = 0; rj < B; rj++) {
-                    E av[EPT], bv[EPT];
+                    for (int r = 0; r < B; r++) {
+                        const H h = hr[rj * B + r];
+                        if constexpr (S::CPLX) {
 #pragma unroll
-                    for (int q = 0; q < NP; q++) {
-                        Packet<E, EPP> pa, pb;
-                        pa.u = *slot(BF, 0, rj, q);
-                        pb.u = *slot(BF, 1, rj, q);
+                            for (int e = 0; e < EPT; e++) { S::mac(accA[r][e], h, av[e]); S::mac(accB[r][e], h, bv[e]); }
+                        } else {
 #pragma unroll
-                        for (int e = 0; e < EPP; e++) { av[q * EPP + e] = pa.e[e]; bv[q * EPP + e] = pb.e[e]; }
-                    }
-                    if constexpr (IDENT) {
-#pragma unroll
-                        for (int e = 0; e < EPT; e++) { S::mac_re(accA[rj][e], hd, av[e]); S::mac_re(accB[rj][e], hd, bv[e]); }
-                    } else {
-#pragma unroll
-                        for (int r = 0; r < B; r++) {
-                            const H h = hr[rj * B + r];
-                            if constexpr (S::CPLX) {
-#pragma unroll
-                                for (int e = 0; e < EPT; e++) { S::mac(accA[r][e], h, av[e]); S::mac(accB[r][e], h, bv[e]); }
-                            } else {
-#pragma unroll
-                                for (int e = 0; e < EPT; e++) { S::mac_re(accA[r][e], S::hreal(h), av[e]); S::mac_re(accB[r][e], S::hreal(h), bv[e]); }
-                            }
+                            for (int e = 0; e < EPT; e++) { S::mac_re(accA[r][e], S::hreal(h), av[e]); S::mac_re(accB[r][e], S::hreal(h), bv[e]); }
                         }
                     }
-#pragma unroll
-                    for (int r = 0; r < B; r++)
-#pragma unroll
-                        for (int e = 0; e < EPT; e++) S::oa_mac(of[rj * B + r], Ai[r][e], bv[e]);
                 }
-            };
-            auto block = [&](int kk, auto tag) {
-                constexpr int BF = decltype(tag)::value;
-                const int k = kb + kk;
-                if constexpr (kHAhead) __syncwarp();   // every lane is done with buffer BF ^ 1's H entries
-                if (kk + 1 < nrow) issue(k + 1, BufTag<BF ^ 1>());
-                cp_async_commit();
-                cp_async_wait<1>();   // this thread's copies of block k have landed
-                if constexpr (kHAhead) __syncwarp();   // ... and the H entries the warp's first lanes copied
-                const unsigned cc = ccb[BF];
-                const H* hm = kHAhead ? h_slot(BF) : (tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B);
-                const double2 dpre = d_prefetch<S, B>(a.Dacc, (size_t)k, own, own.writer);
+#pragma unroll
+                for (int r = 0; r < B; r++)
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) S::oa_mac(of[rj * B + r], Ai[r][e], bv[e]);
+            }
+        };
+
+        issue(0, 0, 0);
+        issue(0, 1, 1);                           // per >= 2: unit 1 is (chunk 0, position 1)
+        int pc = 0, pr = 0;                       // the unit being processed: chunk, position
+        int ic = 2 / per, ir = 2 % per;           // the next unit to issue
+        int sl = 0;                               // its ring slot: u % kRing
+#pragma unroll 1
+        for (int u = 0; u < U; u++) {
+            const int sl_next = sl == 0 ? 2 : sl - 1;   // (u + 2) % kRing
+            __syncwarp();   // every lane is done with unit u - 1, whose slot unit u + 2 takes
+            if (u + 2 < U) {
+                issue(ic, ir, sl_next);
+                if (++ir == per) { ir = 0; ic++; }
+            } else {
+                cp_async_commit();   // one group per unit keeps the wait count fixed
+            }
+            cp_async_wait<2>();   // unit u's copies have landed (units u + 1, u + 2 may be in flight)
+            __syncwarp();         // ... and those of the warp's shared H / D entries, copied by other lanes
+            if (pr == 0) {        // A: the chunk's alpha_m rows; accumulators start
+#pragma unroll
+                for (int r = 0; r < B; r++) {
+#pragma unroll
+                    for (int q = 0; q < NP; q++) {
+                        Packet<E, EPP> pa;
+                        pa.u = *slot(sl, 0, r, q);
+#pragma unroll
+                        for (int e = 0; e < EPP; e++) Ai[r][q * EPP + e] = pa.e[e];
+                    }
+#pragma unroll
+                    for (int e = 0; e < EPT; e++) { accA[r][e] = S::zero(); accB[r][e] = S::zero(); }
+                }
+            } else if (pr < per - 1) {   // K: block kb + pr - 1
+                const int k = kb + pr - 1;
+                const unsigned cc = __shfl_sync(0xffffffffu, ccl, pr - 1);
                 OAcc of[B * B];
 #pragma unroll
                 for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
-                if ((cc >> 30) == 2u) body(BufTag<1>(), BufTag<BF>(), hm, of);
-                else body(BufTag<0>(), BufTag<BF>(), hm, of);
-                {
-                    // of[rj * B + r] holds D entry (bj = rj ^ sw, bi = r ^ sw)
-                    if constexpr (B == 2) {
-                        // lane ^ 16 has the other swap: its (1,1) and (1,0) slots are this lane's (0,0), (0,1)
-                        of[0] = S::oa_add(of[0], S::oa_shfl(of[3], 16));
-                        of[1] = S::oa_add(of[1], S::oa_shfl(of[2], 16));
-                        // now of[0] = (bj sw, bi sw), of[1] = (bj sw, bi sw ^ 1); lane bit 3 picks bi
-                        const bool k0 = ((lane >> 3) & 1) == sw;
-                        const OAcc keep = k0 ? of[0] : of[1];
-                        const OAcc send = k0 ? of[1] : of[0];
-                        of[0] = S::oa_add(keep, S::oa_shfl(send, 8));
+                if ((cc >> 30) == 2u) body(BufTag<1>(), sl, of);
+                else body(BufTag<0>(), sl, of);
+                // of[rj * B + r] holds D entry (bj = rj ^ sw, bi = r ^ sw)
+                if constexpr (B == 2) {
+                    // lane ^ 16 has the other swap: its (1,1) and (1,0) slots are this lane's (0,0), (0,1)
+                    of[0] = S::oa_add(of[0], S::oa_shfl(of[3], 16));
+                    of[1] = S::oa_add(of[1], S::oa_shfl(of[2], 16));
+                    // now of[0] = (bj sw, bi sw), of[1] = (bj sw, bi sw ^ 1); lane bit 3 picks bi
+                    const bool k0 = ((lane >> 3) & 1) == sw;
+                    const OAcc keep = k0 ? of[0] : of[1];
+                    const OAcc send = k0 ? of[1] : of[0];
+                    of[0] = S::oa_add(keep, S::oa_shfl(send, 8));
+                    if constexpr (kCompSplit) {
+                        // third level: lane bit 2 picks the real (0) or imaginary (1) part, so each of the
+                        // 8 writer lanes (lane & 3 == 0) finishes and stores one real of the block
+                        const bool im = (lane >> 2) & 1;
+                        const float kp = im ? of[0].y : of[0].x;
+                        const float sd = im ? of[0].x : of[0].y;
+                        float v = kp + __shfl_xor_sync(0xffffffffu, sd, 4);
+                        v += __shfl_xor_sync(0xffffffffu, v, 2);
+                        v += __shfl_xor_sync(0xffffffffu, v, 1);
+                        if ((lane & 3) == 0) {
+                            const int ent = sw * 2 + ((lane >> 3) & 1);   // entry bj * 2 + bi
+                            const size_t q = ((size_t)k * B * B + ent) * 2 + (im ? 1 : 0);
+                            const unsigned char* dp = wbase + sl * kWarpSlotBytes + 32 + ent * 16 + (im ? 8 : 0);
+                            if constexpr (S::DACC_DS) {
+                                float2 cur = *reinterpret_cast<const float2*>(dp);
+                                ds_mac(cur, dscale_ds, make_float2(v, 0.f));
+                                reinterpret_cast<float2*>(a.Dacc)[q] = ds_norm(cur);
+                            } else {
+                                a.Dacc[q] = *reinterpret_cast<const double*>(dp) + a.dscale * (double)v;
+                            }
+                        }
+                    } else {
 #pragma unroll
                         for (int off = 4; off > 0; off >>= 1) of[0] = S::oa_add(of[0], S::oa_shfl(of[0], off));
-                    } else {
-                        group_sum_transposed<S, B * B>(of, G, lane);
                     }
-                    d_write<S, B>(of, true, (size_t)k, a.dscale, dscale_ds, a.Dacc, own, dpre);
+                } else {
+                    group_sum_transposed<S, B * B>(of, G, lane);
                 }
-            };
-            if constexpr (kHAhead) __syncwarp();   // the previous chunk's last block is done with its H slot
-            if (nrow > 0) issue(kb, BufTag<0>());
-            cp_async_commit();
-            int kk = 0;
-#pragma unroll 1
-            for (; kk + 2 <= nrow; kk += 2) {
-                block(kk, BufTag<0>());
-                block(kk + 1, BufTag<1>());
-            }
-            if (kk < nrow) block(kk, BufTag<0>());
-            cp_async_wait<0>();
+                if constexpr (!kCompSplit) {
+                    double2 pre = make_double2(0.0, 0.0);
+                    if (own.writer) {   // the D entry, copied with the unit (by lane kHP + first in the fast form)
+                        const unsigned char* dp = wbase + sl * kWarpSlotBytes + 32 + own.first * kDBytes;
+                        if constexpr (S::CPLX) pre = *reinterpret_cast<const double2*>(dp);
+                        else pre.x = *reinterpret_cast<const double*>(dp);
+                    }
+                    d_write<S, B>(of, true, (size_t)k, a.dscale, dscale_ds, a.Dacc, own, pre);
+                }
+            } else {   // O: alpha_{m-1} and beta_m of the chunk
+                const unsigned coff = (unsigned)(pc * W + lane) * 16u;
 #pragma unroll
-            for (int r = 0; r < B; r++) {
-                E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
-                uint4* rap = const_cast<uint4*>(row_at(Apc, (unsigned)(B * i + (r ^ sw)), rb));
-                uint4* rbp = const_cast<uint4*>(row_at(Bpc, (unsigned)(B * i + (r ^ sw)), rb));
+                for (int r = 0; r < B; r++) {
+                    E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
 #pragma unroll
-                for (int q = 0; q < NP; q++) {
-                    Packet<E, EPP> pa, pb;
-                    if constexpr (kOwnAsync) {
-                        pa.u = *own_slot(0, r, q);
-                        pb.u = *own_slot(1, r, q);
-                    } else {
-                        pa.u = rap[q * G];
-                        pb.u = rbp[q * G];
+                    for (int q = 0; q < NP; q++) {
+                        Packet<E, EPP> pa, pb;
+                        pa.u = *slot(sl, 0, r, q);
+                        pb.u = *slot(sl, 1, r, q);
+#pragma unroll
+                        for (int e = 0; e < EPP; e++) { apv[q * EPP + e] = pa.e[e]; bpv[q * EPP + e] = pb.e[e]; }
                     }
 #pragma unroll
-                    for (int e = 0; e < EPP; e++) { apv[q * EPP + e] = pa.e[e]; bpv[q * EPP + e] = pb.e[e]; }
-                }
+                    for (int e = 0; e < EPT; e++) {
+                        an[e] = S::fin(accA[r][e], true, true, apv[e]);
+                        typename S::Acc tb = S::from(S::fin(accB[r][e], true, true, bpv[e]));
+                        S::axpy(tb, cA, Ai[r][e]);
+                        S::axpy(tb, cAp, apv[e]);
+                        S::axpy(tb, cAn, an[e]);
+                        bn[e] = S::to(tb);
+                    }
+                    uint4* rap = const_cast<uint4*>(row_at(static_cast<char*>(a.Ap) + coff, (unsigned)(B * i + (r ^ sw)), rb));
+                    uint4* rbp = const_cast<uint4*>(row_at(static_cast<char*>(a.Bp) + coff, (unsigned)(B * i + (r ^ sw)), rb));
 #pragma unroll
-                for (int e = 0; e < EPT; e++) {
-                    an[e] = S::fin(accA[r][e], true, true, apv[e]);
-                    typename S::Acc tb = S::from(S::fin(accB[r][e], true, true, bpv[e]));
-                    S::axpy(tb, cA, Ai[r][e]);
-                    S::axpy(tb, cAp, apv[e]);
-                    S::axpy(tb, cAn, an[e]);
-                    bn[e] = S::to(tb);
-                }
+                    for (int q = 0; q < NP; q++) {
+                        Packet<E, EPP> pa, pb;
 #pragma unroll
-                for (int q = 0; q < NP; q++) {
-                    Packet<E, EPP> pa, pb;
-#pragma unroll
-                    for (int e = 0; e < EPP; e++) { pa.e[e] = an[q * EPP + e]; pb.e[e] = bn[q * EPP + e]; }
-                    rap[q * G] = pa.u;
-                    rbp[q * G] = pb.u;
+                        for (int e = 0; e < EPP; e++) { pa.e[e] = an[q * EPP + e]; pb.e[e] = bn[q * EPP + e]; }
+                        rap[q * G] = pa.u;
+                        rbp[q * G] = pb.u;
+                    }
                 }
             }
+            if (++pr == per) { pr = 0; pc++; }
+            sl = sl == kRing - 1 ? 0 : sl + 1;
         }
+        cp_async_wait<0>();
+        __syncwarp();   // the next row's first copies reuse slots the other lanes have just read
     }
 }
 
