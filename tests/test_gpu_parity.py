@@ -539,13 +539,16 @@ def test_acc64_option_reads_back(gpu):
 
 
 @pytest.mark.parametrize("prec", ["fp32"])
-@pytest.mark.parametrize("opts", [{L.FK_OPT_ACC64: 1}, {L.FK_OPT_ACC64: 0}, {L.FK_OPT_FUSE_D: 0}])
+@pytest.mark.parametrize("opts", [{L.FK_OPT_ACC64: 1}, {L.FK_OPT_ACC64: 0}, {L.FK_OPT_FUSE_D: 0},
+                                  {L.FK_OPT_CTAS_PER_SM: 1}])
 def test_warp_row_adjoint_against_general(gpu, prec, opts):
     # b=2 complex rows with S=256 columns are served by a whole warp (32 lanes, whole chunks):
     # the FP32 reverse step runs k_adjoint_warp by default (FK_OPT_WARP_ROWS 1) and k_adjoint_pipe
     # with the option off. Same moments (the forward step is shared); D within the engine's
-    # tolerance of the oracle, and within FP32 rounding (1e-5, Frobenius) of the general kernel
-    H, es, _ = W.cubic_spin_lattice(4, -1.0, 1.0, seed=17)
+    # tolerance of the oracle, and within FP32 rounding (1e-5, Frobenius) of the general kernel.
+    # L=16: 4,096 rows in 512 tiles, more than the CTAs of one wave (and 152 CTAs with one per SM),
+    # so warps walk several rows and the unit stream continues across rows
+    H, es, _ = W.cubic_spin_lattice(16, -1.0, 1.0, seed=17)
     R = fk.probe_uncorrelated(H.n_rows * H.b_len, 256, fk.RNG(17), complex_values=True)
     M = 24
     c = W.fermi_coefficients(M, es, "fermi_energy")
