@@ -513,6 +513,11 @@ int configure(fk_engine* e) {
         // 9.75 ms; FP32 1.85 vs 2.14 ms)
         c.warp = kind == fk::kAdjoint && c.pipe && e->opt_warp && e->prec == fk::kF32 && Gp == 32 &&
                  P % (32 * NP) == 0 && fk::max_row_blocks(e->h_row_ptr.data(), e->n_b) <= 32;
+        // FP64 b=2 complex: the warp-per-row step (k_adjoint_step_warp), fewer FP64-pipe additions
+        // in the D reduction
+        if (kind == fk::kAdjoint && !c.pipe && !c.split && e->opt_warp && e->prec == fk::kF64 && e->cplx &&
+            e->b == 2 && Gp == 32 && P % (32 * NP) == 0)
+            c.warp = true;
         if (c.split) c.smem += 2 * (size_t)fk::kThreads * e->b * NP * 16;   // kept alpha_{m+1}, alpha_{m-1}
         if (c.pipe) c.smem = stage_smem + (kind == fk::kStep ? fk::pipe_smem_bytes(e->b, NP)
                                            : c.warp ? fk::adj_warp_smem_bytes(e->b, NP) : fk::adj_pipe_smem_bytes(e->b, NP));
@@ -522,7 +527,7 @@ int configure(fk_engine* e) {
         }
         int occ = 0;
         const int okind = c.split ? (int)fk::kAdjointSplit
-                        : c.warp ? (int)fk::kAdjointWarp
+                        : c.warp ? (int)fk::kAdjointWarp   // (FP64: k_adjoint_step_warp)
                         : c.pipe ? (kind == fk::kStep ? (int)fk::kStepPipe : (int)fk::kAdjointPipe)
                         : !c.staged ? kind : (e->opt_tma == 1 ? (int)fk::kStepStaged : (int)fk::kStepStagedAsync);
         FK_TRY(prec_occupancy(e, okind, c.NP, c.smem, &occ), "occupancy query");

@@ -86,6 +86,12 @@ cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
         if (a.pipe) return whole ? adj_pipe_launch<S, B, NP, true>(a, l) : adj_pipe_launch<S, B, NP, false>(a, l);
     }
     if (a.split) return whole ? adj_split_launch<S, B, NP, true>(a, l) : adj_split_launch<S, B, NP, false>(a, l);
+    if constexpr (S::PREC == 0 && S::CPLX && B == 2) {   // FP64 complex rows served by a whole warp
+        if (a.warp && whole && a.Gp == 32 && a.Dacc) {
+            k_adjoint_step_warp<S, NP><<<l.grid, kThreads, l.smem, l.stream>>>(a);
+            return cudaGetLastError();
+        }
+    }
     if (whole) k_adjoint_step<S, B, NP, true><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     else k_adjoint_step<S, B, NP, false><<<l.grid, kThreads, l.smem, l.stream>>>(a);
     return cudaGetLastError();
@@ -108,7 +114,12 @@ const void* pipe_fn(int kind) {
 template <class S, int B, int NP>
 cudaError_t occ_one(int kind, size_t smem, int* n) {
     if constexpr (S::PREC == 0) {
-        if (kind == kStepPipe || kind == kAdjointPipe || kind == kAdjointWarp) return cudaErrorInvalidValue;
+        if (kind == kStepPipe || kind == kAdjointPipe) return cudaErrorInvalidValue;
+        if (kind == kAdjointWarp) {
+            if constexpr (S::CPLX && B == 2)
+                return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, (const void*)k_adjoint_step_warp<S, NP>, kThreads, smem);
+            else return cudaErrorInvalidValue;
+        }
     }
     const void* f = kind == kStep ? (const void*)k_cheb_step<S, B, NP>
                   : (kind == kStepPipe || kind == kAdjointPipe || kind == kAdjointWarp) ? pipe_fn<S, B, NP>(kind)

@@ -622,6 +622,150 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
 }
 
 // ---------------------------------------------------------------------------------
+// FP64 reverse step for block rows served by a whole warp (Gp == 32, whole chunks, fused D
+// epilogue, b=2 complex): k_adjoint_step's loads and arithmetic, with the D reduction arranged to
+// spend fewer FP64-pipe additions, the resource that bounds the FP64 engine:
+//  * a lane whose bit 4 is set (sw = 1) holds every block index swapped -- gathered rows
+//    b j + (bj ^ sw), own rows b i + (bi ^ sw), accumulators and H entries permuted to match -- so
+//    the first transposed level exchanges exactly the entries the partner keeps (no selects);
+//  * the third level splits real and imaginary parts (lane bit 2), so 8 writer lanes each finish
+//    one real of the block: 9 DADDs and one DFMA per block and chunk instead of 12 and two;
+//  * lane offsets are compile-time and every lane of the warp walks the same row (no per-block
+//    row test, no zero fill, no warp-wide maximum of the row lengths).
+// Results equal k_adjoint_step's up to the order of the two bj terms of a general block in the
+// swapped lanes (rounding), and the reduction adds the same partials in the same pairs.
+// ---------------------------------------------------------------------------------
+template <class S, int NP>
+__global__ void __launch_bounds__(kThreads, 2) k_adjoint_step_warp(AdjArgs a) {
+    typedef typename S::E E;
+    typedef typename S::H H;
+    typedef typename S::OAcc OAcc;
+    constexpr int B = 2;
+    constexpr int G = 32;
+    constexpr int EPT = NP * S::EPP;
+    static_assert(S::CPLX && S::PREC == 0, "FP64 complex systems");
+    extern __shared__ __align__(16) unsigned char smem[];
+    H* s_h = reinterpret_cast<H*>(smem);
+    unsigned* s_col = reinterpret_cast<unsigned*>(smem + sizeof(H) * B * B * (size_t)a.stage_cap);
+
+    const int sidx = a.cta_sys[blockIdx.x];
+    const SysDesc sd = a.sys[sidx];
+    const int lc = blockIdx.x - sd.cta_base;
+    const int P = a.P, W = G * NP;
+    const int nch = P / W;
+    const long long items = (long long)sd.n_b * G;
+    const E* A = reinterpret_cast<const E*>(a.A);
+    E* Ap = reinterpret_cast<E*>(a.Ap);
+    const E* Bv = reinterpret_cast<const E*>(a.Bv);
+    E* Bp = reinterpret_cast<E*>(a.Bp);
+    const H* hval = reinterpret_cast<const H*>(a.hval);
+    const typename S::Coef cA = S::coef(a.coef[sidx * a.cstride + 0]);
+    const typename S::Coef cAp = S::coef(a.coef[sidx * a.cstride + 1]);
+    const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
+    const int lane = threadIdx.x & 31;
+    const int sw = (lane >> 4) & 1;                       // block-index swap of this lane
+    const int hx = sw * 3;                                // H entry (bi, bj) -> (bi ^ sw, bj ^ sw)
+    const bool im = (lane >> 2) & 1;                      // the part this lane finishes
+    const int ent = sw * 2 + ((lane >> 3) & 1);           // the D entry (bj * 2 + bi) it finishes
+    const bool writer = (lane & 3) == 0;
+
+    for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
+        const Tile tl = tile_range(a.row_ptr, sd, t0, items, G, a.stage_cap);
+        if (tl.staged) {
+            __syncthreads();
+            stage_h<S, B>(s_col, s_h, a.colc, hval, tl.k_lo, tl.nk);
+            __syncthreads();
+        }
+        const long long t = t0 + threadIdx.x;
+        if (t >= items) continue;   // items is a multiple of 32: whole warps leave together
+        const int i = sd.row_base + (int)(t >> 5);
+        const int kb = a.row_ptr[i], ke = a.row_ptr[i + 1];
+        for (int c = 0; c < nch; c++) {
+            const int base = c * W;
+            E Ai[B][EPT];
+#pragma unroll
+            for (int r = 0; r < B; r++) ld_nc<S, NP, true>(Ai[r], A + (size_t)(B * i + (r ^ sw)) * a.ld, base, lane, G, P);
+            typename S::Acc accA[B][EPT], accB[B][EPT];
+#pragma unroll
+            for (int r = 0; r < B; r++)
+#pragma unroll
+                for (int e = 0; e < EPT; e++) { accA[r][e] = S::zero(); accB[r][e] = S::zero(); }
+            for (int k = kb; k < ke; k++) {
+                const unsigned cc = tl.staged ? s_col[k - tl.k_lo] : __ldg(a.colc + k);
+                const H* hk = tl.staged ? s_h + (size_t)(k - tl.k_lo) * B * B : hval + (size_t)k * B * B;
+                const int j = (int)(cc & kColMask);
+                const size_t dq = ((size_t)k * B * B + ent) * 2 + (im ? 1 : 0);
+                const double dpre = writer ? a.Dacc[dq] : 0.0;   // read early: used after the block's work
+                OAcc of[B * B];
+#pragma unroll
+                for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
+                const bool ident = (cc >> 30) == 2u;
+#pragma unroll
+                for (int rj = 0; rj < B; rj++) {
+                    E av[EPT], bv[EPT];
+                    ld_nc<S, NP, true>(av, A + (size_t)(B * j + (rj ^ sw)) * a.ld, base, lane, G, P);
+                    ld_nc<S, NP, true>(bv, Bv + (size_t)(B * j + (rj ^ sw)) * a.ld, base, lane, G, P);
+                    if (ident) {   // real multiple of the identity: H(0,0) = H(1,1)
+                        const typename S::Hr h = S::hreal(hk[0]);
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) { S::mac_re(accA[rj][e], h, av[e]); S::mac_re(accB[rj][e], h, bv[e]); }
+                    } else if ((cc >> 30) == 1u) {   // real entries
+#pragma unroll
+                        for (int r = 0; r < B; r++) {
+                            const typename S::Hr h = S::hreal(hk[(rj * B + r) ^ hx]);
+#pragma unroll
+                            for (int e = 0; e < EPT; e++) { S::mac_re(accA[r][e], h, av[e]); S::mac_re(accB[r][e], h, bv[e]); }
+                        }
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < B; r++) {
+                            const H h = hk[(rj * B + r) ^ hx];
+#pragma unroll
+                            for (int e = 0; e < EPT; e++) { S::mac(accA[r][e], h, av[e]); S::mac(accB[r][e], h, bv[e]); }
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < B; r++)
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) S::oa_mac(of[rj * B + r], Ai[r][e], bv[e]);
+                }
+                // of[rj * B + r] holds D entry (bj = rj ^ sw, bi = r ^ sw); lane ^ 16 has the other swap
+                of[0] = S::oa_add(of[0], S::oa_shfl(of[3], 16));
+                of[1] = S::oa_add(of[1], S::oa_shfl(of[2], 16));
+                const bool k0 = ((lane >> 3) & 1) == sw;   // lane bit 3 picks bi
+                const OAcc keep = k0 ? of[0] : of[1];
+                const OAcc send = k0 ? of[1] : of[0];
+                const OAcc e2 = S::oa_add(keep, S::oa_shfl(send, 8));
+                const double kp = im ? e2.y : e2.x;
+                const double sd2 = im ? e2.x : e2.y;
+                double v = kp + __shfl_xor_sync(0xffffffffu, sd2, 4);
+                v += __shfl_xor_sync(0xffffffffu, v, 2);
+                v += __shfl_xor_sync(0xffffffffu, v, 1);
+                if (writer) a.Dacc[dq] = dpre + a.dscale * v;
+            }
+#pragma unroll
+            for (int r = 0; r < B; r++) {
+                const size_t roff = (size_t)(B * i + (r ^ sw)) * a.ld;
+                E apv[EPT], bpv[EPT], an[EPT], bn[EPT];
+                ld_rw<S, NP, true>(apv, Ap + roff, base, lane, G, P);
+                ld_rw<S, NP, true>(bpv, Bp + roff, base, lane, G, P);
+#pragma unroll
+                for (int e = 0; e < EPT; e++) {
+                    an[e] = S::fin(accA[r][e], true, true, apv[e]);
+                    typename S::Acc tb = S::from(S::fin(accB[r][e], true, true, bpv[e]));
+                    S::axpy(tb, cA, Ai[r][e]);
+                    S::axpy(tb, cAp, apv[e]);
+                    S::axpy(tb, cAn, an[e]);
+                    bn[e] = S::to(tb);
+                }
+                st<S, NP, true>(Ap + roff, an, base, lane, G, P);
+                st<S, NP, true>(Bp + roff, bn, base, lane, G, P);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
 // The same reverse step in two passes over the row's blocks, to hold fewer values in
 // registers at a time: pass 1 gathers alpha_m and writes alpha_{m-1} (keeping alpha_{m+1}
 // and alpha_{m-1} of the thread's own rows in shared memory, which only that thread
