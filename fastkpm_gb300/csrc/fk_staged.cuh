@@ -641,9 +641,11 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
                     }
                     if (fuse) {
 #pragma unroll
-                        for (int bi = 0; bi < B; bi++)
+                        for (int bi = 0; bi < B; bi++) {   // each entry's first product starts it (of is zero): no add to zero
+                            of[bj * B + bi] = S::oa_first(Ai[bi][0], bv[0]);
 #pragma unroll
-                            for (int e = 0; e < EPT; e++) S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
+                            for (int e = 1; e < EPT; e++) S::oa_mac(of[bj * B + bi], Ai[bi][e], bv[e]);
+                        }
                     }
                 }
                 if (fuse) flush_block<S, B>(of, Gp, g, has, (size_t)k, a.dscale, dscale_ds, a.Dacc, own, dpre);
@@ -905,9 +907,11 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                     }
                 }
 #pragma unroll
-                for (int r = 0; r < B; r++)
+                for (int r = 0; r < B; r++) {   // each entry's first product starts it (of is zero): no add to zero
+                    of[rj * B + r] = S::oa_first(Ai[r][0], bv[0]);
 #pragma unroll
-                    for (int e = 0; e < EPT; e++) S::oa_mac(of[rj * B + r], Ai[r][e], bv[e]);
+                    for (int e = 1; e < EPT; e++) S::oa_mac(of[rj * B + r], Ai[r][e], bv[e]);
+                }
             }
         };
 

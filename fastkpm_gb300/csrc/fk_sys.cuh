@@ -46,6 +46,15 @@ __device__ __forceinline__ void ds_mac(float2& acc, float2 a, float2 b) {
     acc.x = s.x;
     acc.y = __fadd_rn(acc.y, __fadd_rn(s.y, e));
 }
+// a * b as an unevaluated hi + lo pair: what ds_mac gives from a zero accumulator, without the
+// error-free addition to zero (4 instead of 12 FP32 instructions)
+__device__ __forceinline__ float2 ds_mul(float2 a, float2 b) {
+    float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    return make_float2(p, e);
+}
 // acc -= a * b
 __device__ __forceinline__ void ds_msub(float2& acc, float2 a, float2 b) {
     ds_mac(acc, make_float2(-a.x, -a.y), b);
@@ -98,6 +107,7 @@ struct SysF64R {
     __device__ static double dot_get(Dot d) { return d; }
     __device__ static OAcc oa_zero() { return 0.0; }
     __device__ static void oa_mac(OAcc& o, E a, E b) { o = fma(a, b, o); }          // o += a conj(b)
+    __device__ static OAcc oa_first(E a, E b) { return a * b; }                        // a conj(b)
     __device__ static OAcc oa_shfl_add(OAcc o, int off) { return o + __shfl_xor_sync(0xffffffffu, o, off); }
     static constexpr bool DACC_DS = false;   // D accumulated in FP64
     __device__ static float2 oa_ds(OAcc, int) { return make_float2(0.f, 0.f); }
@@ -140,6 +150,9 @@ struct SysF64C {
     __device__ static void oa_mac(OAcc& o, E a, E b) {   // o += a * conj(b)
         o.x = fma(a.x, b.x, o.x); o.x = fma(a.y, b.y, o.x);
         o.y = fma(a.y, b.x, o.y); o.y = fma(-a.x, b.y, o.y);
+    }
+    __device__ static OAcc oa_first(E a, E b) {          // a * conj(b), the same roundings as oa_mac from zero
+        return make_double2(fma(a.y, b.y, a.x * b.x), fma(-a.x, b.y, a.y * b.x));
     }
     __device__ static OAcc oa_shfl_add(OAcc o, int off) {
         return make_double2(o.x + __shfl_xor_sync(0xffffffffu, o.x, off),
@@ -187,6 +200,7 @@ struct SysF32R {
     __device__ static double dot_get(Dot d) { return ds_to_double(d); }
     __device__ static OAcc oa_zero() { return 0.f; }
     __device__ static void oa_mac(OAcc& o, E a, E b) { o = fmaf(a, b, o); }
+    __device__ static OAcc oa_first(E a, E b) { return a * b; }
     __device__ static OAcc oa_shfl_add(OAcc o, int off) { return o + __shfl_xor_sync(0xffffffffu, o, off); }
     // D accumulated as float-float on the FP32 pipe (the FP64 pipe is ~1/58 of it)
     static constexpr bool DACC_DS = true;
@@ -234,6 +248,9 @@ struct SysF32C {
     __device__ static void oa_mac(OAcc& o, E a, E b) {
         o.x = fmaf(a.x, b.x, o.x); o.x = fmaf(a.y, b.y, o.x);
         o.y = fmaf(a.y, b.x, o.y); o.y = fmaf(-a.x, b.y, o.y);
+    }
+    __device__ static OAcc oa_first(E a, E b) {
+        return make_float2(fmaf(a.y, b.y, a.x * b.x), fmaf(-a.x, b.y, a.y * b.x));
     }
     __device__ static OAcc oa_shfl_add(OAcc o, int off) {
         return make_float2(o.x + __shfl_xor_sync(0xffffffffu, o.x, off),
@@ -303,6 +320,7 @@ struct SysDSR {
     __device__ static double dot_get(Dot d) { return ds_to_double(d); }
     __device__ static OAcc oa_zero() { return make_float2(0.f, 0.f); }
     __device__ static void oa_mac(OAcc& o, E a, E b) { ds_mac(o, a, b); }
+    __device__ static OAcc oa_first(E a, E b) { return ds_mul(a, b); }
     __device__ static OAcc oa_shfl_add(OAcc o, int off) {
         float2 t = make_float2(__shfl_xor_sync(0xffffffffu, o.x, off), __shfl_xor_sync(0xffffffffu, o.y, off));
         ds_add(o, t);
@@ -371,6 +389,12 @@ struct SysDSC {
         ds_mac(orr, re(a), re(b)); ds_mac(orr, im(a), im(b));
         ds_mac(oi, im(a), re(b)); ds_msub(oi, re(a), im(b));
         o = pack(orr, oi);
+    }
+    __device__ static OAcc oa_first(E a, E b) {          // a * conj(b): oa_mac from zero, first products exact
+        float2 orr = ds_mul(re(a), re(b)), oi = ds_mul(im(a), re(b));
+        ds_mac(orr, im(a), im(b));
+        ds_msub(oi, re(a), im(b));
+        return pack(orr, oi);
     }
     __device__ static OAcc oa_shfl_add(OAcc o, int off) {
         return pack(SysDSR::oa_shfl_add(re(o), off), SysDSR::oa_shfl_add(im(o), off));
