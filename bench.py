@@ -229,8 +229,8 @@ def step_flops_per_launch(H, S):
 # cubic L=32 case (65,536 rows; summarised under profiles/): traffic grows in proportion to the
 # rows, so the L=64 launch's traffic is these times N. Keys: (precision, FP64 accumulators). An
 # engine form without a capture of its current kernel reports null.
-ADJ_TRAFFIC_PER_ROW = {("fp64", 1): (1.856638e9 + 0.721797e9) / 65536,
-                       ("fp32", 1): (0.577735e9 + 0.248611e9) / 65536,
+ADJ_TRAFFIC_PER_ROW = {("fp64", 1): (1.857997e9 + 0.721861e9) / 65536,
+                       ("fp32", 1): (0.577800e9 + 0.248626e9) / 65536,
                        ("ds", 0): (1.570807e9 + 0.529550e9) / 65536}
 ADJ_WARP_INST_PER_ROW = {("ds", 0): 1108457856 / 65536}
 ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
