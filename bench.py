@@ -188,12 +188,12 @@ def h_bytes(nnzb, b, sv, n_b):
     return nnzb * (b * b * sv + 4) + 4 * (n_b + 1)
 
 
-def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused):
+def adjoint_bytes_per_launch(N, S, nnzb, b, sv, fused, cplx=True):
     """Algorithmic bytes of one adjoint launch (the kernel walks all S columns itself): read alpha_m,
     alpha_{m+1}, beta_{m+1}, beta_{m+2}, write alpha_{m-1}, beta_m (6 vectors), H once (entries +
     4-byte column index), row_ptr, and, when the D epilogue is fused, the D accumulator read + write
-    (8 bytes per real: double or float-float)."""
-    d = 2 * nnzb * b * b * 16 if fused else 0
+    (8 bytes per real: double or float-float; two reals per complex entry)."""
+    d = 2 * nnzb * b * b * (16 if cplx else 8) if fused else 0
     return 6 * N * S * sv + h_bytes(nnzb, b, sv, N // b) + d
 
 
@@ -231,8 +231,8 @@ def step_flops_per_launch(H, S):
 # engine form without a capture of its current kernel reports null.
 ADJ_TRAFFIC_PER_ROW = {("fp64", 1): (1.857997e9 + 0.721861e9) / 65536,
                        ("fp32", 1): (0.577800e9 + 0.248626e9) / 65536,
-                       ("ds", 0): (1.570807e9 + 0.529550e9) / 65536}
-ADJ_WARP_INST_PER_ROW = {("ds", 0): 1108457856 / 65536}
+                       ("ds", 0): (1.525888e9 + 0.527933e9) / 65536}
+ADJ_WARP_INST_PER_ROW = {("ds", 0): 1049737600 / 65536}
 ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
 
 
@@ -666,14 +666,26 @@ def run_batch(args):
     eng.close()
     if pinned:
         lib.fk_host_unregister(d_out.ctypes.data)
-    solve = {"what": "moments(M) + autodiff_matrix(c_sys) for all 64 systems (host wall clock, D copied out)",
-             "ms": ms_solve, "value": float(total_rows) * M * S / (ms_solve / 1e3), "unit": UNIT,
-             "sequential_fp64_ms": t_seq_solve, "speedup_vs_sequential_fp64": t_seq_solve / ms_solve,
-             "D_rel_fro_vs_fp64": d_err, "D_buffer_pinned": pinned}
     per = float(total_rows) * M * S
     bytes_step = 3 * total_rows * S * 4 + sum(s["H"].n_blocks() * 8 + 4 * (s["H"].n_rows + 1) for s in systems)
     achieved = bytes_step / (ms_b / (M // 2) * 1e-3) / 1e9
     peak, kind = peaks()
+    # the whole solve's algorithmic bytes: M/2 forward steps and M/2 - 1 fused reverse steps (b=1 real
+    # FP32, D accumulator 8 bytes per entry), over the host wall clock of moments + autodiff_matrix
+    nnzb_all = sum(s["H"].n_blocks() for s in systems)
+    bytes_adj = sum(adjoint_bytes_per_launch(s["H"].n_rows, S, s["H"].n_blocks(), 1, 4, True, cplx=False)
+                    for s in systems)
+    solve_bytes = (M // 2) * bytes_step + (M // 2 - 1) * bytes_adj
+    ach_solve = solve_bytes / (ms_solve * 1e-3) / 1e9
+    solve = {"what": "moments(M) + autodiff_matrix(c_sys) for all 64 systems (host wall clock, D copied out)",
+             "ms": ms_solve, "value": float(total_rows) * M * S / (ms_solve / 1e3), "unit": UNIT,
+             "sequential_fp64_ms": t_seq_solve, "speedup_vs_sequential_fp64": t_seq_solve / ms_solve,
+             "D_rel_fro_vs_fp64": d_err, "D_buffer_pinned": pinned,
+             "roofline_over_wall": {"bound": "hbm", "achieved": ach_solve, "peak": peak, "unit": "GB/s",
+                                    "frac": ach_solve / peak, "bytes_per_solve": solve_bytes,
+                                    "blocks": nnzb_all, "peak_source": kind,
+                                    "over": "host wall clock of the whole solve (moments graph, batched reverse "
+                                            "steps, D copied out to pinned memory)"}}
     line = {"metric": METRIC, "value": per / (ms_b / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 recursion; float-float per-thread sums, f64 across CTAs (FK_OPT_ACC64 0)",
