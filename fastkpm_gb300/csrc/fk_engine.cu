@@ -507,19 +507,19 @@ int configure(fk_engine* e) {
         c.pipe = (kind == fk::kStep && !e->opt_tma && use_pipe(e, fk::kStep, NP)) ||
                  (kind == fk::kAdjoint && use_pipe(e, fk::kAdjoint, NP));
         c.split = kind == fk::kAdjoint && !c.pipe && use_adjoint_split(e, NP);
-        // the warp-per-row kernel (FP32) keeps a row's block columns one per lane: rows of at most
-        // 32 blocks. Float-float keeps k_adjoint_pipe: its blocks' code is ~4x longer, and the warp
-        // kernel's unrolled, class-specialised copies measured slower (cubic L=64, S=256: 10.54 vs
-        // 9.75 ms; FP32 1.85 vs 2.14 ms)
-        c.warp = kind == fk::kAdjoint && c.pipe && e->opt_warp && e->prec == fk::kF32 && Gp == 32 &&
+        // the warp-per-row kernel (FP32 and float-float) keeps a row's block columns one per lane:
+        // rows of at most 32 blocks (cubic L=64, S=256: FP32 1.669 vs 2.141 ms, float-float 8.32 vs
+        // 9.38 ms against k_adjoint_pipe)
+        c.warp = kind == fk::kAdjoint && c.pipe && e->opt_warp && e->prec != fk::kF64 && Gp == 32 &&
                  P % (32 * NP) == 0 && fk::max_row_blocks(e->h_row_ptr.data(), e->n_b) <= 32;
+        if (c.warp) c.stage_cap = 0;   // its H entries travel with the units: no per-tile stage
         // FP64 b=2 complex: the warp-per-row step (k_adjoint_step_warp), fewer FP64-pipe additions
         // in the D reduction
         if (kind == fk::kAdjoint && !c.pipe && !c.split && e->opt_warp && e->prec == fk::kF64 && e->cplx &&
             e->b == 2 && Gp == 32 && P % (32 * NP) == 0)
             c.warp = true;
         if (c.split) c.smem += 2 * (size_t)fk::kThreads * e->b * NP * 16;   // kept alpha_{m+1}, alpha_{m-1}
-        if (c.pipe) c.smem = stage_smem + (kind == fk::kStep ? fk::pipe_smem_bytes(e->b, NP)
+        if (c.pipe) c.smem = (c.warp ? 0 : stage_smem) + (kind == fk::kStep ? fk::pipe_smem_bytes(e->b, NP)
                                            : c.warp ? fk::adj_warp_smem_bytes(e->b, NP) : fk::adj_pipe_smem_bytes(e->b, NP));
         if (kind == fk::kStep && e->opt_tma) {
             int rc = configure_staged(e, c, Gp, nk_max, per_blk);

@@ -79,7 +79,7 @@ cudaError_t adj_warp_launch(const AdjArgs& a, const Launch& l) {
 template <class S, int B, int NP>
 cudaError_t adj_one(const AdjArgs& a, const Launch& l) {
     const bool whole = whole_chunks(a.P, a.Gp, NP);
-    if constexpr (S::PREC == 1) {   // FP32: rows served by a whole warp
+    if constexpr (S::PREC != 0) {   // FP32 / float-float rows served by a whole warp
         if (a.pipe && a.warp && whole && a.Gp == 32 && a.Dacc) return adj_warp_launch<S, B, NP>(a, l);
     }
     if constexpr (S::PREC != 0) {   // double-buffered gathers: FP32 and float-float systems
@@ -104,7 +104,7 @@ cudaError_t outer_one(const OuterArgs& a, const Launch& l) {
 }
 template <class S, int B, int NP>
 const void* pipe_fn(int kind) {
-    if constexpr (S::PREC == 1) {
+    if constexpr (S::PREC != 0) {
         if (kind == kAdjointWarp) return (const void*)k_adjoint_warp<S, B, NP>;
     }
     if constexpr (S::PREC != 0)

@@ -692,8 +692,8 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
 }
 
 // ---------------------------------------------------------------------------------
-// The FP32 reverse step for block rows served by a whole warp (Gp == 32) whose column chunks
-// are all whole: the shape of wide probe blocks (b=2 complex, S >= 128). Same recursions and
+// The FP32 / float-float reverse step for block rows served by a whole warp (Gp == 32) whose
+// column chunks are all whole: the shape of wide probe blocks (b=2 complex, S >= 128). Same recursions and
 // fused D epilogue as k_adjoint_pipe, organised around the fixed shape:
 //  * a warp walks one row as a stream of units, chunk by chunk: A (the own alpha_m rows of the
 //    chunk), K (one H block: its alpha_m / beta_{m+1} rows, H entries and D entries) for each of
@@ -711,14 +711,16 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
 //    so the two D entries it sends at the first transposed reduction level are exactly the two
 //    its partner (lane ^ 16, the other swap) keeps, and that level needs no selects.
 // It runs with the fused D epilogue only (D's pattern is H's). Results equal k_adjoint_pipe's up to
-// the order of the two bj terms of a general block in the swapped lanes (FP32 rounding), and the
-// same lanes write the same D entries.
+// the order of the two bj terms of a general block in the swapped lanes (rounding), and the same
+// lanes write the same D entries. Float-float blocks carry 64-byte H blocks; each warp's slot part
+// holds them with the D entries.
 // ---------------------------------------------------------------------------------
 template <int V>
 struct BufTag { static constexpr int value = V; };
 
 constexpr int kRing = 3;          // shared-memory slots of the unit stream
-constexpr int kWarpSlotBytes = 96;   // per warp and slot: H block (32 B) + the 4 writer lanes' D entries (16 B each)
+constexpr int kWarpHBytes = 64;      // per warp and slot: the H block (up to 64 B: 2x2 float-float complex) ...
+constexpr int kWarpSlotBytes = 128;  // ... then the 4 writer lanes' D entries (16 B each)
 
 // Shared memory of k_adjoint_warp after the H stage: kRing slots of 2 vectors x B rows x NP packets
 // per thread, then the per-warp H / D slots.
@@ -766,7 +768,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
     constexpr int W = G * NP;        // packets per column chunk
     constexpr int kHBytes = B * B * (int)sizeof(H);
     constexpr int kDBytes = S::CPLX ? 16 : 8;   // one D entry of the accumulator (8 bytes per real)
-    static_assert(kHBytes <= 32 && B * B * kDBytes <= 64, "per-warp slot sizes");
+    static_assert(kHBytes <= kWarpHBytes && B * B * kDBytes <= 64, "per-warp slot sizes");
     extern __shared__ __align__(16) unsigned char smem[];
     uint4* sbuf = reinterpret_cast<uint4*>(smem + ((sizeof(H) * B * B + sizeof(unsigned)) * (size_t)a.stage_cap + 15) / 16 * 16);
     uint4* const mine = sbuf + threadIdx.x;
@@ -783,7 +785,8 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
     constexpr int kHP = kHBytes / 16;
     constexpr bool kFast = kHBytes % 16 == 0 && kDBytes == 16 && kHP + B * B <= 32;
     // complex b=2 (FP32: OAcc is a float pair): the last reduction levels split real and imaginary parts
-    constexpr bool kCompSplit = kFast && B == 2 && sizeof(OAcc) == 8;
+    // (FP32: a float pair; float-float: two float-float values)
+    constexpr bool kCompSplit = kFast && B == 2 && S::CPLX && S::PREC != 0;
     auto h_slot = [&](int sl) -> const H* { return reinterpret_cast<const H*>(wbase + sl * kWarpSlotBytes); };
 
     const int sidx = a.cta_sys[blockIdx.x];
@@ -847,7 +850,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                     const bool dlane = dl >= 0 && dl < B * B;
                     const char* src = hl ? reinterpret_cast<const char*>(hval + (size_t)k * B * B) + lane * 16
                                          : reinterpret_cast<const char*>(a.Dacc + ((size_t)k * B * B + (dlane ? dl : 0)) * 2);
-                    cp_async16_if(hl ? ws + lane * 16 : ws + 32 + dl * 16, src, hl || dlane);
+                    cp_async16_if(hl ? ws + lane * 16 : ws + kWarpHBytes + dl * 16, src, hl || dlane);
                 } else {
                     constexpr int kPieces = kHBytes >= 16 ? kHBytes / 16 : 1;
                     constexpr int kPiece = kHBytes >= 16 ? 16 : kHBytes;
@@ -855,7 +858,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                     if (lane < kPieces)
                         cp_async_n<kPiece>(wsp + lane * kPiece, reinterpret_cast<const char*>(hval + (size_t)k * B * B) + lane * kPiece);
                     if (own.writer)   // the D entry this lane will update
-                        cp_async_n<kDBytes>(wsp + 32 + own.first * kDBytes,
+                        cp_async_n<kDBytes>(wsp + kWarpHBytes + own.first * kDBytes,
                                             a.Dacc + ((size_t)k * B * B + own.first) * (S::CPLX ? 2 : 1));
                 }
                 rows(BufTag<0>(), a.A, j);
@@ -967,21 +970,36 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                         // third level: lane bit 2 picks the real (0) or imaginary (1) part, so each of the
                         // 8 writer lanes (lane & 3 == 0) finishes and stores one real of the block
                         const bool im = (lane >> 2) & 1;
-                        const float kp = im ? of[0].y : of[0].x;
-                        const float sd = im ? of[0].x : of[0].y;
-                        float v = kp + __shfl_xor_sync(0xffffffffu, sd, 4);
-                        v += __shfl_xor_sync(0xffffffffu, v, 2);
-                        v += __shfl_xor_sync(0xffffffffu, v, 1);
-                        if ((lane & 3) == 0) {
-                            const int ent = sw * 2 + ((lane >> 3) & 1);   // entry bj * 2 + bi
-                            const size_t q = ((size_t)k * B * B + ent) * 2 + (im ? 1 : 0);
-                            const unsigned char* dp = wbase + sl * kWarpSlotBytes + 32 + ent * 16 + (im ? 8 : 0);
-                            if constexpr (S::DACC_DS) {
-                                float2 cur = *reinterpret_cast<const float2*>(dp);
-                                ds_mac(cur, dscale_ds, make_float2(v, 0.f));
-                                reinterpret_cast<float2*>(a.Dacc)[q] = ds_norm(cur);
-                            } else {
-                                a.Dacc[q] = *reinterpret_cast<const double*>(dp) + a.dscale * (double)v;
+                        const int ent = sw * 2 + ((lane >> 3) & 1);   // entry bj * 2 + bi
+                        const size_t q = ((size_t)k * B * B + ent) * 2 + (im ? 1 : 0);
+                        const unsigned char* dp = wbase + sl * kWarpSlotBytes + kWarpHBytes + ent * 16 + (im ? 8 : 0);
+                        if constexpr (S::PREC == 2) {   // float-float parts (hi, lo)
+                            const float2 kp = im ? make_float2(of[0].z, of[0].w) : make_float2(of[0].x, of[0].y);
+                            const float2 sd2 = im ? make_float2(of[0].x, of[0].y) : make_float2(of[0].z, of[0].w);
+                            float2 v = kp;
+                            ds_add(v, make_float2(__shfl_xor_sync(0xffffffffu, sd2.x, 4), __shfl_xor_sync(0xffffffffu, sd2.y, 4)));
+#pragma unroll
+                            for (int off = 2; off > 0; off >>= 1)
+                                ds_add(v, make_float2(__shfl_xor_sync(0xffffffffu, v.x, off), __shfl_xor_sync(0xffffffffu, v.y, off)));
+                            if ((lane & 3) == 0) {
+                                float2 cur2 = *reinterpret_cast<const float2*>(dp);
+                                ds_mac(cur2, dscale_ds, v);
+                                reinterpret_cast<float2*>(a.Dacc)[q] = ds_norm(cur2);
+                            }
+                        } else {
+                            const float kp = im ? of[0].y : of[0].x;
+                            const float sd2 = im ? of[0].x : of[0].y;
+                            float v = kp + __shfl_xor_sync(0xffffffffu, sd2, 4);
+                            v += __shfl_xor_sync(0xffffffffu, v, 2);
+                            v += __shfl_xor_sync(0xffffffffu, v, 1);
+                            if ((lane & 3) == 0) {
+                                if constexpr (S::DACC_DS) {
+                                    float2 cur2 = *reinterpret_cast<const float2*>(dp);
+                                    ds_mac(cur2, dscale_ds, make_float2(v, 0.f));
+                                    reinterpret_cast<float2*>(a.Dacc)[q] = ds_norm(cur2);
+                                } else {
+                                    a.Dacc[q] = *reinterpret_cast<const double*>(dp) + a.dscale * (double)v;
+                                }
                             }
                         }
                     } else {
@@ -994,7 +1012,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                 if constexpr (!kCompSplit) {
                     double2 pre = make_double2(0.0, 0.0);
                     if (own.writer) {   // the D entry, copied with the unit (by lane kHP + first in the fast form)
-                        const unsigned char* dp = wbase + sl * kWarpSlotBytes + 32 + own.first * kDBytes;
+                        const unsigned char* dp = wbase + sl * kWarpSlotBytes + kWarpHBytes + own.first * kDBytes;
                         if constexpr (S::CPLX) pre = *reinterpret_cast<const double2*>(dp);
                         else pre.x = *reinterpret_cast<const double*>(dp);
                     }

@@ -107,9 +107,9 @@ int  fk_engine_synchronize(fk_engine* e);
                                 * same GPU start sooner (the serving loop's short solves); moment sums are then
                                 * added over more CTA partials (last-bit differences, deterministic)          */
 #define FK_OPT_WARP_ROWS  15   /* 1 (default): when a warp serves each block row (32 lanes), every column
-                                * chunk is whole and D's pattern is H's (fused epilogue), the FP32 reverse
-                                * step runs the warp-per-row kernel (a three-slot copy ring, compile-time
-                                * offsets) and the FP64 b=2 complex one its warp-per-row form (fewer FP64
+                                * chunk is whole and D's pattern is H's (fused epilogue), the FP32 and
+                                * float-float reverse steps run the warp-per-row kernel (a three-slot copy
+                                * ring, compile-time offsets) and the FP64 b=2 complex one its warp-per-row form (fewer FP64
                                 * additions in the D reduction); 0 the general kernels. Results agree to the
                                 * last bits of rounding                                               */
 int  fk_engine_set_option(fk_engine* e, int option, int value);

@@ -541,13 +541,14 @@ def test_acc64_option_reads_back(gpu):
 
 @pytest.mark.parametrize("prec,opts", [("fp32", {L.FK_OPT_ACC64: 1}), ("fp32", {L.FK_OPT_ACC64: 0}),
                                        ("fp32", {L.FK_OPT_FUSE_D: 0}), ("fp32", {L.FK_OPT_CTAS_PER_SM: 1}),
-                                       ("fp64", {}), ("fp64", {L.FK_OPT_CTAS_PER_SM: 1})])
+                                       ("fp64", {}), ("fp64", {L.FK_OPT_CTAS_PER_SM: 1}),
+                                       ("ds", {}), ("ds", {L.FK_OPT_CTAS_PER_SM: 1})])
 def test_warp_row_adjoint_against_general(gpu, prec, opts):
     # b=2 complex rows with S=256 columns are served by a whole warp (32 lanes, whole chunks):
-    # the reverse step runs k_adjoint_warp (FP32) / k_adjoint_step_warp (FP64) by default
+    # the reverse step runs k_adjoint_warp (FP32, float-float) / k_adjoint_step_warp (FP64) by default
     # (FK_OPT_WARP_ROWS 1) and k_adjoint_pipe / k_adjoint_step with the option off. Same moments (the
     # forward step is shared); D within the engine's tolerance of the oracle, and within rounding of
-    # the general kernel (FP32 1e-5, FP64 1e-13, Frobenius).
+    # the general kernel (FP32 1e-5, FP64 and float-float 1e-12, Frobenius).
     # L=16: 4,096 rows in 512 tiles, more than the CTAs of one wave (and 152 CTAs with one per SM),
     # so warps walk several rows and the unit stream continues across rows
     H, es, _ = W.cubic_spin_lattice(16, -1.0, 1.0, seed=17)
@@ -559,8 +560,8 @@ def test_warp_row_adjoint_against_general(gpu, prec, opts):
     assert np.array_equal(warp[0], general[0])
     assert mu_err(warp[0], warp[1]) <= TOL_MU[prec]
     assert rel_err(warp[2], warp[3]) <= TOL_D[prec]
-    assert rel_err(warp[2], general[2]) <= (1e-5 if prec == "fp32" else 1e-13)
-    for p, want in [("fp32", 1), ("ds", 0), ("fp64", 1)]:   # float-float keeps k_adjoint_pipe
+    assert rel_err(warp[2], general[2]) <= (1e-5 if prec == "fp32" else 1e-12)
+    for p, want in [("fp32", 1), ("ds", 1), ("fp64", 1)]:
         eng = fk.Engine(True, p)
         eng.set_H(H, es)
         eng.set_R(R)
