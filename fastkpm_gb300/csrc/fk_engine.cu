@@ -111,6 +111,7 @@ struct fk_engine {
     double es_lo = 0, es_hi = 0;
     std::vector<int> h_row_ptr, h_col;
     DevBuf d_row_ptr, d_colc, d_hval;
+    DevBuf d_row_hsum;   // float-float engines: per row, identity blocks of one value (fk_prep.h)
 
     // probes and work vectors
     int n = 0, s = 0;
@@ -291,7 +292,7 @@ std::vector<long long> graph_signature(const fk_engine* e) {
     addr(e->stream);
     for (const DevBuf* b : {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2],
                             &e->d_V[3], &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc,
-                            &e->d_partials, &e->d_raw, &e->d_coef})
+                            &e->d_partials, &e->d_raw, &e->d_coef, &e->d_row_hsum})
         addr(b->p);
     for (long long v : {(long long)e->n_b, (long long)e->b, (long long)e->nnzb, (long long)e->n, (long long)e->s, e->ld,
                         (long long)e->P, (long long)e->d_nnzb, (long long)e->opt_acc64})
@@ -629,6 +630,7 @@ int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp,
         a.split = c.split ? 1 : 0;
         a.pipe = c.pipe ? 1 : 0;
         a.warp = c.warp ? 1 : 0;
+        a.row_hsum = (c.warp && e->prec == fk::kDS) ? e->d_row_hsum.as<unsigned char>() : nullptr;
         ProfScope ps(e, fk::kAdjoint);
         FK_TRY(prec_launch_adjoint(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "adjoint kernel launch");
     }
@@ -1456,7 +1458,7 @@ int fk_engine_destroy(fk_engine* e) {
     DevBuf* bufs[] = {&e->d_row_ptr, &e->d_colc, &e->d_hval, &e->d_R, &e->d_V[0], &e->d_V[1], &e->d_V[2], &e->d_V[3],
                       &e->dd_row_ptr, &e->dd_colc, &e->dd_rows, &e->dd_pair, &e->dd_acc, &e->d_partials, &e->d_raw,
                       &e->d_coef, &e->d_stage, &e->d_post, &e->d_t_uoff, &e->d_t_ucol, &e->d_t_own, &e->d_t_kslot,
-                      &e->d_t_base, &e->d_err};
+                      &e->d_t_base, &e->d_err, &e->d_row_hsum};
     for (auto* b : bufs) b->release();
     for (auto& c : e->cfg) { c.sys.release(); c.cta_sys.release(); }
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
@@ -1609,6 +1611,11 @@ int fk_engine_set_H(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, 
     FK_TRY(cudaMemcpy(e->d_row_ptr.p, ph.row_ptr.data(), sizeof(int) * (n_b + 1), cudaMemcpyHostToDevice), "upload H row_ptr");
     FK_TRY(cudaMemcpy(e->d_colc.p, ph.colc.data(), sizeof(unsigned) * nk, cudaMemcpyHostToDevice), "upload H columns");
     FK_TRY(cudaMemcpy(e->d_hval.p, ph.hval.data(), ph.hval.size(), cudaMemcpyHostToDevice), "upload H values");
+    if (e->prec == fk::kDS) {
+        FK_TRY(e->d_row_hsum.ensure(std::max<size_t>(ph.row_hsum.size(), 16)), "alloc H row flags");
+        FK_TRY(cudaMemcpy(e->d_row_hsum.p, ph.row_hsum.data(), ph.row_hsum.size(), cudaMemcpyHostToDevice),
+               "upload H row flags");
+    }
     e->n_b = n_b;
     e->b = b;
     e->nnzb = nk;
@@ -2098,7 +2105,7 @@ int fk_engine_memory(const fk_engine* e, size_t* bytes) {
     if (!e || !bytes) return FK_ERR_ARG;
     size_t t = e->d_row_ptr.bytes + e->d_colc.bytes + e->d_hval.bytes + e->d_R.bytes + e->dd_row_ptr.bytes +
                e->dd_colc.bytes + e->dd_rows.bytes + e->dd_pair.bytes + e->dd_acc.bytes + e->d_partials.bytes +
-               e->d_raw.bytes + e->d_coef.bytes + e->d_stage.bytes;
+               e->d_raw.bytes + e->d_coef.bytes + e->d_stage.bytes + e->d_row_hsum.bytes;
     for (auto& v : e->d_V) t += v.bytes;
     *bytes = t;
     return FK_OK;

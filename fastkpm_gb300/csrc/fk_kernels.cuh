@@ -77,6 +77,7 @@ struct AdjArgs {
     int split;            // run k_adjoint_split (two passes over the blocks) instead of k_adjoint_step
     int pipe;             // FP32 systems: run k_adjoint_pipe (double-buffered gathers)
     int warp = 0;         // with pipe, Gp == 32, whole chunks and the fused epilogue: run k_adjoint_warp
+    const unsigned char* row_hsum = nullptr;   // per row (float-float k_adjoint_warp): identity blocks of one value
 };
 
 struct OuterArgs {

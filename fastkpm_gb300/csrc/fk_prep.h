@@ -98,6 +98,7 @@ struct PreparedH {
     std::vector<int> col;                                        // augmented local block columns
     std::vector<unsigned, UninitAlloc<unsigned>> colc;           // (col + col_offset) | class << 30
     std::vector<unsigned char, UninitAlloc<unsigned char>> hval; // entries in the engine precision
+    std::vector<unsigned char> row_hsum;   // per row: 1 if its identity blocks (class 2, at least two) share one value
 };
 
 inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* row_ptr, const int* col_idx,
@@ -126,6 +127,7 @@ inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* ro
     const size_t ebytes = (size_t)elem_bytes(prec, cplx) / cw;   // bytes per real entry
     out.hval.resize((size_t)nk * bb * cw * ebytes);
     unsigned char* hv = out.hval.data();
+    out.row_hsum.assign(n_b, 0);
     // every output block: Hs = (H - avg I) / mag in double, classified, converted to the
     // engine precision; each range of rows writes its own slice of the outputs
     parallel_ranges(n_b, 1 << 14, [&](int lo, int hi) {
@@ -133,6 +135,9 @@ inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* ro
         for (int i = lo; i < hi; i++) {
             int kout = out.row_ptr[i];
             bool diag_done = false;
+            int n_ident = 0;
+            bool same_h = true;
+            double h_ident = 0.0;
             for (int k = row_ptr[i]; k <= row_ptr[i + 1]; k++) {
                 const bool end = k == row_ptr[i + 1];
                 const int j = end ? n_b : col_idx[k];
@@ -165,6 +170,10 @@ inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* ro
                             if (bi == bj && re != v[0]) scal = false;
                         }
                     const unsigned cls = real ? (scal ? 2u : 1u) : 0u;
+                    if (cls == 2u) {
+                        if (n_ident++ == 0) h_ident = v[0];
+                        else if (v[0] != h_ident) same_h = false;
+                    }
                     out.col[kout] = jc;
                     out.colc[kout] = (unsigned)(jc + col_offset) | (cls << 30);
                     const size_t base = (size_t)kout * bb * cw;
@@ -185,6 +194,7 @@ inline int prepare_H(int prec, int cplx, int n_b, int b, int nnzb, const int* ro
                 }
                 if (end) break;
             }
+            out.row_hsum[i] = (n_ident >= 2 && same_h) ? 1 : 0;
         }
     });
     return FK_OK;

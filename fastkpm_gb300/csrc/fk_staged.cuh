@@ -725,7 +725,7 @@ constexpr int kWarpSlotBytes = 128;  // ... then the 4 writer lanes' D entries (
 // Shared memory of k_adjoint_warp after the H stage: kRing slots of 2 vectors x B rows x NP packets
 // per thread, then the per-warp H / D slots.
 __host__ __device__ inline size_t adj_warp_smem_bytes(int B, int NP) {
-    return (size_t)kRing * 2 * B * NP * kThreads * 16 + (size_t)(kThreads / 32) * kRing * kWarpSlotBytes;
+    return (size_t)kRing * 2 * B * NP * kThreads * 16 + (size_t)(kThreads / 32) * (kRing * kWarpSlotBytes + 32);
 }
 // cp.async of N = 4, 8 or 16 bytes (N < 16 goes through L1: the .cg form moves 16 bytes only)
 template <int N>
@@ -778,6 +778,9 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                                  (threadIdx.x >> 5) * kRing * kWarpSlotBytes;
     // the same places as 32-bit shared addresses, and the strides of the ring slots (bytes)
     const unsigned s_mine = smem_addr(mine), s_warp = smem_addr(wbase);
+    // per-warp scratch of 32 bytes after all the warps' slot parts: a row's unit order (float-float)
+    unsigned char* const worder = reinterpret_cast<unsigned char*>(sbuf + (size_t)kRing * 2 * B * NP * kThreads) +
+                                  (kThreads / 32) * kRing * kWarpSlotBytes + (threadIdx.x >> 5) * 32;
     constexpr int kQStride = kThreads * 16, kRowStride = NP * kQStride, kVecStride = B * kRowStride;
     constexpr unsigned kSlotStride = 2u * kVecStride;
     // complex b=2: the H block is kHP whole 16-byte pieces and a D entry is 16 bytes, so one predicated
@@ -814,6 +817,28 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
         const unsigned ccl = lane < nrow ? __ldg(a.colc + kb + lane) : 0u;   // lane kk: block kb + kk
         const int per = nrow + 2;                  // units per chunk: A, K x nrow, O
         const int U = nch * per;
+        // Float-float rows whose identity blocks share one value h (host flag): those blocks come first,
+        // their rows are summed (a float-float addition instead of a multiply-add each) and the sum is
+        // scaled by h once, before the other blocks add their products. `ord` (lane p): the lane, i.e.
+        // block kb + ord, that unit position p takes; n_id: the identity blocks.
+        bool hsum = false;
+        unsigned ord = lane;
+        int n_id = 0;
+        if constexpr (S::PREC == 2) {
+            hsum = a.row_hsum != nullptr && a.row_hsum[i] != 0;
+            if (hsum) {
+                const bool isid = lane < nrow && (ccl >> 30) == 2u;
+                const unsigned mid = __ballot_sync(0xffffffffu, isid);
+                const unsigned mrow = nrow >= 32 ? 0xffffffffu : ((1u << nrow) - 1u);
+                const unsigned lt = (1u << lane) - 1u;
+                n_id = __popc(mid);
+                const int pos = isid ? __popc(mid & lt) : n_id + __popc(mrow & ~mid & lt);
+                if (lane < nrow) worder[pos] = (unsigned char)lane;
+                __syncwarp();
+                ord = lane < nrow ? worder[lane] : lane;
+                __syncwarp();
+            }
+        }
 
         // ---- issue: put unit (ic, ir) in flight into ring slot sl (one commit group per unit)
         auto issue = [&](int ic, int ir, int sl) {
@@ -836,8 +861,8 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
             } else if (ir == per - 1) {    // O: alpha_{m+1}, beta_{m+2} own rows
                 rows(BufTag<0>(), a.Ap, (unsigned)i);
                 rows(BufTag<1>(), a.Bp, (unsigned)i);
-            } else {                       // K: block kb + kk
-                const int kk = ir - 1;
+            } else {                       // K: the block at unit position ir - 1 (identity-first order in hsum rows)
+                const int kk = hsum ? (int)__shfl_sync(0xffffffffu, ord, ir - 1) : ir - 1;
                 const int k = kb + kk;
                 const unsigned cc = __shfl_sync(0xffffffffu, ccl, kk);
                 const unsigned j = cc & kColMask;
@@ -872,13 +897,22 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
         // one block's multiply-adds and epilogue products from ring slot sl; IDENT: a real multiple
         // of the identity (class 2, read from its (0,0) entry), else general (real systems, or complex
         // with class 0 or 1: a class-1 block's zero imaginary parts make the complex product exact)
-        auto body = [&](auto itag, int sl, OAcc (&of)[B * B]) {
-            constexpr bool IDENT = decltype(itag)::value != 0;
+        // FP32: both rows' multiply-adds, then the epilogue once for every block kind (beta_{m+1}'s
+        // packets read from shared memory again): 1.628 vs 1.669 ms at cubic L=64, S=256. Float-float
+        // keeps each row's epilogue with its multiply-adds (8.10 vs 8.44 ms split).
+        constexpr bool kEpiInside = S::PREC != 1;
+        // one block's recursion multiply-adds from ring slot sl (and, kEpiInside, its epilogue
+        // products); MODE 0: general (real systems, or complex with class 0 or 1: a class-1 block's
+        // zero imaginary parts make the complex product exact), 1: a real multiple of the identity
+        // (class 2, its (0,0) entry), 2: an identity block of an hsum row (its rows added; the sum is
+        // scaled after the row's last identity block)
+        auto body = [&](auto mtag, int sl, OAcc (&of)[B * B]) {
+            constexpr int MODE = decltype(mtag)::value;
             const H* hm = h_slot(sl);
             typename S::Hr hd;
             H hr[B * B];
-            if constexpr (IDENT) hd = S::hreal(hm[0]);
-            else {
+            if constexpr (MODE == 1) hd = S::hreal(hm[0]);
+            else if constexpr (MODE == 0) {
 #pragma unroll
                 for (int q = 0; q < B * B; q++) hr[q] = hm[q ^ hx];   // this lane's order
             }
@@ -893,7 +927,12 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
 #pragma unroll
                     for (int e = 0; e < EPP; e++) { av[q * EPP + e] = pa.e[e]; bv[q * EPP + e] = pb.e[e]; }
                 }
-                if constexpr (IDENT) {
+                if constexpr (MODE == 2) {
+                    if constexpr (S::PREC == 2) {
+#pragma unroll
+                        for (int e = 0; e < EPT; e++) { S::acc_add(accA[rj][e], av[e]); S::acc_add(accB[rj][e], bv[e]); }
+                    }
+                } else if constexpr (MODE == 1) {
 #pragma unroll
                     for (int e = 0; e < EPT; e++) { S::mac_re(accA[rj][e], hd, av[e]); S::mac_re(accB[rj][e], hd, bv[e]); }
                 } else {
@@ -908,6 +947,29 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                             for (int e = 0; e < EPT; e++) { S::mac_re(accA[r][e], S::hreal(h), av[e]); S::mac_re(accB[r][e], S::hreal(h), bv[e]); }
                         }
                     }
+                }
+                if constexpr (kEpiInside) {
+#pragma unroll
+                    for (int r = 0; r < B; r++) {   // each entry's first product starts it (of is zero): no add to zero
+                        of[rj * B + r] = S::oa_first(Ai[r][0], bv[0]);
+#pragma unroll
+                        for (int e = 1; e < EPT; e++) S::oa_mac(of[rj * B + r], Ai[r][e], bv[e]);
+                    }
+                }
+            }
+        };
+        // the block's epilogue products after its multiply-adds (FP32): one copy of this code for all
+        // block kinds, beta_{m+1}'s packets read from shared memory again
+        auto epi = [&](int sl, OAcc (&of)[B * B]) {
+#pragma unroll
+            for (int rj = 0; rj < B; rj++) {
+                E bv[EPT];
+#pragma unroll
+                for (int q = 0; q < NP; q++) {
+                    Packet<E, EPP> pb;
+                    pb.u = *slot(sl, 1, rj, q);
+#pragma unroll
+                    for (int e = 0; e < EPP; e++) bv[q * EPP + e] = pb.e[e];
                 }
 #pragma unroll
                 for (int r = 0; r < B; r++) {   // each entry's first product starts it (of is zero): no add to zero
@@ -948,14 +1010,33 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
 #pragma unroll
                     for (int e = 0; e < EPT; e++) { accA[r][e] = S::zero(); accB[r][e] = S::zero(); }
                 }
-            } else if (pr < per - 1) {   // K: block kb + pr - 1
-                const int k = kb + pr - 1;
-                const unsigned cc = __shfl_sync(0xffffffffu, ccl, pr - 1);
+            } else if (pr < per - 1) {   // K: the block at unit position pr - 1
+                const int kk = hsum ? (int)__shfl_sync(0xffffffffu, ord, pr - 1) : pr - 1;
+                const int k = kb + kk;
+                const unsigned cc = __shfl_sync(0xffffffffu, ccl, kk);
                 OAcc of[B * B];
 #pragma unroll
                 for (int q = 0; q < B * B; q++) of[q] = S::oa_zero();
-                if ((cc >> 30) == 2u) body(BufTag<1>(), sl, of);
-                else body(BufTag<0>(), sl, of);
+                if ((cc >> 30) == 2u) {
+                    bool summed = false;
+                    if constexpr (S::PREC == 2) {
+                        if (hsum) {
+                            body(BufTag<2>(), sl, of);
+                            summed = true;
+                            if (pr - 1 == n_id - 1) {   // the last identity block: scale the sums by h
+                                const typename S::Hr h = S::hreal(h_slot(sl)[0]);
+#pragma unroll
+                                for (int r = 0; r < B; r++)
+#pragma unroll
+                                    for (int e = 0; e < EPT; e++) { S::acc_scale(accA[r][e], h); S::acc_scale(accB[r][e], h); }
+                            }
+                        }
+                    }
+                    if (!summed) body(BufTag<1>(), sl, of);
+                } else {
+                    body(BufTag<0>(), sl, of);
+                }
+                if constexpr (!kEpiInside) epi(sl, of);
                 // of[rj * B + r] holds D entry (bj = rj ^ sw, bi = r ^ sw)
                 if constexpr (B == 2) {
                     // lane ^ 16 has the other swap: its (1,1) and (1,0) slots are this lane's (0,0), (0,1)

@@ -297,6 +297,9 @@ struct SysDSR {
     __device__ static Hr hreal(H h) { return h; }
     __device__ static void mac(Acc& a, H h, E x) { ds_mac(a, h, x); }
     __device__ static void mac_re(Acc& a, Hr h, E x) { ds_mac(a, h, x); }
+    // a += x and a = h a: a row's identity blocks of one value h summed first, scaled once
+    __device__ static void acc_add(Acc& a, E x) { ds_add(a, x); }
+    __device__ static void acc_scale(Acc& a, Hr h) { a = ds_mul(h, a); }
     __device__ static E fin(Acc a, bool two, bool has_z, E z) {
         float2 v = ds_norm(a);
         if (two) { v.x *= 2.f; v.y *= 2.f; }
@@ -359,6 +362,12 @@ struct SysDSC {
         ds_mac(ar, h, re(x)); ds_mac(ai, h, im(x));
         a = pack(ar, ai);
     }
+    __device__ static void acc_add(Acc& a, E x) {   // a += x
+        float2 ar = re(a), ai = im(a);
+        ds_add(ar, re(x)); ds_add(ai, im(x));
+        a = pack(ar, ai);
+    }
+    __device__ static void acc_scale(Acc& a, Hr h) { a = pack(ds_mul(h, re(a)), ds_mul(h, im(a))); }   // a = h a
     __device__ static E fin(Acc a, bool two, bool has_z, E z) {
         float2 vr = SysDSR::fin(re(a), two, has_z, re(z));
         float2 vi = SysDSR::fin(im(a), two, has_z, im(z));

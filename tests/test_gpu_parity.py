@@ -569,3 +569,28 @@ def test_warp_row_adjoint_against_general(gpu, prec, opts):
         eng.set_option(L.FK_OPT_WARP_ROWS, 0)
         assert eng.get_option(L.FK_OPT_WARP_ROWS) == 0
         eng.close()
+
+
+@pytest.mark.parametrize("prec", ["ds", "fp32"])
+def test_warp_row_adjoint_nonuniform_hopping(gpu, prec):
+    # Rows whose identity (hopping) blocks do not all share one value: every third bond of the 16^3
+    # spin lattice hops with 1.5 t (bond (i, j) and (j, i) alike, so H stays Hermitian). Float-float
+    # rows with one hopping value sum their identity blocks' rows first and scale once; the others
+    # (and every FP32 row) multiply-add block by block. Against the oracle and the general kernel.
+    H, es0, _ = W.cubic_spin_lattice(16, -1.0, 1.0, seed=23)
+    rows = np.repeat(np.arange(H.n_rows), np.diff(H.row_ptr))
+    cols = H.col_idx
+    b2 = H.b_len * H.b_len
+    pick = (rows != cols) & ((rows + cols) % 3 == 0)
+    val = H.val.reshape(-1, b2).copy()
+    val[pick] *= 1.5
+    H = H.with_values(val.ravel())
+    es = fk.EnergyScale(1.6 * es0.lo, 1.6 * es0.hi)
+    R = fk.probe_uncorrelated(H.n_rows * H.b_len, 256, fk.RNG(23), complex_values=True)
+    M = 24
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    warp = run_pair(H, es, R, True, prec, M, c, "autodiff")
+    general = run_pair(H, es, R, True, prec, M, c, "autodiff", {L.FK_OPT_WARP_ROWS: 0})
+    assert mu_err(warp[0], warp[1]) <= TOL_MU[prec]
+    assert rel_err(warp[2], warp[3]) <= TOL_D[prec]
+    assert rel_err(warp[2], general[2]) <= (1e-5 if prec == "fp32" else 1e-12)
