@@ -230,9 +230,9 @@ def step_flops_per_launch(H, S):
 # rows, so the L=64 launch's traffic is these times N. Keys: (precision, FP64 accumulators). An
 # engine form without a capture of its current kernel reports null.
 ADJ_TRAFFIC_PER_ROW = {("fp64", 1): (1.857997e9 + 0.721861e9) / 65536,
-                       ("fp32", 1): (0.577800e9 + 0.248626e9) / 65536,
-                       ("ds", 0): (1.700167e9 + 0.530617e9) / 65536}
-ADJ_WARP_INST_PER_ROW = {("ds", 0): 933429888 / 65536}
+                       ("fp32", 1): (0.578174e9 + 0.250220e9) / 65536,
+                       ("ds", 0): (1.709504e9 + 0.530700e9) / 65536}
+ADJ_WARP_INST_PER_ROW = {("ds", 0): 914440192 / 65536}
 ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
 
 
