@@ -594,3 +594,27 @@ def test_warp_row_adjoint_nonuniform_hopping(gpu, prec):
     assert mu_err(warp[0], warp[1]) <= TOL_MU[prec]
     assert rel_err(warp[2], warp[3]) <= TOL_D[prec]
     assert rel_err(warp[2], general[2]) <= (1e-5 if prec == "fp32" else 1e-12)
+
+
+@pytest.mark.parametrize("prec", ["ds", "fp32", "fp64"])
+def test_warp_row_adjoint_real_b2(gpu, prec):
+    # Real 2x2 blocks with S=256 probe columns (the real part of the cubic spin lattice: symmetric,
+    # hopping blocks t I2 and real exchange blocks): rows served by a whole warp take the warp-per-row
+    # reverse step (FP32 and float-float: real block entries, D entries 8 bytes each) in FP32 and
+    # float-float; FP64 keeps k_adjoint_step (its warp form is for complex blocks). Against the
+    # oracle and the general kernel.
+    Hc, es, _ = W.cubic_spin_lattice(16, -1.0, 1.0, seed=29)
+    H = Hc.with_values(np.ascontiguousarray(Hc.val.real))
+    R = fk.probe_uncorrelated(H.n_rows * H.b_len, 256, fk.RNG(29))
+    M = 24
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    warp = run_pair(H, es, R, False, prec, M, c, "autodiff")
+    general = run_pair(H, es, R, False, prec, M, c, "autodiff", {L.FK_OPT_WARP_ROWS: 0})
+    assert mu_err(warp[0], warp[1]) <= TOL_MU[prec]
+    assert rel_err(warp[2], warp[3]) <= TOL_D[prec]
+    assert rel_err(warp[2], general[2]) <= (1e-5 if prec == "fp32" else 1e-12)
+    eng = fk.Engine(False, prec)
+    eng.set_H(H, es)
+    eng.set_R(R)
+    assert eng.get_option(L.FK_OPT_WARP_ROWS) == (0 if prec == "fp64" else 1)
+    eng.close()
