@@ -91,9 +91,12 @@ struct fk_batch {
     std::string err;
     std::vector<PendingSystem> pending;
     // committed state
-    int b = 0, s = 0, n_sys = 0, P = 0;
+    int b = 0, s = 0, n_sys = 0, P = 0;   // s, P: the widest system's probe columns and packets per row
     long long ld = 0, total_rows = 0;
     std::vector<int> row_base, n_b;
+    std::vector<int> Pk;                  // per system: its packets per row (probe counts may differ)
+    int P_launch = 0;                     // the launches' P: P when every system's rows split into whole
+                                          // chunks of the mapping (the unmasked kernels), else one that does not
     std::vector<int> h_row_ptr;          // global
     std::vector<int> h_col;              // global block columns of the prepared pattern
     Buf d_row_ptr, d_colc, d_hval, d_R, d_V[4], d_stage;
@@ -220,6 +223,9 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     if (m.cap_per_sm > 0) occ = std::min(occ, m.cap_per_sm);
     const long long cap = (long long)occ * bt->num_sms;
     bt->sysd.resize(bt->n_sys);
+    bool all_whole = true;
+    for (int k = 0; k < bt->n_sys; k++) all_whole = all_whole && bt->Pk[k] % (Gp * NP) == 0;
+    bt->P_launch = all_whole || Gp * NP == 1 ? P : Gp * NP + 1;   // (the kernels read each system's own P)
     std::vector<int> cta_sys, order(bt->n_sys);
     std::vector<long long> tiles(bt->n_sys);
     std::vector<int> ctas(bt->n_sys);
@@ -236,7 +242,7 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     });
     int base = 0;
     for (int k : order) {
-        bt->sysd[k] = SysDesc{bt->row_base[k], bt->n_b[k], base, ctas[k]};
+        bt->sysd[k] = SysDesc{bt->row_base[k], bt->n_b[k], base, ctas[k], bt->Pk[k]};
         cta_sys.insert(cta_sys.end(), ctas[k], k);
         base += ctas[k];
     }
@@ -275,7 +281,7 @@ int batch_enqueue_moments(fk_batch* bt, int M) {
             a.sys = bt->d_sys.as<SysDesc>();
             a.cta_sys = bt->d_cta_sys.as<int>();
             a.Gp = bt->Gp;
-            a.P = std::min(bt->W, bt->P - sl * bt->W);
+            a.P = bt->P_launch;   // (one column slice: bt->W == bt->P)
             a.ld = bt->ld;
             a.row_ptr = bt->d_row_ptr.as<int>();
             a.colc = bt->d_colc.as<unsigned>();
@@ -460,7 +466,7 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
         o.sys = bt->d_sys.as<SysDesc>();
         o.cta_sys = bt->d_cta_sys.as<int>();
         o.Gp = bt->Gp;
-        o.P = bt->P;
+        o.P = bt->P_launch;
         o.ld = bt->ld;
         o.row_ptr = bt->d_row_ptr.as<int>();
         o.colc = bt->d_colc.as<unsigned>();
@@ -484,7 +490,7 @@ int batch_autodiff(fk_batch* bt, int M, const double* c, double* D_out) {
             a.sys = bt->d_sys.as<SysDesc>();
             a.cta_sys = bt->d_cta_sys.as<int>();
             a.Gp = bt->Gp;
-            a.P = bt->P;
+            a.P = bt->P_launch;
             a.ld = bt->ld;
             a.row_ptr = bt->d_row_ptr.as<int>();
             a.colc = bt->d_colc.as<unsigned>();
@@ -589,8 +595,7 @@ int fk_batch_add(fk_batch* bt, int n_b, int b, int nnzb, const int* row_ptr, con
     if (!bt) return FK_ERR_ARG;
     if (s <= 0 || !R) return bt->fail(FK_ERR_ARG, "batch_add: need a probe block with s >= 1 columns");
     const int ref_b = bt->pending.empty() ? (bt->n_sys ? bt->b : b) : bt->pending.front().b;
-    const int ref_s = bt->pending.empty() ? (bt->n_sys ? bt->s : s) : bt->pending.front().s;
-    if (b != ref_b || s != ref_s) return bt->fail(FK_ERR_ARG, "batch_add: every system needs the same b and s");
+    if (b != ref_b) return bt->fail(FK_ERR_ARG, "batch_add: every system needs the same block size b");
     PendingSystem ps;
     std::string why;
     int rc = fk::prepare_H(bt->prec, bt->cplx, n_b, b, nnzb, row_ptr, col_idx, val, es_lo, es_hi, 0, ps.h, why);
@@ -620,11 +625,14 @@ int fk_batch_commit(fk_batch* bt) {
     cudaSetDevice(bt->device);
     auto& ps = bt->pending;
     bt->b = ps[0].b;
-    bt->s = ps[0].s;
+    bt->s = 0;
+    for (const auto& q : ps) bt->s = std::max(bt->s, q.s);
     bt->n_sys = (int)ps.size();
     const int epp = bt->epp();
-    bt->ld = ((long long)bt->s + epp - 1) / epp * epp;
+    bt->ld = ((long long)bt->s + epp - 1) / epp * epp;   // every system's rows use the widest one's stride
     bt->P = (int)(bt->ld / epp);
+    bt->Pk.resize(bt->n_sys);
+    for (int k = 0; k < bt->n_sys; k++) bt->Pk[k] = (ps[k].s + epp - 1) / epp;
     long long rows = 0, nk = 0;
     bt->row_base.resize(bt->n_sys);
     bt->n_b.resize(bt->n_sys);
@@ -676,7 +684,7 @@ int fk_batch_commit(fk_batch* bt) {
         BT_TRY(bt->d_stage.ensure(bytes), "alloc staging");
         BT_TRY(cudaMemcpyAsync(bt->d_stage.p, ps[k].R.data(), bytes, cudaMemcpyHostToDevice, bt->stream), "upload R");
         char* dst = (char*)bt->d_R.p + (size_t)bt->row_base[k] * bt->b * bt->ld * bt->esize();
-        BT_TRY(batch_load(bt, bt->d_stage.as<double>(), n, bt->s, 0, dst), "R layout kernel");
+        BT_TRY(batch_load(bt, bt->d_stage.as<double>(), n, ps[k].s, 0, dst), "R layout kernel");
         BT_TRY(cudaStreamSynchronize(bt->stream), "upload R");
     }
     bt->d_stage.release();

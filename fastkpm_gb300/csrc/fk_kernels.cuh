@@ -35,6 +35,8 @@ struct SysDesc {
     int n_b;         // block rows
     int cta_base;    // first CTA of this system
     int ctas;        // CTAs assigned to this system
+    int P;           // packets per row of this system's probe columns (0: the launch's P); systems of a
+                     // batch may have different probe counts and share the row stride of the widest
 };
 
 struct StepArgs {
@@ -266,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(Ste
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* x = reinterpret_cast<const E*>(a.x);
@@ -508,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);
@@ -654,7 +656,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adjoint_step_warp(AdjArgs a) {
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int P = a.P, W = G * NP;
+    const int P = sd.P > 0 ? sd.P : a.P, W = G * NP;
     const int nch = P / W;
     const long long items = (long long)sd.n_b * G;
     const E* A = reinterpret_cast<const E*>(a.A);
@@ -795,7 +797,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointSplitCtas<S, B, NP>) k_adjoi
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);
@@ -954,7 +956,7 @@ __global__ void __launch_bounds__(kThreads, kOuterCtas<S, B, NP>) k_outer(OuterA
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);

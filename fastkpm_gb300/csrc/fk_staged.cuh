@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_cheb_step_staged(StepArgs a, St
     constexpr int EPP = S::EPP;
     constexpr int EPT = NP * EPP;
     extern __shared__ __align__(16) unsigned char smem[];   // dynamic shared memory starts 16-byte aligned or better
-    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int Gp = a.Gp, P = a.P, W = Gp * NP;   // (single-engine kernel: one system, the launch's P)
     const int nch = (P + W - 1) / W;
     unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem);
     __shared__ int s_fail;
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step_pip
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* x = reinterpret_cast<const E*>(a.x);
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = a.P, W = Gp * NP;
+    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);
@@ -795,7 +795,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int nch = a.P / W;
+    const int nch = (sd.P > 0 ? sd.P : a.P) / W;
     const long long items = (long long)sd.n_b * G;
     const unsigned rb = (unsigned)(a.ld * (long long)sizeof(E));   // bytes per scalar row
     const int lane = threadIdx.x & 31;

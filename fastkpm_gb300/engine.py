@@ -486,8 +486,8 @@ class Engine:
 
 
 class Batch:
-    """Many Hamiltonians of uneven size (same b and s) solved together: one launch per
-    Chebyshev step covers every system; moments for all systems at once."""
+    """Many Hamiltonians of uneven size and probe count (same block size b) solved together: one
+    launch per Chebyshev step covers every system; moments for all systems at once."""
 
     def __init__(self, complex_values=False, precision="fp32", device=0):
         self.lib = L.load()

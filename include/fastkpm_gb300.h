@@ -233,7 +233,8 @@ int  fk_engine_memory(const fk_engine* e, size_t* bytes);
 /* ---- batched engine: many Hamiltonians of uneven size in one launch per Chebyshev step ----
  * No reference counterpart: the reference solves one Hamiltonian per Engine<T> call; this is the
  * batched form of Engine<T>::moments (reference src/engine_cusparse.cpp:755-791) over independent
- * systems that share the block size b and the probe count s. */
+ * systems that share the block size b; their probe counts s may differ (each system's rows use the
+ * widest system's row stride and the kernels walk only that system's own columns). */
 typedef struct fk_batch fk_batch;
 int  fk_batch_create(int device, int kind, int precision, fk_batch** out);
 int  fk_batch_destroy(fk_batch* bt);

@@ -98,12 +98,16 @@ def test_autotune_keeps_results(gpu):
 
 
 def test_batch_rejects_mixed_shapes(gpu):
-    bt = fk.Batch(False, "fp32")
+    # systems of one batch share the block size b (probe counts may differ)
+    bt = fk.Batch(True, "fp32")
     H, es = W.square_lattice(4, -1.0, 1.0, 0)
-    bt.add(H, es, fk.probe_uncorrelated(16, 8, fk.RNG(1)))
+    bt.add(H.with_values(H.val.astype(np.complex128)), es, fk.probe_uncorrelated(16, 8, fk.RNG(1), complex_values=True))
+    Hs, ess, _ = W.cubic_spin_lattice(2, -1.0, 1.0, seed=1)
     with pytest.raises(L.FkError) as ei:
-        bt.add(H, es, fk.probe_uncorrelated(16, 4, fk.RNG(1)))
+        bt.add(Hs, ess, fk.probe_uncorrelated(16, 8, fk.RNG(1), complex_values=True))
     assert ei.value.status == L.FK_ERR_ARG
+    bt = fk.Batch(False, "fp32")
+    bt.add(H, es, fk.probe_uncorrelated(16, 8, fk.RNG(1)))
     with pytest.raises(ValueError):
         bt.add(H, es, fk.probe_uncorrelated(15, 8, fk.RNG(1)))   # R rows must be b * n_b
     with pytest.raises(L.FkError) as ei:
@@ -225,3 +229,32 @@ def test_batch_profile_moments(gpu):
     bt.set_option(L.FK_OPT_GRAPHS, 1)
     b = bt.moments(M)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec,tol,dtol", [("fp64", 1e-10, 1e-10), ("ds", 1e-10, 1e-10), ("fp32", 1e-5, 1e-4)])
+def test_batch_mixed_probe_counts(gpu, prec, tol, dtol):
+    # Systems with different probe counts share one launch per step: the rows of all of them use the
+    # widest system's stride and each system walks only its own packets (S = 8, 24, 32, 40, 64: whole
+    # and ragged chunks). moments and autodiff_matrix per system against the oracle.
+    Ss = [8, 24, 32, 40, 64]
+    systems = []
+    for k, S in enumerate(Ss):
+        H, es = W.square_lattice([5, 9, 16, 3, 12][k], -1.0, 1.0 + k, seed=500 + k)
+        systems.append((H, es, fk.probe_uncorrelated(H.n_rows, S, fk.RNG(500 + k))))
+    M = 40
+    bt = fk.Batch(False, prec)
+    for H, es, R in systems:
+        bt.add(H, es, R)
+    bt.commit()
+    mu = bt.moments(M)
+    cs = np.stack([W.fermi_coefficients(M, es, "fermi_energy") for _, es, _ in systems])
+    Ds = bt.autodiff_matrix(M, cs)
+    for k, (H, es, R) in enumerate(systems):
+        o = O.OracleEngine(False, nthreads=2)
+        o.set_H(H, es)
+        o.set_R(R)
+        ref = o.moments(M)
+        assert np.max(np.abs(mu[k] - ref)) / ref[0] <= tol, (k, Ss[k])
+        D_ref = o.autodiff_matrix(cs[k], H.pattern_like(False))
+        assert rel_err(Ds[k].val, D_ref) <= dtol, (k, Ss[k])
+
