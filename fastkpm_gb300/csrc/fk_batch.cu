@@ -95,6 +95,7 @@ struct fk_batch {
     long long ld = 0, total_rows = 0;
     std::vector<int> row_base, n_b;
     std::vector<int> Pk;                  // per system: its packets per row (probe counts may differ)
+    std::vector<int> Gpk;                 // per system: its lanes per block row
     int P_launch = 0;                     // the launches' P: P when every system's rows split into whole
                                           // chunks of the mapping (the unmasked kernels), else one that does not
     std::vector<int> h_row_ptr;          // global
@@ -185,19 +186,15 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     bt->mom_M = 0;   // a new mapping (or the autotuner's trial runs) leaves no usable alpha state
     bt->drop_graphs();
     const int P = bt->P;
-    int Gp, NP;
-    if (m.Gp > 0) {
-        Gp = m.Gp;
-        NP = m.NP > 0 ? m.NP : 1;
-    } else if (P <= 32) {
-        // narrow rows: two packets per lane (measured faster than one on b=1, S=32 lattices)
-        NP = P >= 2 ? 2 : 1;
-        Gp = next_pow2((P + NP - 1) / NP);
-    } else {
-        Gp = 32;
-        NP = (P + 31) / 32;
-        NP = NP <= 1 ? 1 : NP <= 2 ? 2 : 4;
+    // packets per lane: as requested, else by the widest system's packets (narrow rows: two per lane,
+    // measured faster than one on b=1, S=32 lattices; wider: enough for 32 lanes, 1, 2 or 4); lanes
+    // per row: as requested, else the fewest that cover the row in one chunk (at most 32)
+    int NP = m.NP;
+    if (NP <= 0) {
+        if (P <= 32) NP = P >= 2 ? 2 : 1;
+        else NP = (P + 31) / 32 <= 1 ? 1 : (P + 31) / 32 <= 2 ? 2 : 4;
     }
+    const int Gp = m.Gp > 0 ? m.Gp : std::min(32, next_pow2((P + NP - 1) / NP));
     if (!(Gp == 1 || Gp == 2 || Gp == 4 || Gp == 8 || Gp == 16 || Gp == 32)) return bt->fail(FK_ERR_ARG, "bad lanes per row %d", Gp);
     if (!(NP == 1 || NP == 2 || NP == 4)) return bt->fail(FK_ERR_ARG, "bad packets per lane %d", NP);
     // the kernel walks the row's column chunks of Gp * NP packets itself: one launch per step
@@ -205,13 +202,19 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     bt->NP = NP;
     bt->W = P;
     bt->slices = 1;
+    // lanes per row of each system: a forced mapping's for all; else the fewest (a power of two, at
+    // most 32) that cover the system's own packets in one chunk of NP each, so that a system's tiles,
+    // CTAs and sums depend on its own probe count and not on the widest system in the batch
+    bt->Gpk.resize(bt->n_sys);
+    for (int k = 0; k < bt->n_sys; k++)
+        bt->Gpk[k] = m.Gp > 0 ? Gp : std::min(32, next_pow2((bt->Pk[k] + NP - 1) / NP));
     // shared-memory stage: largest tile over all systems
     int nk_max = 0;
     for (int k = 0; k < bt->n_sys; k++) {
         const int* rp = bt->h_row_ptr.data() + bt->row_base[k];
         std::vector<int> local(rp, rp + bt->n_b[k] + 1);
         for (auto& v : local) v -= rp[0];
-        nk_max = std::max(nk_max, fk::max_tile_blocks(local.data(), bt->n_b[k], Gp));
+        nk_max = std::max(nk_max, fk::max_tile_blocks(local.data(), bt->n_b[k], bt->Gpk[k]));
     }
     const size_t per_blk = (size_t)bt->b * bt->b * bt->esize() + sizeof(unsigned);
     const int stage = m.stage >= 0 ? m.stage : (bt->prec == fk::kF32 ? 0 : 1);
@@ -224,13 +227,14 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     const long long cap = (long long)occ * bt->num_sms;
     bt->sysd.resize(bt->n_sys);
     bool all_whole = true;
-    for (int k = 0; k < bt->n_sys; k++) all_whole = all_whole && bt->Pk[k] % (Gp * NP) == 0;
-    bt->P_launch = all_whole || Gp * NP == 1 ? P : Gp * NP + 1;   // (the kernels read each system's own P)
+    for (int k = 0; k < bt->n_sys; k++) all_whole = all_whole && bt->Pk[k] % (bt->Gpk[k] * NP) == 0;
+    // (the kernels read each system's own P and Gp; the launch's P only selects the unmasked instances)
+    bt->P_launch = all_whole || Gp * NP == 1 ? Gp * NP : Gp * NP + 1;
     std::vector<int> cta_sys, order(bt->n_sys);
     std::vector<long long> tiles(bt->n_sys);
     std::vector<int> ctas(bt->n_sys);
     for (int k = 0; k < bt->n_sys; k++) {
-        tiles[k] = ((long long)bt->n_b[k] * Gp + fk::kThreads - 1) / fk::kThreads;
+        tiles[k] = ((long long)bt->n_b[k] * bt->Gpk[k] + fk::kThreads - 1) / fk::kThreads;
         ctas[k] = (int)std::max<long long>(1, std::min(tiles[k], cap));
         order[k] = k;
     }
@@ -242,7 +246,7 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     });
     int base = 0;
     for (int k : order) {
-        bt->sysd[k] = SysDesc{bt->row_base[k], bt->n_b[k], base, ctas[k], bt->Pk[k]};
+        bt->sysd[k] = SysDesc{bt->row_base[k], bt->n_b[k], base, ctas[k], bt->Pk[k], bt->Gpk[k]};
         cta_sys.insert(cta_sys.end(), ctas[k], k);
         base += ctas[k];
     }
@@ -251,7 +255,7 @@ int batch_configure(fk_batch* bt, const Mapping& m) {
     BT_TRY(bt->d_cta_sys.ensure(sizeof(int) * base), "alloc CTA table");
     BT_TRY(cudaMemcpy(bt->d_sys.p, bt->sysd.data(), sizeof(SysDesc) * bt->n_sys, cudaMemcpyHostToDevice), "upload system table");
     BT_TRY(cudaMemcpy(bt->d_cta_sys.p, cta_sys.data(), sizeof(int) * base, cudaMemcpyHostToDevice), "upload CTA table");
-    bt->cur = Mapping{Gp, NP, m.cap_per_sm, stage};
+    bt->cur = m;   // as requested (automatic fields stay automatic when the tables are rebuilt)
     bt->configured = true;
     return FK_OK;
 }
@@ -755,12 +759,7 @@ int fk_batch_set_option(fk_batch* bt, int option, int value) {
         default: return bt->fail(FK_ERR_ARG, "unknown option %d", option);
     }
     if (!bt->n_sys) return FK_OK;
-    Mapping m = bt->opt;
-    if (m.NP > 0 && m.Gp == 0) {
-        m.Gp = bt->P <= 32 * m.NP ? next_pow2((bt->P + m.NP - 1) / m.NP) : 32;
-        if (m.Gp > 32) m.Gp = 32;
-    }
-    return batch_configure(bt, m);
+    return batch_configure(bt, bt->opt);   // (lanes per row follow the packets per lane, per system)
 }
 
 int fk_batch_get_option(const fk_batch* bt, int option, int* value) {
@@ -780,14 +779,11 @@ int fk_batch_autotune(fk_batch* bt, int trial_steps, int* lanes, int* np_out, in
     if (!bt->configured) return bt->fail(FK_ERR_STATE, "batch_autotune: commit the batch first");
     if (trial_steps < 1) trial_steps = 8;
     cudaSetDevice(bt->device);
-    // candidate mappings: packets per lane (lanes per row follow), CTA caps, H staging
+    // candidate mappings: packets per lane (each system's lanes per row follow), CTA caps, H staging
     std::vector<Mapping> cands;
-    for (int np : {1, 2, 4}) {
-        int gp = next_pow2((bt->P + np - 1) / np);
-        if (gp > 32) gp = 32;
+    for (int np : {1, 2, 4})
         for (int cap : {0, 1, 2, 3, 4, 6})
-            for (int st : {1, 0}) cands.push_back(Mapping{gp, np, cap, st});
-    }
+            for (int st : {1, 0}) cands.push_back(Mapping{0, np, cap, st});
     const int M = 2 * (trial_steps + 1);
     if (!bt->t0) cudaEventCreate(&bt->t0);
     if (!bt->t1) cudaEventCreate(&bt->t1);
@@ -819,7 +815,7 @@ int fk_batch_autotune(fk_batch* bt, int trial_steps, int* lanes, int* np_out, in
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tuned[std::make_tuple(bt->prec, bt->cplx, bt->b, bt->P, (long long)bt->total_rows, bt->n_sys)] = best;
     }
-    if (lanes) *lanes = best.Gp;
+    if (lanes) *lanes = bt->Gp;   // (the widest system's; narrower ones take fewer)
     if (np_out) *np_out = best.NP;
     if (cap_out) *cap_out = best.cap_per_sm;
     if (stage_out) *stage_out = best.stage;

@@ -37,6 +37,7 @@ struct SysDesc {
     int ctas;        // CTAs assigned to this system
     int P;           // packets per row of this system's probe columns (0: the launch's P); systems of a
                      // batch may have different probe counts and share the row stride of the widest
+    int Gp;          // lanes per block row of this system (0: the launch's Gp)
 };
 
 struct StepArgs {
@@ -268,7 +269,7 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step(Ste
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
+    const int Gp = sd.Gp > 0 ? sd.Gp : a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* x = reinterpret_cast<const E*>(a.x);
@@ -510,7 +511,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_st
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
+    const int Gp = sd.Gp > 0 ? sd.Gp : a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);
@@ -797,7 +798,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointSplitCtas<S, B, NP>) k_adjoi
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
+    const int Gp = sd.Gp > 0 ? sd.Gp : a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);
@@ -956,7 +957,7 @@ __global__ void __launch_bounds__(kThreads, kOuterCtas<S, B, NP>) k_outer(OuterA
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
+    const int Gp = sd.Gp > 0 ? sd.Gp : a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);

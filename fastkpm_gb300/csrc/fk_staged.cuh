@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(kThreads, kStepCtas<S, B, NP>) k_cheb_step_pip
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
+    const int Gp = sd.Gp > 0 ? sd.Gp : a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* x = reinterpret_cast<const E*>(a.x);
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_pi
     const int sidx = a.cta_sys[blockIdx.x];
     const SysDesc sd = a.sys[sidx];
     const int lc = blockIdx.x - sd.cta_base;
-    const int Gp = a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
+    const int Gp = sd.Gp > 0 ? sd.Gp : a.Gp, P = sd.P > 0 ? sd.P : a.P, W = Gp * NP;
     const int nch = (P + W - 1) / W;
     const long long items = (long long)sd.n_b * Gp;
     const E* A = reinterpret_cast<const E*>(a.A);

@@ -9,13 +9,15 @@ running starts as soon as a slot and its memory are free. Probe and recursion
 state stay on the device for the whole solve (moments -> autodiff_matrix).
 
 Small autodiff solves share launches: a request whose footprint is at most
-`pack_bytes` has a pack key (value kind, block size, probe count, order,
-precision); when one is admitted while queued requests have the same key, up to
+`pack_bytes` has a pack key (value kind, block size, order, precision, and the
+packets per lane a batch gives its probe count -- probe counts 8 to 128 of FP32
+complex blocks all take two); when one is admitted while queued requests have the same key, up to
 `pack_max` of them are admitted together as one pack, solved by a Batch: every
 Chebyshev step of every system in the pack is one launch, and the reverse
 recursion and D of all of them too. A request admitted with no partner runs on
 an engine of its own (creating a batch for one request costs more than it
-saves). Every kernel's per-system reduction order depends only on that system,
+saves). Every kernel's per-system reduction order depends only on that system
+(its lanes per row follow its own probe count; the packets per lane are the key's),
 so a request's result in a pack of any composition is bit-identical to its
 result as a pack of one, and on its own engine the same as alone; the two paths
 agree within the FP32 tolerance. Solves whose algorithmic traffic is below `urgent_bytes` run on
@@ -38,6 +40,18 @@ from .engine import Batch, Engine
 
 # FK_OPT_CTA_WAVES of the slots' engines: grids of 8 resident-CTA waves (see Server)
 DEFAULT_CTA_WAVES = 8
+
+
+def batch_packets_per_lane(s, precision, complex_values):
+    """The packets per lane a batch picks for a system of s probe columns when it is the widest
+    (fk_batch.cu batch_configure): packets of 16 bytes per row, two per lane up to 32 packets, else
+    enough for 32 lanes (1, 2 or 4)."""
+    elem = {"fp32": 4, "ds": 8, "fp64": 8}[precision] * (2 if complex_values else 1)
+    P = -(-s * elem // 16)
+    if P <= 32:
+        return 2 if P >= 2 else 1
+    np_ = -(-P // 32)
+    return 1 if np_ <= 1 else 2 if np_ <= 2 else 4
 
 
 class Request:
@@ -87,11 +101,13 @@ class Request:
 
     def pack_key(self, max_bytes):
         """Requests with equal keys can share one batched launch per Chebyshev step: autodiff solves
-        of the same value kind, block size, probe count, order and precision, each of footprint at
-        most max_bytes. None: the request runs on an engine of its own."""
+        of the same value kind, block size, order and precision whose probe counts give the batch
+        the same packets per lane (batch_packets_per_lane), each of footprint at most max_bytes.
+        None: the request runs on an engine of its own."""
         if self.kind != "autodiff" or self.footprint() > max_bytes:
             return None
-        return (self.complex_values, self.H.b_len, self.s, self.M, self.precision)
+        return (self.complex_values, self.H.b_len, batch_packets_per_lane(self.s, self.precision, self.complex_values),
+                self.M, self.precision)
 
     def dense_R(self):
         """The probe block as a column-major n x s array (expanded from its nonzeros if needed)."""

@@ -257,4 +257,11 @@ def test_batch_mixed_probe_counts(gpu, prec, tol, dtol):
         assert np.max(np.abs(mu[k] - ref)) / ref[0] <= tol, (k, Ss[k])
         D_ref = o.autodiff_matrix(cs[k], H.pattern_like(False))
         assert rel_err(Ds[k].val, D_ref) <= dtol, (k, Ss[k])
+        # a system's lanes per row follow its own probe count, so alone in a batch it gives the same
+        # bits (the packets per lane, two, are the same for every probe count here)
+        one = fk.Batch(False, prec)
+        one.add(H, es, R)
+        one.commit()
+        assert np.array_equal(one.moments(M)[0], mu[k]), (k, Ss[k])
+        assert np.array_equal(one.autodiff_matrix(M, cs[k:k + 1])[0].val, Ds[k].val), (k, Ss[k])
 

@@ -68,11 +68,22 @@ def test_pack_group_takes_same_key_requests_in_order():
 
     def req(H, es, S=8, M=10, kind="autodiff"):
         return Request(H, es, np.ones((H.n_rows, S)), M, np.zeros(M), kind, "fp32")
-    a, b, c, d, e = req(H8, es8), req(H6, es6), req(H8, es8, S=16), req(H8, es8, M=12), req(H6, es6, kind="stoch")
-    f, g = req(H6, es6), req(H8, es8)
-    queue = [a, b, c, d, e, f, g]
-    assert pack_group(a, queue, 1 << 30, 16) == [a, b, f, g]        # same kind, b, S, M, precision
+    a, b, c, d, e = req(H8, es8), req(H6, es6), req(H8, es8, S=512), req(H8, es8, M=12), req(H6, es6, kind="stoch")
+    f, g, h = req(H6, es6), req(H8, es8), req(H6, es6, S=24)
+    queue = [a, b, c, d, e, f, g, h]
+    # same kind, b, M, precision and packets per lane: probe counts 8 and 24 (2 and 6 packets) share
+    # packs, 512 (128 packets: four per lane) does not
+    assert pack_group(a, queue, 1 << 30, 16) == [a, b, f, g, h]
     assert pack_group(a, queue, 1 << 30, 3) == [a, b, f]            # at most pack_max
     assert pack_group(e, queue, 1 << 30, 16) == [e]                 # stoch solves are not packed
     assert pack_group(a, queue, a.footprint() - 1, 16) == [a]       # above the footprint bound: alone
     assert a.pack_key(1 << 30) != c.pack_key(1 << 30) != d.pack_key(1 << 30)
+    assert a.pack_key(1 << 30) == h.pack_key(1 << 30)
+
+
+def test_batch_packets_per_lane_rule():
+    from fastkpm_gb300.serve import batch_packets_per_lane as np_of
+    # FP32 complex (8-byte elements, 2 per packet): S = 8..128 -> 4..64 packets -> two per lane
+    assert {np_of(s, "fp32", True) for s in (8, 32, 64, 128)} == {2}
+    assert np_of(256, "fp32", True) == 4 and np_of(2, "fp32", False) == 1
+    assert np_of(256, "ds", True) == 4 and np_of(64, "fp64", False) == 2
