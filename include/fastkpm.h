@@ -51,7 +51,7 @@ namespace fkpm {
     typedef std::complex<float>  cx_float;
     typedef std::complex<double> cx_double;
 
-    // complex conjugation that preserves real values
+    // conj() for every element type: the identity on float and double, std::conj on complex
     inline float     conj(float x)     { return x; }
     inline double    conj(double x)    { return x; }
     inline cx_float  conj(cx_float x)  { return std::conj(x); }
@@ -85,7 +85,7 @@ namespace fkpm {
 
     // -- spmat ------------------------------------------------------------------
 
-    // Blocks of matrix elements in unsorted order
+    // Coordinate list of b x b blocks (row, column, b*b values each), any order; build() sorts it
     template <typename T>
     class SpMatElems {
     public:
@@ -137,7 +137,7 @@ namespace fkpm {
 
     // -- KPM host math ------------------------------------------------------------
 
-    // Scale eigenvalues within range (-1, +1)
+    // Affine map of the spectrum [lo, hi] onto [-1, +1] and back
     class EnergyScale {
     public:
         double lo, hi;
@@ -194,10 +194,10 @@ namespace fkpm {
         virtual void set_R_correlated(Vec<int> const& groups, RNG& rng, int j_start, int j_end);
         virtual void set_R_correlated(Vec<int> const& groups, RNG& rng);
 
-        // Transfer R matrix to device
+        // Upload the host probe block R to the engine's device copy; every set_R_* calls it
         virtual void transfer_R() {}
 
-        // Set Hamiltonian and energy scale
+        // Upload H, scaled to Hs = (H - avg) / mag by the given energy scale
         virtual void set_H(SpMatBsr<T> const& H, EnergyScale const& es) = 0;
         void set_H(SpMatBsr<T> const& H) { set_H(H, energy_scale(H, 0.01)); }
 
