@@ -738,6 +738,28 @@ template <int DOFF, int SOFF>
 __device__ __forceinline__ void cp_async16_at(unsigned dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0+%2], [%1+%3], 16;" ::"r"(dst), "l"(src), "n"(DOFF), "n"(SOFF) : "memory");
 }
+// An L2 policy that makes the lines it tags the first to be evicted. The own rows of a
+// reverse step are read once and overwritten in place (a stream); tagging them keeps L2 for
+// the gathered rows, which every neighbouring row reads again: on a cubic lattice with the
+// site index running through planes, a row is gathered again two planes later.
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+// cp_async16_at with an L2 cache policy
+template <int DOFF, int SOFF>
+__device__ __forceinline__ void cp_async16_at_pol(unsigned dst, const void* src, unsigned long long pol) {
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0+%2], [%1+%3], 16, %4;" ::"r"(dst), "l"(src), "n"(DOFF),
+                 "n"(SOFF), "l"(pol)
+                 : "memory");
+}
+// 16-byte store with an L2 cache policy
+__device__ __forceinline__ void st16_pol(uint4* p, uint4 v, unsigned long long pol) {
+    asm volatile("st.global.L2::cache_hint.v4.b32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w), "l"(pol)
+                 : "memory");
+}
 // 16-byte cp.async issued only where `on` holds: a predicated instruction, no branch
 __device__ __forceinline__ void cp_async16_if(unsigned dst, const void* src, bool on) {
     asm volatile(
@@ -807,6 +829,7 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
     const typename S::Coef cAn = S::coef(a.coef[sidx * a.cstride + 2]);
     const float2 dscale_ds = ds_from_double(a.dscale);   // a.Dacc is never null here (fused epilogue only)
     const Owner own = transposed_owner<B * B>(G, lane);
+    const unsigned long long pol_stream = l2_evict_first();   // alpha_{m+1}, beta_{m+2}: read once, overwritten
 
     for (long long t0 = (long long)lc * kThreads; t0 < items; t0 += (long long)sd.ctas * kThreads) {
         const long long t = t0 + threadIdx.x;
@@ -844,23 +867,29 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
         auto issue = [&](int ic, int ir, int sl) {
             const unsigned coff = (unsigned)(ic * W + lane) * 16u;
             const unsigned sdst = s_mine + (unsigned)sl * kSlotStride;   // this thread's part of slot sl
-            // the B x NP packets of vector V (slot part) from the rows b r0 + (r ^ sw) of `base`
+            // the B x NP packets of vector V (slot part) from the rows b r0 + (r ^ sw) of `base`;
+            // tag V + 2: the rows are a stream (read once here, overwritten by this warp), copied
+            // with the evict-first L2 policy
             auto rows = [&](auto vt, const void* base, unsigned r0) {
-                constexpr int V = decltype(vt)::value;
+                constexpr int V = decltype(vt)::value & 1;
+                constexpr bool kStream = decltype(vt)::value >= 2;
                 static_for<0, B>([&](auto rt) {
                     constexpr int R = decltype(rt)::value;
                     const uint4* src = row_at(static_cast<const char*>(base) + coff, (unsigned)(B * r0 + (R ^ sw)), rb);
                     static_for<0, NP>([&](auto qt) {
                         constexpr int Q = decltype(qt)::value;
-                        cp_async16_at<V * kVecStride + R * kRowStride + Q * kQStride, Q * G * 16>(sdst, src);
+                        if constexpr (kStream)
+                            cp_async16_at_pol<V * kVecStride + R * kRowStride + Q * kQStride, Q * G * 16>(sdst, src, pol_stream);
+                        else
+                            cp_async16_at<V * kVecStride + R * kRowStride + Q * kQStride, Q * G * 16>(sdst, src);
                     });
                 });
             };
             if (ir == 0) {                 // A: alpha_m own rows
                 rows(BufTag<0>(), a.A, (unsigned)i);
-            } else if (ir == per - 1) {    // O: alpha_{m+1}, beta_{m+2} own rows
-                rows(BufTag<0>(), a.Ap, (unsigned)i);
-                rows(BufTag<1>(), a.Bp, (unsigned)i);
+            } else if (ir == per - 1) {    // O: alpha_{m+1}, beta_{m+2} own rows (streams)
+                rows(BufTag<2>(), a.Ap, (unsigned)i);
+                rows(BufTag<3>(), a.Bp, (unsigned)i);
             } else {                       // K: the block at unit position ir - 1 (identity-first order in hsum rows)
                 const int kk = hsum ? (int)__shfl_sync(0xffffffffu, ord, ir - 1) : ir - 1;
                 const int k = kb + kk;
@@ -1128,8 +1157,8 @@ __global__ void __launch_bounds__(kThreads, kAdjointCtas<S, B, NP>) k_adjoint_wa
                         Packet<E, EPP> pa, pb;
 #pragma unroll
                         for (int e = 0; e < EPP; e++) { pa.e[e] = an[q * EPP + e]; pb.e[e] = bn[q * EPP + e]; }
-                        rap[q * G] = pa.u;
-                        rbp[q * G] = pb.u;
+                        st16_pol(rap + q * G, pa.u, pol_stream);
+                        st16_pol(rbp + q * G, pb.u, pol_stream);
                     }
                 }
             }
