@@ -225,13 +225,18 @@ def step_flops_per_launch(H, S):
     return float(hop * 8 + gen * 32 + H.n_rows * 2 * 12) * S
 
 
-# DRAM bytes and warp instructions per row of one fused adjoint launch, from ncu captures on the
-# cubic L=32 case (65,536 rows; summarised under profiles/): traffic grows in proportion to the
-# rows, so the L=64 launch's traffic is these times N. Keys: (precision, FP64 accumulators). An
-# engine form without a capture of its current kernel reports null.
-ADJ_TRAFFIC_PER_ROW = {("fp64", 1): (1.857997e9 + 0.721861e9) / 65536,
-                       ("fp32", 1): (0.578174e9 + 0.250220e9) / 65536,
-                       ("ds", 0): (1.709504e9 + 0.530700e9) / 65536}
+# DRAM bytes (read + write) of one fused reverse step, all its launches, at the cubic L=64, S=256
+# workload (524,288 rows), from ncu captures summarised under profiles/. Float-float runs the step
+# as four column-sweep launches (FK_OPT_ADJ_SWEEP): their sum. Keys: (precision, FP64
+# accumulators). Other workloads, and engine forms without a capture of their kernels, report null.
+# (Traffic does not grow in proportion to the rows: at L=32 the rows gathered a lattice plane
+# later still hit L2, at L=64 they do not.)
+ADJ_TRAFFIC_L64 = {("fp64", 1): 18615305216 + 6046837248,
+                   ("fp32", 1): 8037847296 + 2240859904,
+                   ("ds", 0): 14741449984 + 4654563072}
+ADJ_TRAFFIC_ROWS = 524288
+# warp instructions per row of the float-float reverse step (cubic L=32 capture, one launch over
+# whole rows; the four sweeps add the per-row setup three more times)
 ADJ_WARP_INST_PER_ROW = {("ds", 0): 914440192 / 65536}
 ISSUE_PEAK_WARP_INST_PER_CYCLE = 152 * 4
 
@@ -367,7 +372,8 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=Non
     ach_adj = bytes_adj / (avg_adj_ms * 1e-3) / 1e9
     ach_step = bytes_step / (avg_step_ms * 1e-3) / 1e9
     key = (prec, acc64)
-    traffic = ADJ_TRAFFIC_PER_ROW[key] * N if (key in ADJ_TRAFFIC_PER_ROW and S == 256 and fused) else None
+    traffic = (ADJ_TRAFFIC_L64[key] if (key in ADJ_TRAFFIC_L64 and N == ADJ_TRAFFIC_ROWS and S == 256 and fused)
+               else None)
     clocks = clk.summary()
     out = dict(prec=prec, value=replica_value(per_solve, steps, ws, ms_max), ms=ms_max, steps=steps, warmup=warmup,
                clocks=clocks, launches=sum(v[0] for v in prof.values()), mu=mu, D=D.val.copy(), fused=fused,
@@ -377,7 +383,7 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=Non
                        "traffic": traffic,
                        "kernel": "fused adjoint step (both recursions%s)" % (
                            " + D epilogue" if fused else "; D outer product apart"),
-                       "traffic_source": ("ncu DRAM bytes of the L=32 launch scaled by rows (profiles/)"
+                       "traffic_source": ("ncu DRAM bytes of one reverse step of this workload (profiles/)"
                                           if traffic else None),
                        "peak_source": peak_kind, "bytes_per_launch": bytes_adj, "avg_launch_ms": avg_adj_ms,
                        "launches": n_adj}

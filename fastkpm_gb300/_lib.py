@@ -23,6 +23,7 @@ FK_OPT_PIPE = 12
 FK_OPT_ACC64 = 13
 FK_OPT_CTA_WAVES = 14
 FK_OPT_WARP_ROWS = 15
+FK_OPT_ADJ_SWEEP = 16
 
 PRECISIONS = {"fp64": FK_PREC_FP64, "fp32": FK_PREC_FP32, "ds": FK_PREC_DS}
 

@@ -92,6 +92,8 @@ struct fk_engine {
     int cplx = 0;
     int prec = fk::kF64;
     int num_sms = 1;
+    long long l2_bytes = 0;   // the device's L2 cache
+    long long gather_dist = 0;   // 90th percentile of H's block-column distances |j - i| (set_H)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int opt_priority = 0;   // CUDA priority of the engine's own stream
@@ -142,6 +144,7 @@ struct fk_engine {
     int opt_acc64 = 1;         // FK_OPT_ACC64 (FP32 engines): 1 FP64 moment sums and D accumulator, 0 float-float
     int opt_waves = 1;         // FK_OPT_CTA_WAVES: grids of this many times the resident CTAs (shorter-lived CTAs)
     int opt_warp = 1;          // FK_OPT_WARP_ROWS: warp-per-row kernels where a warp serves each block row
+    int opt_sweep = 2;         // FK_OPT_ADJ_SWEEP: 0 one launch, 1 a launch per column chunk, 2 (default) by size
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     DevBuf d_post;   // post-processing: [mu M][gamma Mq][energies Mq][result 4][coefficients M]
     int post_M = 0, post_Mq = 0;
@@ -444,6 +447,30 @@ bool use_adjoint_split(const fk_engine* e, int NP) {
     return e->b == 1 && e->prec != fk::kF64 && !light;
 }
 
+// FK_OPT_ADJ_SWEEP 2 (default): float-float engines sweep the columns when a launch over whole
+// rows would put more through L2 between a row's first and last gathers than half of L2 holds
+// (FP32 engines run one launch: see configure): six vectors
+// (alpha_m, beta_{m+1} gathered; alpha_{m+1}, beta_{m+2} read and written) per block row, over
+// twice the block-column distance |j - i| that 90% of H's blocks keep within (periodic lattices:
+// the few wrap-around bonds do not count; cubic: L^2 sites).
+bool use_sweeps(const fk_engine* e, int NP) {
+    if (e->P % (32 * NP) != 0 || e->P / (32 * NP) < 2) return false;
+    if (e->opt_sweep != 2) return e->opt_sweep != 0;
+    if (e->prec != fk::kDS) return false;
+    const double window = 2.0 * (double)e->gather_dist * e->b * 6.0 * (double)e->P * 16.0;
+    return e->l2_bytes > 0 && window > 0.5 * (double)e->l2_bytes;
+}
+// the block-column distance |j - i| that 90% of the blocks keep within
+long long gather_distance(const std::vector<int>& row_ptr, const std::vector<int>& col, int n_b) {
+    if (col.empty()) return 0;
+    std::vector<int> d(col.size());
+    for (int i = 0; i < n_b; i++)
+        for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++) d[k] = std::abs(col[k] - i);
+    const size_t q = (d.size() * 9) / 10;
+    std::nth_element(d.begin(), d.begin() + q, d.end());
+    return d[q];
+}
+
 // FK_OPT_PIPE: step / adjoint kernels with double-buffered gathers (FP32, float-float). FP32: the
 // step kernel for b=2 (cubic L=64, S=256: 0.67 vs 0.85 ms; 10^6-site cubic S=128: 1.34 vs
 // 1.59; b=1 S=128 stays plain: 0.301 vs 0.293); the adjoint kernel except for light rows
@@ -514,6 +541,18 @@ int configure(fk_engine* e) {
         c.warp = kind == fk::kAdjoint && c.pipe && e->opt_warp && e->prec != fk::kF64 && Gp == 32 &&
                  P % (32 * NP) == 0 && fk::max_row_blocks(e->h_row_ptr.data(), e->n_b) <= 32;
         if (c.warp) c.stage_cap = 0;   // its H entries travel with the units: no per-tile stage
+        // column sweeps: the warp-per-row reverse step launched once per column chunk, so that the
+        // rows gathered again a bandwidth later are still in L2 (each launch puts a chunk's width
+        // of six vectors per row through L2 instead of the whole row's). Cubic L=64, S=256, DRAM
+        // bytes per reverse step: float-float 26.2 GB in one launch (1.98x the algorithmic 13.2),
+        // 19.4 GB in four (7.98 -> 7.65 ms); FP32 10.3 GB in one (1.52x 6.7), 8.4 GB in two, but
+        // 1.620 -> 1.663 ms: a launch over single-chunk rows starts and drains the copy ring once
+        // per row and chunk, and FP32 already drew 0.93 of the DRAM peak. D's entries are read and
+        // written once per launch.
+        if (c.warp && use_sweeps(e, NP)) {
+            c.W = 32 * NP;
+            c.slices = P / c.W;
+        }
         // FP64 b=2 complex: the warp-per-row step (k_adjoint_step_warp), fewer FP64-pipe additions
         // in the D reduction
         if (kind == fk::kAdjoint && !c.pipe && !c.split && e->opt_warp && e->prec == fk::kF64 && e->cplx &&
@@ -607,6 +646,7 @@ int run_step(fk_engine* e, const void* x, const void* z, void* y, bool two, bool
 int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp, const double* coef_dev, double* Dacc) {
     const KCfg& c = e->cfg[fk::kAdjoint];
     const size_t es = e->esize();
+    ProfScope ps(e, fk::kAdjoint);   // one reverse step, all its column sweeps
     for (int sl = 0; sl < c.slices; sl++) {
         const long long off = (long long)sl * c.W * e->epp();
         fk::AdjArgs a;
@@ -631,7 +671,6 @@ int run_adjoint(fk_engine* e, const void* A, void* Ap, const void* Bv, void* Bp,
         a.pipe = c.pipe ? 1 : 0;
         a.warp = c.warp ? 1 : 0;
         a.row_hsum = (c.warp && e->prec == fk::kDS) ? e->d_row_hsum.as<unsigned char>() : nullptr;
-        ProfScope ps(e, fk::kAdjoint);
         FK_TRY(prec_launch_adjoint(e, c.NP, a, fk::Launch{c.ctas, c.smem, e->stream}), "adjoint kernel launch");
     }
     return FK_OK;
@@ -1422,6 +1461,11 @@ int fk_engine_create(int device, int kind, int precision, fk_engine** out) {
     e->cplx = kind;
     e->prec = precision;
     cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device);
+    {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device);
+        e->l2_bytes = l2;
+    }
     if (cudaDeviceGetAttribute(&e->pageable_access, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
         cudaGetLastError();
         e->pageable_access = 0;
@@ -1541,6 +1585,11 @@ int fk_engine_set_option(fk_engine* e, int option, int value) {
             e->opt_warp = value;
             drop_graphs(e);
             return configure(e);
+        case FK_OPT_ADJ_SWEEP:
+            if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "ADJ_SWEEP must be 0, 1 or 2");
+            e->opt_sweep = value;
+            drop_graphs(e);
+            return configure(e);
         case FK_OPT_ADJ_SPLIT:
             if (value < 0 || value > 2) return e->fail(FK_ERR_ARG, "ADJ_SPLIT must be 0, 1 or 2");
             e->opt_adj_split = value;
@@ -1590,6 +1639,7 @@ int fk_engine_get_option(const fk_engine* e, int option, int* value) {
         case FK_OPT_ACC64: *value = e->prec == fk::kF64 ? 1 : e->prec == fk::kF32 ? e->opt_acc64 : 0; return FK_OK;
         case FK_OPT_CTA_WAVES: *value = e->opt_waves; return FK_OK;
         case FK_OPT_WARP_ROWS: *value = e->cfg[fk::kAdjoint].valid ? (int)e->cfg[fk::kAdjoint].warp : e->opt_warp; return FK_OK;
+        case FK_OPT_ADJ_SWEEP: *value = e->cfg[fk::kAdjoint].valid ? (int)(e->cfg[fk::kAdjoint].slices > 1) : e->opt_sweep; return FK_OK;
         case FK_OPT_TMA: *value = e->cfg[fk::kStep].valid ? (e->cfg[fk::kStep].staged ? e->opt_tma : 0) : e->opt_tma; return FK_OK;
         default: return FK_ERR_ARG;
     }
@@ -1623,6 +1673,7 @@ int fk_engine_set_H(fk_engine* e, int n_b, int b, int nnzb, const int* row_ptr, 
     e->es_hi = es_hi;
     e->h_row_ptr.swap(ph.row_ptr);
     e->h_col.swap(ph.col);
+    e->gather_dist = gather_distance(e->h_row_ptr, e->h_col, n_b);
     e->mom_M = 0;
     e->mom_a0 = e->mom_a1 = -2;
     e->d_nb = -1;   // D pattern comparison against H must be redone

@@ -112,6 +112,13 @@ int  fk_engine_synchronize(fk_engine* e);
                                 * ring, compile-time offsets) and the FP64 b=2 complex one its warp-per-row form (fewer FP64
                                 * additions in the D reduction); 0 the general kernels. Results agree to the
                                 * last bits of rounding                                               */
+#define FK_OPT_ADJ_SWEEP  16   /* the warp-per-row FP32 / float-float reverse step: 1 one launch per column chunk
+                                * (D's entries read and written per launch, gathered rows kept in L2 a whole
+                                * lattice plane later), 0 one launch over whole rows, 2 (default) float-float
+                                * engines sweep when the rows moved between a row's first and last gathers
+                                * exceed half of L2 (FP32 engines: one launch, faster at cubic L=64).
+                                * Same results either way (each D entry adds its chunks in the same order);
+                                * reads back whether the configured reverse step sweeps              */
 int  fk_engine_set_option(fk_engine* e, int option, int value);
 int  fk_engine_get_option(const fk_engine* e, int option, int* value);
 

@@ -571,6 +571,51 @@ def test_warp_row_adjoint_against_general(gpu, prec, opts):
         eng.close()
 
 
+@pytest.mark.parametrize("prec,opts", [("fp32", {L.FK_OPT_ACC64: 1}), ("fp32", {L.FK_OPT_ACC64: 0}), ("ds", {})])
+def test_adjoint_column_sweeps_same_bits(gpu, prec, opts):
+    # FK_OPT_ADJ_SWEEP 1: the warp-per-row reverse step runs as one launch per column chunk (S=256
+    # complex columns: FP32 2 chunks, float-float 4). Every D entry adds its chunks in the same order
+    # as in one launch over whole rows, so D is the same to the bit; the moments come from the shared
+    # forward step. D against the oracle within the engine's tolerance.
+    H, es, _ = W.cubic_spin_lattice(16, -1.0, 1.0, seed=31)
+    R = fk.probe_uncorrelated(H.n_rows * H.b_len, 256, fk.RNG(31), complex_values=True)
+    M = 24
+    c = W.fermi_coefficients(M, es, "fermi_energy")
+    swept = run_pair(H, es, R, True, prec, M, c, "autodiff", {**opts, L.FK_OPT_ADJ_SWEEP: 1})
+    whole = run_pair(H, es, R, True, prec, M, c, "autodiff", {**opts, L.FK_OPT_ADJ_SWEEP: 0})
+    assert np.array_equal(swept[0], whole[0])
+    assert np.array_equal(swept[2], whole[2])
+    assert mu_err(swept[0], swept[1]) <= TOL_MU[prec]
+    assert rel_err(swept[2], swept[3]) <= TOL_D[prec]
+    eng = fk.Engine(True, prec)
+    eng.set_H(H, es)
+    eng.set_R(R)
+    assert eng.get_option(L.FK_OPT_ADJ_SWEEP) == 0   # 16^3: two planes of rows fit L2 many times over
+    eng.set_option(L.FK_OPT_ADJ_SWEEP, 1)
+    assert eng.get_option(L.FK_OPT_ADJ_SWEEP) == 1
+    eng.close()
+
+
+def test_adjoint_column_sweeps_by_size(gpu):
+    # Float-float engines sweep by default when the six vectors' rows moved between a row's first
+    # and last gathers (twice the block-column distance 90% of H's blocks keep within: L^2 sites on
+    # the periodic cubic lattice) exceed half of L2: cubic L=32 with S=256 complex columns moves
+    # 2 x 1024 sites x 2 rows x 6 x 4 KB = 101 MB (sweeps on a GPU whose L2 is below 201 MB).
+    # FP32 engines run one launch by default.
+    import torch
+    l2 = getattr(torch.cuda.get_device_properties(0), "L2_cache_size", None)
+    if not l2:
+        pytest.skip("torch does not report the L2 size")
+    H, es, _ = W.cubic_spin_lattice(32, -1.0, 1.0, seed=37)
+    R = fk.probe_uncorrelated(H.n_rows * H.b_len, 256, fk.RNG(37), complex_values=True)
+    for prec, want in [("ds", 1 if 2 * 1024 * 2 * 6 * 256 * 16 > l2 / 2 else 0), ("fp32", 0)]:
+        eng = fk.Engine(True, prec)
+        eng.set_H(H, es)
+        eng.set_R(R)
+        assert eng.get_option(L.FK_OPT_ADJ_SWEEP) == want
+        eng.close()
+
+
 @pytest.mark.parametrize("prec", ["ds", "fp32"])
 def test_warp_row_adjoint_nonuniform_hopping(gpu, prec):
     # Rows whose identity (hopping) blocks do not all share one value: every third bond of the 16^3
