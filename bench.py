@@ -358,9 +358,14 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=Non
     eng.fetch_D(D)
     fused = eng.get_option(Lb.FK_OPT_FUSE_D) != 0
     acc64 = eng.get_option(Lb.FK_OPT_ACC64)
+    # kernel launches per reverse step: one, or one per column chunk when the engine sweeps
+    sweeps = 1
+    if eng.get_option(Lb.FK_OPT_ADJ_SWEEP):
+        packets = S * (8 if prec == "fp32" else 16) // 16
+        sweeps = max(1, packets // (32 * eng.get_option(Lb.FK_OPT_NP_ADJOINT)))
     eng.close()
 
-    n_adj, t_adj = prof[1]
+    n_adj, t_adj = prof[1]   # reverse steps (each `sweeps` kernel launches)
     n_step, t_step = prof[0]
     sv = 8 if prec == "fp32" else 16
     nnzb = H.n_blocks()
@@ -376,7 +381,7 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=Non
                else None)
     clocks = clk.summary()
     out = dict(prec=prec, value=replica_value(per_solve, steps, ws, ms_max), ms=ms_max, steps=steps, warmup=warmup,
-               clocks=clocks, launches=sum(v[0] for v in prof.values()), mu=mu, D=D.val.copy(), fused=fused,
+               clocks=clocks, launches=sum(v[0] for v in prof.values()) + (sweeps - 1) * n_adj, mu=mu, D=D.val.copy(), fused=fused,
                N=N, S=S, M=M, nnzb=nnzb, n_adj=n_adj, n_step=n_step, avg_adj_ms=avg_adj_ms, avg_step_ms=avg_step_ms,
                acc64=acc64)
     out["roofline"] = {"bound": "hbm", "achieved": ach_adj, "peak": peak, "unit": "GB/s", "frac": ach_adj / peak,
@@ -386,7 +391,7 @@ def run_leg(args, prec, steps, warmup, wl, ws, dist, dev, e2e_steps, options=Non
                        "traffic_source": ("ncu DRAM bytes of one reverse step of this workload (profiles/)"
                                           if traffic else None),
                        "peak_source": peak_kind, "bytes_per_launch": bytes_adj, "avg_launch_ms": avg_adj_ms,
-                       "launches": n_adj}
+                       "launches": n_adj, "kernel_launches_per_reverse_step": sweeps}
     out["roofline_step"] = {"bound": "hbm", "achieved": ach_step, "peak": peak, "unit": "GB/s",
                             "frac": ach_step / peak, "kernel": "Chebyshev step (moments)",
                             "bytes_per_launch": bytes_step, "avg_launch_ms": avg_step_ms, "launches": n_step}
